@@ -1,0 +1,105 @@
+"""ctypes binding of ``libephg.so`` (the C ABI declared in ``include/ephg.h``).
+
+The library is the only compute path: if it is missing, or no GPU is visible,
+calls raise instead of falling back to anything on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libephg.so")
+
+EPHG_OK = 0
+EPHG_ERR_ARG = 1
+EPHG_ERR_CUDA = 2
+EPHG_ERR_NEG_PHONON = 3
+EPHG_ERR_EMPTY_WINDOW = 4
+EPHG_ERR_EIG = 5
+EPHG_ERR_NOMEM = 6
+EPHG_ERR_TIMEOUT = 7
+EPHG_ERR_INDEX = 8
+
+PREC_FP64 = 0
+PREC_SPLIT_TF32 = 1
+DELTA_GAUSSIAN, DELTA_TRIANGLE, DELTA_TETRA = 0, 1, 2
+WANNSPACE_EL, WANNSPACE_PH = 0, 1
+
+c_i64p = ct.POINTER(ct.c_int64)
+c_dp = ct.POINTER(ct.c_double)
+
+# every symbol include/ephg.h declares
+EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count", "ephg_el_wann",
+           "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates"]
+
+
+class EphgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("ephg error %d: %s" % (code, msg))
+        self.code = code
+
+
+class WannierDesc(ct.Structure):
+    _fields_ = [("numwannbands", ct.c_int64), ("numbranches", ct.c_int64),
+                ("nwsk", ct.c_int64), ("nwsq", ct.c_int64), ("nwsg", ct.c_int64),
+                ("numatoms", ct.c_int64), ("coarse_qmesh", ct.c_int64 * 3),
+                ("lattvecs", c_dp), ("basis", c_dp), ("masses", c_dp),
+                ("rcells_k", c_i64p), ("rcells_q", c_i64p), ("rcells_g", c_i64p),
+                ("elwsdeg", c_i64p), ("phwsdeg", c_i64p), ("gwsdeg", c_i64p),
+                ("Hwann", c_dp), ("Dphwann", c_dp), ("gwann", c_dp)]
+
+
+class RateRequest(ct.Structure):
+    _fields_ = [("mesh", ct.c_int64 * 3), ("enref", ct.c_double), ("fsthick", ct.c_double),
+                ("chempot", ct.c_double), ("T", ct.c_double), ("delta_kind", ct.c_int64),
+                ("sigma", ct.c_double), ("precision", ct.c_int64)]
+
+
+class RateStats(ct.Structure):
+    _fields_ = [("nwv", ct.c_int64), ("nstates_inwindow", ct.c_int64), ("nstates", ct.c_int64),
+                ("vertices", ct.c_int64), ("pairs", ct.c_int64), ("kernel_launches", ct.c_int64),
+                ("ms_setup", ct.c_double), ("ms_stage_a", ct.c_double),
+                ("ms_stage_bc", ct.c_double), ("ms_total", ct.c_double),
+                ("stage_b_gflop", ct.c_double), ("stage_a_gflop", ct.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libephg.so is not built: run elphbolt_gb300.build.build() "
+                           "(there is no CPU fallback)")
+    L = ct.CDLL(path)
+    L.ephg_last_error.restype = ct.c_char_p
+    L.ephg_device_count.restype = ct.c_int
+    vp = ct.c_void_p
+    L.ephg_create.argtypes = [ct.POINTER(WannierDesc), ct.POINTER(vp)]
+    L.ephg_destroy.argtypes = [vp]
+    L.ephg_el_wann.argtypes = [vp, ct.c_int64, c_dp, c_dp, c_dp, c_dp, c_dp]
+    L.ephg_ph_wann.argtypes = [vp, ct.c_int64, c_dp, c_dp, c_dp, c_dp]
+    L.ephg_gkRp.argtypes = [vp, ct.c_int64, c_dp, c_dp]
+    L.ephg_gReq.argtypes = [vp, ct.c_int64, c_dp, c_dp]
+    L.ephg_g2.argtypes = [vp, ct.c_int64, ct.c_int64, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp,
+                          ct.c_int64, c_dp, c_i64p, c_dp]
+    L.ephg_kq_index.argtypes = [vp, c_i64p, ct.c_int64, c_i64p, ct.c_int64, c_i64p, c_i64p]
+    L.ephg_el_rates.argtypes = [vp, ct.POINTER(RateRequest), c_dp, c_i64p, ct.POINTER(RateStats),
+                                c_dp, c_dp, c_dp, ct.c_int64]
+    for name in EXPORTS:
+        getattr(L, name).restype = getattr(L, name).restype or ct.c_int
+    L.ephg_last_error.restype = ct.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != EPHG_OK:
+        raise EphgError(rc, load().ephg_last_error().decode(errors="replace"))

@@ -1,0 +1,827 @@
+// ephg_api.cu - the C ABI (include/ephg.h): handle, uploads and the
+// orchestration of the e-ph vertex path on one GPU and one CUDA stream.
+#include <cub/device/device_scan.cuh>
+#include <cub/device/device_select.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/ephg.h"
+#include "ephg_kernels.cuh"
+#include "ephg_tc.cuh"
+#include "ephg_ws.cuh"
+
+using namespace ephg;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(EPHG_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,                \
+                  cudaGetErrorString(e_));                                                \
+  } while (0)
+
+#define CKL()                                                                             \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(EPHG_ERR_CUDA, "%s:%d launch: %s", __FILE__, __LINE__,                   \
+                  cudaGetErrorString(e_));                                                \
+  } while (0)
+
+namespace {
+
+int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
+int lcm3(const int m[3]) {
+  int l = m[0];
+  l = l / gcd_i(l, m[1]) * m[1];
+  l = l / gcd_i(l, m[2]) * m[2];
+  return l;
+}
+
+// ws_wrapping_vectors (wannier.f90:532-582), q independent: evaluated once per
+// (R, atom pair) at create time instead of once per q.
+std::vector<int> ws_wrap(const double lvec[9], const double vl[3], double eps) {
+  int iv0[3];
+  double wl[3];
+  for (int i = 0; i < 3; ++i) {
+    iv0[i] = (int)std::trunc(vl[i]);
+    wl[i] = vl[i] - (double)iv0[i];
+  }
+  double d = 1.79769313486231570815e308;
+  auto norm = [&](int i, int j, int k) {
+    double v[3] = {wl[0] + i, wl[1] + j, wl[2] + k}, wc[3];
+    for (int r = 0; r < 3; ++r) wc[r] = lvec[r] * v[0] + lvec[r + 3] * v[1] + lvec[r + 6] * v[2];
+    return std::sqrt(wc[0] * wc[0] + wc[1] * wc[1] + wc[2] * wc[2]);
+  };
+  for (int k = -3; k <= 3; ++k)
+    for (int j = -3; j <= 3; ++j)
+      for (int i = -3; i <= 3; ++i) {
+        double nr = norm(i, j, k);
+        if (std::fabs(nr - d) < eps) {
+        } else if (nr < d) d = nr;
+      }
+  std::vector<int> out;
+  for (int k = -3; k <= 3; ++k)
+    for (int j = -3; j <= 3; ++j)
+      for (int i = -3; i <= 3; ++i)
+        if (std::fabs(norm(i, j, k) - d) < eps) {
+          out.push_back(i - iv0[0]);
+          out.push_back(j - iv0[1]);
+          out.push_back(k - iv0[2]);
+        }
+  return out;
+}
+
+}  // namespace
+
+struct ephg_handle {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int nw = 0, nb = 0, nwsk = 0, nwsq = 0, nwsg = 0, nat = 0;
+  int cq[3] = {0, 0, 0};
+  double lattvecs[9];
+  std::vector<double> masses_h;
+  int64_t Nn = 0;   // nw*nw*nb*nwsg, the stage-A row length
+  // resident device data
+  int *Rk = nullptr, *Rq = nullptr, *Rg = nullptr;         // (n,3) int
+  double *degk = nullptr, *degq = nullptr, *degg = nullptr;
+  double2 *Hext = nullptr;   // [Re][4*nw*nw]: H, i rx H, i ry H, i rz H
+  double2 *graw = nullptr;   // epmatwp order (i,j,Re,s,Rp)
+  double2 *G64 = nullptr;    // stage-A matrix [Re][Nn]
+  double *masses = nullptr;
+  // phonon wrap terms
+  int *pair_off = nullptr, *ent_iuc = nullptr, *ent_woff = nullptr, *wrapR = nullptr;
+  double *ent_den = nullptr, *rcartq = nullptr;
+  double2 *D = nullptr;
+  PhTerms terms;
+  int *err = nullptr;        // device error word
+  Workspace ws;
+  tc::SplitOperands split;   // split-TF32 operand planes (lazy)
+  int64_t launches = 0;
+};
+
+static int read_err(ephg_handle *h, int *word) {
+  CK(cudaMemcpyAsync(word, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->st));
+  return EPHG_OK;
+}
+
+static int check_err(ephg_handle *h) {
+  int w = 0;
+  int rc = read_err(h, &w);
+  if (rc) return rc;
+  if (w & DERR_NEG_PHONON) return fail(EPHG_ERR_NEG_PHONON, "Large negative phonon energy found!");
+  if (w & DERR_EIG) return fail(EPHG_ERR_EIG, "Jacobi eigensolver did not converge");
+  if (w & DERR_INDEX) return fail(EPHG_ERR_INDEX, "device index check failed");
+  if (w & DERR_TIMEOUT) return fail(EPHG_ERR_TIMEOUT, "bounded device wait gave up");
+  return EPHG_OK;
+}
+
+// workspace failures carry their own message
+#define WSFAIL(rc) fail((rc), "%s", h->ws.msg.c_str())
+
+template <typename T>
+static int upload(T **dst, const T *src, size_t n, cudaStream_t st) {
+  CK(cudaMalloc((void **)dst, std::max<size_t>(n, 1) * sizeof(T)));
+  if (n) CK(cudaMemcpyAsync(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  return EPHG_OK;
+}
+
+extern "C" {
+
+const char *ephg_last_error(void) { return g_err.c_str(); }
+
+int ephg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int ephg_destroy(ephg_handle *h) {
+  if (!h) return EPHG_OK;
+  void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->graw, h->G64,
+                  h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_den,
+                  h->rcartq, h->D, h->err};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  h->ws.release();
+  tc::free_split(h->split);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return EPHG_OK;
+}
+
+int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
+  if (!d || !out) return fail(EPHG_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (ephg_device_count() <= 0) return fail(EPHG_ERR_CUDA, "no CUDA device visible");
+  if (d->numwannbands < 1 || d->numwannbands > 32)
+    return fail(EPHG_ERR_ARG, "numwannbands must be in [1, 32]");
+  if (d->numbranches != 3 * d->numatoms || d->numbranches > 32)
+    return fail(EPHG_ERR_ARG, "numbranches must be 3*numatoms <= 32");
+  if (d->nwsg != d->nwsq)
+    return fail(EPHG_ERR_ARG, "nwsg must equal nwsq (the vertex Fourier uses rcells_q, wannier.f90:947)");
+  for (int64_t i = 0; i < 3 * d->nwsq; ++i)
+    if (d->rcells_g[i] != d->rcells_q[i])
+      return fail(EPHG_ERR_ARG, "rcells_g must equal rcells_q (wannier.f90:947-951,988-990)");
+  for (int64_t i = 0; i < d->nwsq; ++i)
+    if (d->gwsdeg[i] != d->phwsdeg[i]) return fail(EPHG_ERR_ARG, "gwsdeg must equal phwsdeg");
+  for (int i = 0; i < 3; ++i)
+    if (d->coarse_qmesh[i] <= 0) return fail(EPHG_ERR_ARG, "Bad input(s) in wannier.");
+  ephg_handle *h = new ephg_handle();
+  int rc = EPHG_OK;
+  auto bail = [&](int r) {
+    ephg_destroy(h);
+    return r;
+  };
+  if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaGetDevice"));
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(EPHG_ERR_CUDA, "cudaStreamCreate"));
+  h->nw = (int)d->numwannbands;
+  h->nb = (int)d->numbranches;
+  h->nwsk = (int)d->nwsk;
+  h->nwsq = (int)d->nwsq;
+  h->nwsg = (int)d->nwsg;
+  h->nat = (int)d->numatoms;
+  for (int i = 0; i < 3; ++i) h->cq[i] = (int)d->coarse_qmesh[i];
+  for (int i = 0; i < 9; ++i) h->lattvecs[i] = d->lattvecs[i];
+  h->masses_h.assign(d->masses, d->masses + h->nat);
+  const int nw = h->nw, nb = h->nb, nwsk = h->nwsk, nwsq = h->nwsq;
+  h->Nn = (int64_t)nw * nw * nb * nwsq;
+  // R lists as (n,3) int rows and degeneracies as doubles
+  auto rows = [](const int64_t *r, int n) {
+    std::vector<int> v(3 * (size_t)n);
+    for (int i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c) v[3 * i + c] = (int)r[i + (int64_t)n * c];
+    return v;
+  };
+  std::vector<int> rk = rows(d->rcells_k, nwsk), rq = rows(d->rcells_q, nwsq), rg = rows(d->rcells_g, nwsq);
+  std::vector<double> dk(d->elwsdeg, d->elwsdeg + nwsk), dq(d->phwsdeg, d->phwsdeg + nwsq),
+      dg(d->gwsdeg, d->gwsdeg + nwsq);
+  if ((rc = upload(&h->Rk, rk.data(), rk.size(), h->st)) || (rc = upload(&h->Rq, rq.data(), rq.size(), h->st)) ||
+      (rc = upload(&h->Rg, rg.data(), rg.size(), h->st)) || (rc = upload(&h->degk, dk.data(), dk.size(), h->st)) ||
+      (rc = upload(&h->degq, dq.data(), dq.size(), h->st)) || (rc = upload(&h->degg, dg.data(), dg.size(), h->st)) ||
+      (rc = upload(&h->masses, d->masses, (size_t)h->nat, h->st)))
+    return bail(rc);
+  // H(Re) with the velocity companions i*rcart*H (wannier.f90:466-478)
+  {
+    const size_t nn = (size_t)nw * nw;
+    std::vector<double2> hx((size_t)nwsk * 4 * nn);
+    for (int r = 0; r < nwsk; ++r) {
+      double R[3] = {(double)rk[3 * r], (double)rk[3 * r + 1], (double)rk[3 * r + 2]}, rc3[3];
+      for (int i = 0; i < 3; ++i)
+        rc3[i] = h->lattvecs[i] * R[0] + h->lattvecs[i + 3] * R[1] + h->lattvecs[i + 6] * R[2];
+      for (size_t e = 0; e < nn; ++e) {
+        size_t ib = e % nw, jb = e / nw;
+        const double *src = d->Hwann + 2 * (r + (size_t)nwsk * (ib + (size_t)nw * jb));
+        double2 v = make_double2(src[0], src[1]);
+        hx[(size_t)r * 4 * nn + e] = v;
+        for (int p = 0; p < 3; ++p)
+          hx[(size_t)r * 4 * nn + (1 + p) * nn + e] = make_double2(-rc3[p] * v.y, rc3[p] * v.x);
+      }
+    }
+    if ((rc = upload(&h->Hext, hx.data(), hx.size(), h->st))) return bail(rc);
+  }
+  // g(Re,Rp): raw epmatwp order and the stage-A layout
+  {
+    size_t n = (size_t)nw * nw * nwsk * nb * nwsq;
+    if ((rc = upload(&h->graw, (const double2 *)d->gwann, n, h->st))) return bail(rc);
+    if (cudaMalloc(&h->G64, n * sizeof(double2)) != cudaSuccess)
+      return bail(fail(EPHG_ERR_NOMEM, "cudaMalloc g(Re,Rp) %zu bytes", n * 16));
+    launch_permute_gwann(nw, nb, nwsk, nwsq, h->graw, h->G64, h->st);
+  }
+  // phonon terms: for each atom pair and WS cell, the shortest wraps
+  {
+    std::vector<int> pair_off(h->nat * h->nat + 1, 0), ent_iuc, ent_woff(1, 0), wrapR;
+    std::vector<double> ent_den;
+    for (int jat = 0; jat < h->nat; ++jat)
+      for (int iat = 0; iat < h->nat; ++iat) {
+        int pair = iat + h->nat * jat;
+        pair_off[pair] = (int)ent_iuc.size();
+        for (int iuc = 0; iuc < nwsq; ++iuc) {
+          double dist[3];
+          for (int c = 0; c < 3; ++c)
+            dist[c] = ((double)rq[3 * iuc + c] - d->basis[c + 3 * iat] + d->basis[c + 3 * jat]) /
+                      (double)h->cq[c];
+          std::vector<int> w = ws_wrap(h->lattvecs, dist, 1.0e-6);
+          int nwrap = (int)w.size() / 3;
+          ent_iuc.push_back(iuc);
+          ent_den.push_back((double)(d->phwsdeg[iuc] * nwrap));
+          for (int iw = 0; iw < nwrap; ++iw)
+            for (int c = 0; c < 3; ++c) wrapR.push_back(rq[3 * iuc + c] + w[3 * iw + c] * h->cq[c]);
+          ent_woff.push_back((int)wrapR.size() / 3);
+        }
+      }
+    // pair_off must be monotone over the pair index order used by the kernel
+    {
+      std::vector<int> off(h->nat * h->nat + 1);
+      int cur = 0;
+      for (int p = 0; p < h->nat * h->nat; ++p) {
+        off[p] = cur;
+        cur += nwsq;
+      }
+      off[h->nat * h->nat] = cur;
+      // entries were appended in jat-major order, identical to pair = iat + nat*jat
+      pair_off = off;
+    }
+    std::vector<double> rcq((size_t)nwsq * 3);
+    for (int r = 0; r < nwsq; ++r)
+      for (int i = 0; i < 3; ++i)
+        rcq[r + (size_t)nwsq * i] = h->lattvecs[i] * rq[3 * r] + h->lattvecs[i + 3] * rq[3 * r + 1] +
+                                    h->lattvecs[i + 6] * rq[3 * r + 2];
+    if ((rc = upload(&h->pair_off, pair_off.data(), pair_off.size(), h->st)) ||
+        (rc = upload(&h->ent_iuc, ent_iuc.data(), ent_iuc.size(), h->st)) ||
+        (rc = upload(&h->ent_woff, ent_woff.data(), ent_woff.size(), h->st)) ||
+        (rc = upload(&h->wrapR, wrapR.data(), wrapR.size(), h->st)) ||
+        (rc = upload(&h->ent_den, ent_den.data(), ent_den.size(), h->st)) ||
+        (rc = upload(&h->rcartq, rcq.data(), rcq.size(), h->st)) ||
+        (rc = upload(&h->D, (const double2 *)d->Dphwann, (size_t)nwsq * nb * nb, h->st)))
+      return bail(rc);
+    h->terms.npair = h->nat * h->nat;
+    h->terms.pair_off = h->pair_off;
+    h->terms.ent_iuc = h->ent_iuc;
+    h->terms.ent_woff = h->ent_woff;
+    h->terms.wrapR = h->wrapR;
+    h->terms.ent_den = h->ent_den;
+    h->terms.D = h->D;
+    h->terms.rcart = h->rcartq;
+    h->terms.masses = h->masses;
+    h->terms.nwsq = nwsq;
+    h->terms.nb = nb;
+    h->terms.nat = h->nat;
+  }
+  if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaMalloc err"));
+  if (cudaMemsetAsync(h->err, 0, sizeof(int), h->st) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "memset"));
+  if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(EPHG_ERR_CUDA, "create: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = h;
+  return EPHG_OK;
+}
+
+// ------------------------------------------------------------- el_wann
+int ephg_el_wann(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
+                 double *velocities, double *evecs, const double *scissor) {
+  if (!h || nk < 0 || (nk > 0 && (!kvecs || !energies)))
+    return fail(EPHG_ERR_ARG, "el_wann: bad arguments");
+  if (velocities && !evecs)
+    return fail(EPHG_ERR_ARG, "In el_wann, velocity is present but not eigenvecs.");
+  if (nk == 0) return EPHG_OK;
+  const int nw = h->nw, nwsk = h->nwsk;
+  const size_t nn = (size_t)nw * nw;
+  const int with_vel = velocities != nullptr;
+  const int ncol = with_vel ? 4 * (int)nn : (int)nn;
+  double *kv, *w, *ens, *vel, *sc = nullptr;
+  double2 *P, *C, *V, *ev;
+  int rc;
+  if ((rc = wsget(h->ws, "el_kv", (size_t)nk * 3, &kv)) || (rc = wsget(h->ws, "el_P", (size_t)nk * nwsk, &P)) ||
+      (rc = wsget(h->ws, "el_C", (size_t)nk * ncol, &C)) || (rc = wsget(h->ws, "el_w", (size_t)nk * nw, &w)) ||
+      (rc = wsget(h->ws, "el_V", (size_t)nk * nn, &V)) || (rc = wsget(h->ws, "el_e", (size_t)nk * nw, &ens)) ||
+      (rc = wsget(h->ws, "el_vel", with_vel ? (size_t)nk * nw * 3 : 1, &vel)) ||
+      (rc = wsget(h->ws, "el_ev", evecs ? (size_t)nk * nn : 1, &ev)))
+    return WSFAIL(rc);
+  if (scissor) {
+    if ((rc = wsget(h->ws, "el_sc", (size_t)nw, &sc))) return WSFAIL(rc);
+    CK(cudaMemcpyAsync(sc, scissor, nw * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  }
+  CK(cudaMemcpyAsync(kv, kvecs, (size_t)nk * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  launch_phase_frac((int)nk, kv, nwsk, h->Rk, h->degk, P, nwsk, h->st);
+  launch_zgemm((int)nk, ncol, nwsk, P, nwsk, h->Hext, 4 * (int64_t)nn, C, ncol, h->st);
+  launch_heig((int)nk, nw, C, ncol, w, V, h->err, h->st);
+  launch_el_post((int)nk, nw, w, V, C, ncol, with_vel, sc, ens, with_vel ? vel : nullptr,
+                 evecs ? ev : nullptr, nullptr, h->st);
+  h->launches += 4;
+  CKL();
+  CK(cudaMemcpyAsync(energies, ens, (size_t)nk * nw * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (evecs) CK(cudaMemcpyAsync(evecs, ev, (size_t)nk * nn * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  if (with_vel) CK(cudaMemcpyAsync(velocities, vel, (size_t)nk * nw * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return check_err(h);
+}
+
+// ------------------------------------------------------------- ph_wann
+int ephg_ph_wann(ephg_handle *h, int64_t nq, const double *qvecs, double *energies,
+                 double *evecs, double *velocities) {
+  if (!h || nq < 0 || (nq > 0 && (!qvecs || !energies)))
+    return fail(EPHG_ERR_ARG, "ph_wann: bad arguments");
+  if (velocities && !evecs)
+    return fail(EPHG_ERR_ARG, "In ph_wann, velocity is present but not eigenvecs.");
+  if (nq == 0) return EPHG_OK;
+  const int nb = h->nb;
+  const size_t nn = (size_t)nb * nb;
+  const int with_vel = velocities != nullptr;
+  double *qv, *w, *ens, *vel;
+  double2 *Dq, *dDq, *V, *ev;
+  int rc;
+  if ((rc = wsget(h->ws, "ph_qv", (size_t)nq * 3, &qv)) || (rc = wsget(h->ws, "ph_D", (size_t)nq * nn, &Dq)) ||
+      (rc = wsget(h->ws, "ph_dD", with_vel ? (size_t)nq * 3 * nn : 1, &dDq)) ||
+      (rc = wsget(h->ws, "ph_w", (size_t)nq * nb, &w)) || (rc = wsget(h->ws, "ph_V", (size_t)nq * nn, &V)) ||
+      (rc = wsget(h->ws, "ph_e", (size_t)nq * nb, &ens)) ||
+      (rc = wsget(h->ws, "ph_vel", with_vel ? (size_t)nq * nb * 3 : 1, &vel)) ||
+      (rc = wsget(h->ws, "ph_ev", evecs ? (size_t)nq * nn : 1, &ev)))
+    return WSFAIL(rc);
+  CK(cudaMemcpyAsync(qv, qvecs, (size_t)nq * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  launch_dbuild((int)nq, nullptr, nullptr, 1, nullptr, qv, h->terms, with_vel, Dq, dDq, h->st);
+  launch_heig((int)nq, nb, Dq, nn, w, V, h->err, h->st);
+  launch_ph_post((int)nq, nb, nullptr, qv, w, V, dDq, with_vel, h->masses, ens,
+                 evecs ? ev : nullptr, with_vel ? vel : nullptr, nullptr, nullptr, nullptr, h->err,
+                 h->st);
+  h->launches += 3;
+  CKL();
+  CK(cudaMemcpyAsync(energies, ens, (size_t)nq * nb * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (evecs) CK(cudaMemcpyAsync(evecs, ev, (size_t)nq * nn * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  if (with_vel) CK(cudaMemcpyAsync(velocities, vel, (size_t)nq * nb * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return check_err(h);
+}
+
+// ---------------------------------------------------------------- gkRp
+int ephg_gkRp(ephg_handle *h, int64_t nk, const double *kvecs, double *gmixed) {
+  if (!h || nk < 0 || (nk > 0 && (!kvecs || !gmixed))) return fail(EPHG_ERR_ARG, "gkRp: bad arguments");
+  if (nk == 0) return EPHG_OK;
+  const int nwsk = h->nwsk;
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nk, (int64_t)(1u << 30) / (h->Nn * 16)));
+  double *kv;
+  double2 *P, *C;
+  int rc;
+  if ((rc = wsget(h->ws, "gk_kv", (size_t)chunk * 3, &kv)) || (rc = wsget(h->ws, "gk_P", (size_t)chunk * nwsk, &P)) ||
+      (rc = wsget(h->ws, "gk_C", (size_t)chunk * h->Nn, &C)))
+    return WSFAIL(rc);
+  std::vector<double> kc((size_t)chunk * 3);
+  for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
+    int64_t n = std::min(chunk, nk - k0);
+    for (int c = 0; c < 3; ++c)
+      for (int64_t i = 0; i < n; ++i) kc[i + n * c] = kvecs[(k0 + i) + nk * c];
+    CK(cudaMemcpyAsync(kv, kc.data(), (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    launch_phase_frac((int)n, kv, nwsk, h->Rk, h->degk, P, nwsk, h->st);
+    launch_zgemm((int)n, (int)h->Nn, nwsk, P, nwsk, h->G64, h->Nn, C, h->Nn, h->st);
+    h->launches += 2;
+    CKL();
+    CK(cudaMemcpyAsync(gmixed + 2 * k0 * h->Nn, C, (size_t)n * h->Nn * sizeof(double2),
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return check_err(h);
+}
+
+// ---------------------------------------------------------------- gReq
+int ephg_gReq(ephg_handle *h, int64_t nq, const double *qvecs, double *gmixed) {
+  if (!h || nq < 0 || (nq > 0 && (!qvecs || !gmixed))) return fail(EPHG_ERR_ARG, "gReq: bad arguments");
+  if (nq == 0) return EPHG_OK;
+  const int nw = h->nw, nb = h->nb, nwsk = h->nwsk, nwsg = h->nwsg;
+  const int64_t per = (int64_t)nw * nw * nb * nwsk;
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)(1u << 30) / (per * 16)));
+  double *qv;
+  double2 *P, *C, *O;
+  int rc;
+  if ((rc = wsget(h->ws, "gq_qv", (size_t)chunk * 3, &qv)) || (rc = wsget(h->ws, "gq_P", (size_t)chunk * nwsg, &P)) ||
+      (rc = wsget(h->ws, "gq_C", (size_t)chunk * per, &C)) || (rc = wsget(h->ws, "gq_O", (size_t)chunk * per, &O)))
+    return WSFAIL(rc);
+  std::vector<double> qc((size_t)chunk * 3);
+  for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
+    int64_t n = std::min(chunk, nq - q0);
+    for (int c = 0; c < 3; ++c)
+      for (int64_t i = 0; i < n; ++i) qc[i + n * c] = qvecs[(q0 + i) + nq * c];
+    CK(cudaMemcpyAsync(qv, qc.data(), (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    // sum_Rp e^{2 pi i q.Rp}/gwsdeg * g(i,j,Re,s,Rp): rows of the raw array are Rp
+    launch_phase_frac((int)n, qv, nwsg, h->Rg, h->degg, P, nwsg, h->st);
+    launch_zgemm((int)n, (int)per, nwsg, P, nwsg, h->graw, per, C, per, h->st);
+    launch_permute_greq((int)n, nw, nb, nwsk, C, O, h->st);
+    h->launches += 3;
+    CKL();
+    CK(cudaMemcpyAsync(gmixed + 2 * q0 * per, O, (size_t)n * per * sizeof(double2),
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return check_err(h);
+}
+
+// ------------------------------------------------------------------ g2
+int ephg_g2(ephg_handle *h, int64_t wannspace, int64_t nv, const double *kvecs,
+            const double *qvecs, const double *el_evec_k, const double *el_evec_kp,
+            const double *ph_evec_q, const double *ph_en, int64_t ngm, const double *gmixed,
+            const int64_t *gm_index, double *g2_out) {
+  if (!h || nv < 0) return fail(EPHG_ERR_ARG, "g2: bad arguments");
+  if (wannspace != EPHG_WANNSPACE_EL && wannspace != EPHG_WANNSPACE_PH)
+    return fail(EPHG_ERR_ARG, "Invalid value of wannspace in call to g2_epw. Exiting.");
+  if (nv == 0) return EPHG_OK;
+  for (int64_t v = 0; v < nv; ++v)
+    if (gm_index[v] < 1 || gm_index[v] > ngm) return fail(EPHG_ERR_ARG, "g2: gm_index out of range");
+  const int nw = h->nw, nb = h->nb;
+  const int nws = wannspace == EPHG_WANNSPACE_PH ? h->nwsg : h->nwsk;
+  const int64_t gstride = (int64_t)nw * nw * nb * nws;
+  double *qv, *en, *out;
+  double2 *ek, *ekp, *eq, *gm;
+  int64_t *gi;
+  int rc;
+  if ((rc = wsget(h->ws, "g2_qv", (size_t)nv * 3, &qv)) || (rc = wsget(h->ws, "g2_en", (size_t)nv, &en)) ||
+      (rc = wsget(h->ws, "g2_out", (size_t)nv, &out)) || (rc = wsget(h->ws, "g2_ek", (size_t)nv * nw, &ek)) ||
+      (rc = wsget(h->ws, "g2_ekp", (size_t)nv * nw, &ekp)) || (rc = wsget(h->ws, "g2_eq", (size_t)nv * nb, &eq)) ||
+      (rc = wsget(h->ws, "g2_gm", (size_t)ngm * gstride, &gm)) || (rc = wsget(h->ws, "g2_gi", (size_t)nv, &gi)))
+    return WSFAIL(rc);
+  const double *kq = wannspace == EPHG_WANNSPACE_PH ? qvecs : kvecs;
+  CK(cudaMemcpyAsync(qv, kq, (size_t)nv * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(en, ph_en, (size_t)nv * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(ek, el_evec_k, (size_t)nv * nw * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(ekp, el_evec_kp, (size_t)nv * nw * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(eq, ph_evec_q, (size_t)nv * nb * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(gm, gmixed, (size_t)ngm * gstride * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(gi, gm_index, (size_t)nv * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
+  const int *R = wannspace == EPHG_WANNSPACE_PH ? h->Rq : h->Rk;
+  const double *deg = wannspace == EPHG_WANNSPACE_PH ? h->degq : h->degk;
+  launch_g2_batch((int)nv, nw, nb, nws, qv, R, deg, ek, ekp, eq, en, h->masses, gm, gi, gstride,
+                  out, h->st);
+  h->launches += 1;
+  CKL();
+  CK(cudaMemcpyAsync(g2_out, out, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return check_err(h);
+}
+
+// ------------------------------------------------------------ kq index
+int ephg_kq_index(ephg_handle *h, const int64_t mesh[3], int64_t nk, const int64_t *k_idx,
+                  int64_t nkp, const int64_t *kp_idx, int64_t *q_idx) {
+  if (!h || !mesh || nk < 0 || nkp < 0) return fail(EPHG_ERR_ARG, "kq_index: bad arguments");
+  for (int i = 0; i < 3; ++i)
+    if (mesh[i] <= 0) return fail(EPHG_ERR_ARG, "kq_index: bad mesh");
+  if (nk == 0 || nkp == 0) return EPHG_OK;
+  int m[3] = {(int)mesh[0], (int)mesh[1], (int)mesh[2]};
+  int64_t *a, *b, *q;
+  int rc;
+  if ((rc = wsget(h->ws, "kq_a", (size_t)nk, &a)) || (rc = wsget(h->ws, "kq_b", (size_t)nkp, &b)) ||
+      (rc = wsget(h->ws, "kq_q", (size_t)nk * nkp, &q)))
+    return WSFAIL(rc);
+  CK(cudaMemcpyAsync(a, k_idx, nk * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(b, kp_idx, nkp * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
+  launch_kq_index(m, (int)nk, a, (int)nkp, b, q, h->err, h->st);
+  h->launches += 1;
+  CKL();
+  CK(cudaMemcpyAsync(q_idx, q, (size_t)nk * nkp * sizeof(int64_t), cudaMemcpyDeviceToHost, h->st));
+  return check_err(h);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- rates
+namespace {
+
+// form_triangles / form_tetrahedra_3d + fill (delta.f90:494-646,648-788) on the
+// host: integer set-up of the simplices of the window mesh, uploaded once per
+// request.  Output layouts: map (nwv, maxc, 2), count (nwv), evals (ns, nw, nv).
+void build_simplices(int kind, const int mesh[3], const std::vector<int> &widx,
+                     const std::vector<double> &ens_w, int nw, std::vector<int> &map,
+                     std::vector<int> &count, std::vector<double> &sev, int &nsimplex, int &maxc,
+                     int &nv) {
+  const int nk = (int)widx.size();
+  const int per = kind == 1 ? 2 : 6;
+  nv = kind == 1 ? 3 : 4;
+  maxc = kind == 1 ? 6 : 24;
+  nsimplex = per * nk;
+  static const int tri[2][3] = {{1, 2, 3}, {1, 3, 4}};
+  static const int tet[6][4] = {{1, 2, 3, 6}, {1, 3, 5, 6}, {3, 5, 6, 7}, {3, 6, 7, 8}, {3, 4, 6, 8}, {2, 3, 4, 6}};
+  std::vector<int> simplex((size_t)nsimplex * nv, 0);
+  map.assign((size_t)nk * maxc * 2, 0);
+  count.assign(nk, 0);
+  // widx is sorted ascending (0-based mesh index) = indexlist - 1
+  auto find = [&](int mux1) -> int {   // binsearch (misc.f90:738), 1-based or -1
+    auto it = std::lower_bound(widx.begin(), widx.end(), mux1 - 1);
+    if (it != widx.end() && *it == mux1 - 1) return (int)(it - widx.begin()) + 1;
+    return -1;
+  };
+  int cnt = 1;
+  for (int ik = 0; ik < nk; ++ik) {
+    int p = widx[ik];
+    int i = p % mesh[0] + 1, j = (p / mesh[0]) % mesh[1] + 1, k = p / (mesh[0] * mesh[1]) + 1;
+    int ip1 = i == mesh[0] ? 1 : i + 1, jp1 = j == mesh[1] ? 1 : j + 1, kp1 = k == mesh[2] ? 1 : k + 1;
+    int sc[8][3] = {{i, j, k}, {ip1, j, k}, {i, jp1, k}, {ip1, jp1, k},
+                    {i, j, kp1}, {ip1, j, kp1}, {i, jp1, kp1}, {ip1, jp1, kp1}};
+    for (int tk = 0; tk < per; ++tk) {
+      for (int tl = 0; tl < nv; ++tl) {
+        int a = (kind == 1 ? tri[tk][tl] : tet[tk][tl]) - 1;
+        int mux = ((sc[a][2] - 1) * mesh[1] + (sc[a][1] - 1)) * mesh[0] + sc[a][0];
+        int tmp = find(mux);
+        simplex[(size_t)(cnt - 1) * nv + tl] = tmp;
+        if (tmp > 0) {
+          int c = ++count[tmp - 1];
+          map[((size_t)(tmp - 1) * maxc + (c - 1)) * 2] = cnt;
+          map[((size_t)(tmp - 1) * maxc + (c - 1)) * 2 + 1] = tl + 1;
+        }
+      }
+      cnt++;
+    }
+  }
+  sev.assign((size_t)nsimplex * nw * nv, 0.0);
+  for (int it = 0; it < nsimplex; ++it) {
+    for (int iv = 0; iv < nv; ++iv) {
+      int aux = simplex[(size_t)it * nv + iv];
+      if (aux > 0)
+        for (int ib = 0; ib < nw; ++ib) sev[((size_t)it * nw + ib) * nv + iv] = ens_w[(size_t)(aux - 1) * nw + ib];
+    }
+    for (int ib = 0; ib < nw; ++ib) std::sort(&sev[((size_t)it * nw + ib) * nv], &sev[((size_t)it * nw + ib) * nv] + nv);
+  }
+}
+
+struct EvTimer {
+  cudaEvent_t e[6];
+  EvTimer() { for (auto &x : e) cudaEventCreate(&x); }
+  ~EvTimer() { for (auto &x : e) cudaEventDestroy(x); }
+};
+
+}  // namespace
+
+extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
+                             int64_t *indexlist, ephg_rate_stats *stats, double *g2,
+                             double *xplus, double *xminus, int64_t cap) {
+  if (!h || !req || !rates || !indexlist) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
+  for (int i = 0; i < 3; ++i)
+    if (req->mesh[i] <= 0) return fail(EPHG_ERR_ARG, "el_rates: bad mesh");
+  if (req->delta_kind < 0 || req->delta_kind > 2) return fail(EPHG_ERR_ARG, "el_rates: bad delta_kind");
+  if (req->delta_kind == 0 && !(req->sigma > 0)) return fail(EPHG_ERR_ARG, "el_rates: sigma must be > 0");
+  if (!(req->T > 0)) return fail(EPHG_ERR_ARG, "el_rates: T must be > 0");
+  if (req->precision != EPHG_PREC_FP64 && req->precision != EPHG_PREC_SPLIT_TF32)
+    return fail(EPHG_ERR_ARG, "el_rates: bad precision");
+  const int64_t N64 = req->mesh[0] * req->mesh[1] * req->mesh[2];
+  if (N64 > (1 << 24)) return fail(EPHG_ERR_ARG, "el_rates: mesh too large");
+  const int N = (int)N64;
+  const int mesh[3] = {(int)req->mesh[0], (int)req->mesh[1], (int)req->mesh[2]};
+  const int L = lcm3(mesh);
+  const int nw = h->nw, nb = h->nb, nwsk = h->nwsk, nwsq = h->nwsq;
+  const size_t nn = (size_t)nw * nw;
+  const int ncol = nw * nb;   // columns per initial state in stage B
+  const bool split = req->precision == EPHG_PREC_SPLIT_TF32;
+  cudaStream_t st = h->st;
+  int rc;
+  int64_t launches0 = h->launches;
+  EvTimer ev;
+  CK(cudaEventRecord(ev.e[0], st));
+  // ---- set-up: electrons on the full mesh (el_wann, electron.f90:364) ----
+  double2 *roots, *P, *Hk, *V, *Dq, *Vq, *u;
+  double *w, *ens, *wq, *om, *bose, *rates_d;
+  int *flag, *widx, *nwv_d, *sflag, *iota, *st_code, *nst_d, *nin_k, *cum;
+  if ((rc = wsget(h->ws, "r_roots", (size_t)L, &roots)) || (rc = wsget(h->ws, "r_P", (size_t)N * nwsk, &P)) ||
+      (rc = wsget(h->ws, "r_Hk", (size_t)N * nn, &Hk)) || (rc = wsget(h->ws, "r_w", (size_t)N * nw, &w)) ||
+      (rc = wsget(h->ws, "r_V", (size_t)N * nn, &V)) || (rc = wsget(h->ws, "r_ens", (size_t)N * nw, &ens)) ||
+      (rc = wsget(h->ws, "r_flag", (size_t)N, &flag)) || (rc = wsget(h->ws, "r_widx", (size_t)N, &widx)) ||
+      (rc = wsget(h->ws, "r_nwv", 4, &nwv_d)) || (rc = wsget(h->ws, "r_iota", (size_t)N * nw, &iota)) ||
+      (rc = wsget(h->ws, "r_Dq", (size_t)N * nb * nb, &Dq)) || (rc = wsget(h->ws, "r_wq", (size_t)N * nb, &wq)) ||
+      (rc = wsget(h->ws, "r_Vq", (size_t)N * nb * nb, &Vq)) || (rc = wsget(h->ws, "r_om", (size_t)N * nb, &om)) ||
+      (rc = wsget(h->ws, "r_u", (size_t)N * nb * nb, &u)) || (rc = wsget(h->ws, "r_bose", (size_t)N * nb, &bose)) ||
+      (rc = wsget(h->ws, "r_rates", (size_t)N * nw, &rates_d)))
+    return WSFAIL(rc);
+  launch_roots(L, roots, st);
+  launch_phase_mesh(N, nullptr, mesh, L, nwsk, h->Rk, h->degk, 0, roots, P, nwsk, st);
+  launch_zgemm(N, (int)nn, nwsk, P, nwsk, h->Hext, 4 * (int64_t)nn, Hk, nn, st);
+  launch_heig(N, nw, Hk, nn, w, V, h->err, st);
+  launch_el_post(N, nw, w, V, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, ens, st);
+  // ---- window (apply_energy_window, electron.f90:597-636) ----
+  launch_window_flags(N, nw, ens, req->enref, req->fsthick, flag, st);
+  launch_iota(N * nw, iota, st);
+  size_t tmp_bytes = 0, tb2 = 0, tb3 = 0;
+  cub::DeviceSelect::Flagged(nullptr, tmp_bytes, iota, flag, widx, nwv_d, N, st);
+  int *sfl_tmp;
+  if ((rc = wsget(h->ws, "r_sflag", (size_t)N * nw, &sflag)) || (rc = wsget(h->ws, "r_stcode", (size_t)N * nw, &st_code)) ||
+      (rc = wsget(h->ws, "r_nst", 4, &nst_d)) || (rc = wsget(h->ws, "r_nink", (size_t)N + 1, &nin_k)) ||
+      (rc = wsget(h->ws, "r_cum", (size_t)N + 1, &cum)))
+    return WSFAIL(rc);
+  cub::DeviceSelect::Flagged(nullptr, tb2, iota, sflag, st_code, nst_d, N * nw, st);
+  cub::DeviceScan::ExclusiveSum(nullptr, tb3, nin_k, cum, N + 1, st);
+  void *cubtmp;
+  if ((rc = h->ws.get("r_cub", std::max(tmp_bytes, std::max(tb2, tb3)), &cubtmp))) return WSFAIL(rc);
+  size_t tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
+  cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, flag, widx, nwv_d, N, st);
+  h->launches += 8;
+  CKL();
+  int nwv = 0;
+  CK(cudaMemcpyAsync(&nwv, nwv_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_err(h))) return rc;
+  if (nwv == 0) return fail(EPHG_ERR_EMPTY_WINDOW, "No states found within Fermi window.");
+  // ---- phonons on the q mesh (phonon.f90:208-214) ----
+  launch_dbuild(N, iota, mesh, L, roots, nullptr, h->terms, 0, Dq, nullptr, st);
+  launch_heig(N, nb, Dq, (int64_t)nb * nb, wq, Vq, h->err, st);
+  float2 *uf = nullptr;
+  if (split && (rc = wsget(h->ws, "r_uf", (size_t)N * nb * nb, &uf))) return WSFAIL(rc);
+  launch_ph_post(N, nb, iota, nullptr, wq, Vq, nullptr, 0, h->masses, nullptr, nullptr, nullptr, om,
+                 u, uf, h->err, st);
+  launch_bose(N, nb, om, req->T, bose, st);
+  // ---- initial states (demux_state order, interactions.f90:2169-2191) ----
+  launch_state_flags(nwv, nw, widx, ens, req->enref, req->fsthick, sflag, nin_k, st);
+  CK(cudaMemsetAsync(nin_k + nwv, 0, sizeof(int), st));
+  tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
+  cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, sflag, st_code, nst_d, nwv * nw, st);
+  tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
+  cub::DeviceScan::ExclusiveSum(cubtmp, tbytes, nin_k, cum, nwv + 1, st);
+  h->launches += 7;
+  CKL();
+  int nst = 0, nin = 0;
+  CK(cudaMemcpyAsync(&nst, nst_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&nin, cum + nwv, sizeof(int), cudaMemcpyDeviceToHost, st));
+  std::vector<int> widx_h(nwv), code_h;
+  CK(cudaMemcpyAsync(widx_h.data(), widx, nwv * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_err(h))) return rc;
+  code_h.resize(nst);
+  CK(cudaMemcpyAsync(code_h.data(), st_code, nst * sizeof(int), cudaMemcpyDeviceToHost, st));
+  // simplices for triangle / tetrahedron deltas
+  EpiData ed;
+  memset(&ed, 0, sizeof ed);
+  if (req->delta_kind != 0) {
+    std::vector<double> ens_all((size_t)N * nw), ens_w((size_t)nwv * nw);
+    CK(cudaMemcpyAsync(ens_all.data(), ens, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i < nwv; ++i)
+      for (int b = 0; b < nw; ++b) ens_w[(size_t)i * nw + b] = ens_all[(size_t)widx_h[i] * nw + b];
+    std::vector<int> map, count;
+    std::vector<double> sev;
+    int ns, maxc, nvx;
+    build_simplices((int)req->delta_kind, mesh, widx_h, ens_w, nw, map, count, sev, ns, maxc, nvx);
+    int *dmap, *dcount;
+    double *dsev;
+    if ((rc = wsget(h->ws, "r_smap", map.size(), &dmap)) || (rc = wsget(h->ws, "r_scount", count.size(), &dcount)) ||
+        (rc = wsget(h->ws, "r_sev", sev.size(), &dsev)))
+      return WSFAIL(rc);
+    CK(cudaMemcpyAsync(dmap, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dcount, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dsev, sev.data(), sev.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ed.smap = dmap;
+    ed.scount = dcount;
+    ed.sevals = dsev;
+    ed.nsimplex = ns;
+    ed.maxc = maxc;
+    ed.nvx = nvx;
+  }
+  CK(cudaStreamSynchronize(st));
+  std::vector<int> first_state(nwv + 1, nst);
+  for (int j = nst - 1; j >= 0; --j) first_state[code_h[j] / nw] = j;
+  for (int i = nwv - 1; i >= 0; --i)
+    if (first_state[i] > first_state[i + 1]) first_state[i] = first_state[i + 1];
+  CK(cudaEventRecord(ev.e[1], st));
+  // ---- stage A: g(k,Rp) for window k, rotation over m, k-half of the Rp phase ----
+  const int64_t ldb = (int64_t)ncol * nst;
+  const int64_t Nn = h->Nn;
+  RateParams rp;
+  for (int i = 0; i < 3; ++i) rp.mesh[i] = mesh[i];
+  rp.N = N;
+  rp.nw = nw;
+  rp.nb = nb;
+  rp.enref = req->enref;
+  rp.fsthick = req->fsthick;
+  rp.chempot = req->chempot;
+  rp.T = req->T;
+  rp.delta_kind = (int)req->delta_kind;
+  rp.sigma = req->sigma;
+  rp.inv_nk = 1.0 / (double)N;
+  rp.const_tp = 2.0 * 3.141592653589793 / hbar_eVps;
+  ed.widx = widx;
+  ed.st_code = st_code;
+  ed.cum = cum;
+  ed.ens = ens;
+  ed.U = V;
+  ed.om = om;
+  ed.u = u;
+  ed.uf = uf;
+  ed.bose = bose;
+  ed.per_state = (int64_t)nin * nb;
+  double *g2d = nullptr, *xpd = nullptr, *xmd = nullptr;
+  int64_t vtot = (int64_t)nst * nin * nb;
+  int64_t vcap = std::min<int64_t>(cap, vtot);
+  if (g2 && vcap > 0) {
+    if ((rc = wsget(h->ws, "r_vg2", (size_t)vcap, &g2d)) || (rc = wsget(h->ws, "r_vxp", (size_t)vcap, &xpd)) ||
+        (rc = wsget(h->ws, "r_vxm", (size_t)vcap, &xmd)))
+      return WSFAIL(rc);
+    ed.g2 = g2d;
+    ed.xp = xpd;
+    ed.xm = xmd;
+    ed.cap = vcap;
+  }
+  const int nblk = (nwv + 127) / 128;
+  double *partial;
+  if ((rc = wsget(h->ws, "r_partial", (size_t)nst * nblk, &partial))) return WSFAIL(rc);
+  if (!split) {
+    double2 *Pk, *gk, *B, *Pq, *Cb;
+    const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nwv, ((int64_t)1 << 31) / (Nn * 16)));
+    const int64_t sc = std::max<int64_t>(1, std::min<int64_t>(nst, ((int64_t)1 << 31) / ((int64_t)nwv * ncol * 16)));
+    if ((rc = wsget(h->ws, "a_Pk", (size_t)kc * nwsk, &Pk)) || (rc = wsget(h->ws, "a_gk", (size_t)kc * Nn, &gk)) ||
+        (rc = wsget(h->ws, "a_B", (size_t)nwsq * ldb, &B)) || (rc = wsget(h->ws, "b_Pq", (size_t)nwv * nwsq, &Pq)) ||
+        (rc = wsget(h->ws, "b_C", (size_t)nwv * ncol * sc, &Cb)))
+      return WSFAIL(rc);
+    for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
+      int n = (int)std::min<int64_t>(kc, nwv - i0);
+      launch_phase_mesh(n, widx + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
+      launch_zgemm(n, (int)Nn, nwsk, Pk, nwsk, h->G64, Nn, gk, Nn, st);
+      int j0 = first_state[i0], j1 = first_state[i0 + n];
+      // the rotation writes B columns relative to state 0
+      launch_rotate_states_fp64(j0, j1, (int)i0, st_code, nw, nb, nwsq, widx, V, gk, Nn, mesh, L,
+                                roots, h->Rq, h->degq, B + (int64_t)j0 * ncol, ldb, st);
+      h->launches += 3;
+    }
+    CK(cudaEventRecord(ev.e[2], st));
+    // ---- stage B + C: Rp Fourier against e^{2 pi i k'.Rp}, then the epilogue ----
+    launch_phase_mesh(nwv, widx, mesh, L, nwsq, h->Rq, nullptr, 0, roots, Pq, nwsq, st);
+    h->launches += 1;
+    for (int64_t j0 = 0; j0 < nst; j0 += sc) {
+      int ns = (int)std::min<int64_t>(sc, nst - j0);
+      launch_zgemm(nwv, ns * ncol, nwsq, Pq, nwsq, B + j0 * ncol, ldb, Cb, (int64_t)ns * ncol, st);
+      launch_epilogue_fp64(nwv, (int)j0, (int)j0 + ns, Cb, (int64_t)ns * ncol, rp, ed, partial, nblk, st);
+      h->launches += 2;
+    }
+  } else {
+    rc = tc::split_rates_stage(h->split, h->ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
+                               mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->Rq,
+                               h->degq, V, rp, ed, partial, nblk, ev.e[2], &h->launches);
+    if (rc) return fail(rc, "split path: %s", tc::last_error());
+  }
+  CKL();
+  CK(cudaMemsetAsync(rates_d, 0, (size_t)N * nw * sizeof(double), st));
+  launch_rate_final(nst, nblk, partial, st_code, nw, N, rates_d, st);
+  h->launches += 1;
+  CK(cudaEventRecord(ev.e[3], st));
+  CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int i = 0; i < nwv; ++i) indexlist[i] = (int64_t)widx_h[i] + 1;
+  if (g2 && vcap > 0) {
+    CK(cudaMemcpy(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost));
+    if (xplus) CK(cudaMemcpy(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
+    if (xminus) CK(cudaMemcpy(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if ((rc = check_err(h))) return rc;
+  if (stats) {
+    float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
+    cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
+    cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);
+    cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
+    cudaEventElapsedTime(&t03, ev.e[0], ev.e[3]);
+    stats->nwv = nwv;
+    stats->nstates_inwindow = nin;
+    stats->nstates = nst;
+    stats->vertices = vtot;
+    stats->pairs = (int64_t)nst * nwv;
+    stats->kernel_launches = h->launches - launches0;
+    stats->ms_setup = t01;
+    stats->ms_stage_a = t12;
+    stats->ms_stage_bc = t23;
+    stats->ms_total = t03;
+    stats->stage_a_gflop = 8.0 * (double)nwv * nwsk * (double)Nn * 1e-9;
+    stats->stage_b_gflop = 8.0 * (double)nwv * nwsq * (double)ncol * nst * 1e-9;
+  }
+  return EPHG_OK;
+}

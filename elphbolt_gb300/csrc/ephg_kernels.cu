@@ -1,0 +1,912 @@
+// ephg_kernels.cu - FP64 set-up and drop-in kernels of the e-ph vertex path.
+//
+// Phase tables, H(k)/D(q) assembly, the batched warp-level Hermitian Jacobi
+// eigensolver, the FP64 complex GEMM used by the plain drop-in, and the
+// per-(k', state) epilogue that forms |g|^2, X+- and the RTA rate partials.
+// Each kernel names the reference lines it restates.
+#include <cstdio>
+
+#include "ephg_kernels.cuh"
+
+namespace ephg {
+
+static constexpr double PI = 3.141592653589793;   // 4*atan(1), params.f90:44
+static constexpr double TWOPI = 2.0 * PI;
+
+// =================================================================== phases
+
+__global__ void k_roots(int L, double2 *roots) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= L) return;
+  double s, c;
+  sincospi(2.0 * (double)t / (double)L, &s, &c);
+  roots[t] = make_double2(c, s);
+}
+
+void launch_roots(int L, double2 *roots, cudaStream_t st) {
+  k_roots<<<(L + 255) / 256, 256, 0, st>>>(L, roots);
+}
+
+// exact integer modular phase index of k (mesh index p) and integer R
+__device__ inline int phase_index(int p, const int mesh[3], int L, int r1, int r2, int r3) {
+  int v1 = p % mesh[0];
+  int v2 = (p / mesh[0]) % mesh[1];
+  int v3 = p / (mesh[0] * mesh[1]);
+  int64_t t = (int64_t)v1 * r1 * (L / mesh[0]) + (int64_t)v2 * r2 * (L / mesh[1]) +
+              (int64_t)v3 * r3 * (L / mesh[2]);
+  return (int)floormod(t, L);
+}
+
+__global__ void k_phase_mesh(int nrows, const int *rowp, int m1, int m2, int m3, int L, int nR,
+                             const int *R, const double *deg, int conj, const double2 *roots,
+                             double2 *out, int64_t ldo) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nrows * nR) return;
+  int row = (int)(idx / nR), r = (int)(idx % nR);
+  int p = rowp ? rowp[row] : row;
+  const int mesh[3] = {m1, m2, m3};
+  int t = phase_index(p, mesh, L, R[3 * r], R[3 * r + 1], R[3 * r + 2]);
+  double2 v = roots[t];
+  if (conj) v.y = -v.y;
+  if (deg) { v.x /= deg[r]; v.y /= deg[r]; }
+  out[(int64_t)row * ldo + r] = v;
+}
+
+void launch_phase_mesh(int nrows, const int *rowp, const int mesh[3], int L, int nR,
+                       const int *R, const double *deg, int conj, const double2 *roots,
+                       double2 *out, int64_t ldo, cudaStream_t st) {
+  int64_t n = (int64_t)nrows * nR;
+  if (n == 0) return;
+  k_phase_mesh<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nrows, rowp, mesh[0], mesh[1],
+                                                             mesh[2], L, nR, R, deg, conj,
+                                                             roots, out, ldo);
+}
+
+// expi(twopi * dot_product(k, R)) / deg, misc.f90:588 with wannier.f90:467,1097
+__global__ void k_phase_frac(int nrows, const double *kv, int nR, const int *R,
+                             const double *deg, double2 *out, int64_t ldo) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nrows * nR) return;
+  int row = (int)(idx / nR), r = (int)(idx % nR);
+  double dot = kv[row] * (double)R[3 * r];
+  dot += kv[row + nrows] * (double)R[3 * r + 1];
+  dot += kv[row + 2 * nrows] * (double)R[3 * r + 2];
+  double s, c;
+  sincos(TWOPI * dot, &s, &c);
+  double2 v = make_double2(c, s);
+  if (deg) { v.x /= deg[r]; v.y /= deg[r]; }
+  out[(int64_t)row * ldo + r] = v;
+}
+
+void launch_phase_frac(int nrows, const double *kv, int nR, const int *R, const double *deg,
+                       double2 *out, int64_t ldo, cudaStream_t st) {
+  int64_t n = (int64_t)nrows * nR;
+  if (n == 0) return;
+  k_phase_frac<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nrows, kv, nR, R, deg, out, ldo);
+}
+
+// ============================================================ FP64 GEMM
+// C[M][N] = A[M][K] * B[K][N], complex double, row-major.  64x64 tile per
+// 256-thread block, 4x4 complex outputs per thread; FP64-FMA bound on GB300.
+constexpr int ZBM = 64, ZBN = 64, ZBK = 8;
+
+__global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, const double2 *__restrict__ A,
+                                               int64_t lda, const double2 *__restrict__ B,
+                                               int64_t ldb, double2 *__restrict__ C, int64_t ldc) {
+  __shared__ double2 sA[ZBK][ZBM + 1];
+  __shared__ double2 sB[ZBK][ZBN];
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
+  const int64_t m0 = (int64_t)blockIdx.y * ZBM, n0 = (int64_t)blockIdx.x * ZBN;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < K; k0 += ZBK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      int idx = t + 256 * r;
+      int row = idx / ZBK, kk = idx % ZBK;
+      int64_t gm = m0 + row;
+      int gk = k0 + kk;
+      sA[kk][row] = (gm < M && gk < K) ? A[gm * lda + gk] : make_double2(0.0, 0.0);
+      int kb = idx / ZBN, col = idx % ZBN;
+      int64_t gn = n0 + col;
+      int gkb = k0 + kb;
+      sB[kb][col] = (gn < N && gkb < K) ? B[(int64_t)gkb * ldb + gn] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZBK; ++kk) {
+      double2 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int64_t gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t gn = n0 + tx + 16 * j;
+      if (gn < N) C[gm * ldc + gn] = acc[i][j];
+    }
+  }
+}
+
+void launch_zgemm(int M, int N, int K, const double2 *A, int64_t lda, const double2 *B,
+                  int64_t ldb, double2 *C, int64_t ldc, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid((N + ZBN - 1) / ZBN, (M + ZBM - 1) / ZBM);
+  k_zgemm<<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc);
+}
+
+// ====================================================== Jacobi eigensolver
+// One warp per Hermitian matrix (n <= 32).  Parallel cyclic Jacobi with the
+// round-robin ordering: n/2 disjoint rotations per step, n-1 steps per sweep
+// (Golub & Van Loan sec. 8.5.4).  Stands in for zheev('V','U') at
+// wannier.f90:489 and :732.
+constexpr int EIG_MAXSWEEP = 40;
+
+__global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t stride,
+                       double *__restrict__ w, double2 *__restrict__ V, int *err) {
+  extern __shared__ double2 sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int mat = blockIdx.x * wpb + wib;
+  const int nn = n * n;
+  double2 *sA = sm + (size_t)wib * (2 * nn + 3 * 16);
+  double2 *sV = sA + nn;
+  double2 *sP = sV + nn;   // per pair: (c, s), (ph.x, ph.y), (p, q) packed
+  if (mat >= batch) return;
+  const double2 *Am = A + (size_t)mat * stride;
+  for (int idx = lane; idx < nn; idx += 32) {
+    int i = idx % n, j = idx / n;
+    double2 v;
+    if (i < j) {                       // averaged upper triangle (wannier.f90:481-486)
+      double2 aij = Am[i + n * j], aji = Am[j + n * i];
+      v = make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+    } else if (i > j) {
+      double2 aij = Am[i + n * j], aji = Am[j + n * i];
+      v = make_double2(0.5 * (aji.x + aij.x), -0.5 * (aji.y - aij.y));
+    } else {
+      v = make_double2(Am[i + n * i].x, 0.0);
+    }
+    sA[idx] = v;
+    sV[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncwarp();
+  const int m = n + (n & 1);         // even number of players (dummy = n)
+  const int half = m / 2;
+  bool converged = false;
+  for (int sweep = 0; sweep < EIG_MAXSWEEP; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int idx = lane; idx < nn; idx += 32) {
+      double2 a = sA[idx];
+      double a2 = a.x * a.x + a.y * a.y;
+      tot += a2;
+      if (idx % n != idx / n) off += a2;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    if (off <= 1e-30 * tot || off == 0.0) { converged = true; break; }
+    for (int r = 0; r < m - 1; ++r) {
+      if (lane < half) {
+        int a, b;
+        if (lane == 0) { a = 0; b = (r % (m - 1)) + 1; }
+        else {
+          a = ((r + lane) % (m - 1)) + 1;
+          b = ((r - lane + (m - 1)) % (m - 1)) + 1;
+        }
+        int p = min(a, b), q = max(a, b);
+        double c = 1.0, s = 0.0, phx = 1.0, phy = 0.0;
+        if (q < n) {
+          double2 apq = sA[p + n * q];
+          double rr = hypot(apq.x, apq.y);
+          if (rr > 1e-300) {
+            phx = apq.x / rr; phy = apq.y / rr;
+            double app = sA[p + n * p].x, aqq = sA[q + n * q].x;
+            double tau = (aqq - app) / (2.0 * rr);
+            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        sP[3 * lane] = make_double2(c, s);
+        sP[3 * lane + 1] = make_double2(phx, phy);
+        sP[3 * lane + 2] = make_double2((double)p, (double)(q < n ? q : -1));
+      }
+      __syncwarp();
+      // columns: A <- A J, V <- V J;  J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
+      for (int idx = lane; idx < half * n; idx += 32) {
+        int k = idx / n, i = idx % n;
+        int q = (int)sP[3 * k + 2].y;
+        if (q < 0) continue;
+        int p = (int)sP[3 * k + 2].x;
+        double c = sP[3 * k].x, s = sP[3 * k].y;
+        double2 phc = make_double2(sP[3 * k + 1].x, -sP[3 * k + 1].y);
+        double2 aip = sA[i + n * p], aiq = sA[i + n * q];
+        double2 t = cmul(phc, aiq);
+        sA[i + n * p] = make_double2(c * aip.x - s * t.x, c * aip.y - s * t.y);
+        sA[i + n * q] = make_double2(s * aip.x + c * t.x, s * aip.y + c * t.y);
+        double2 vip = sV[i + n * p], viq = sV[i + n * q];
+        t = cmul(phc, viq);
+        sV[i + n * p] = make_double2(c * vip.x - s * t.x, c * vip.y - s * t.y);
+        sV[i + n * q] = make_double2(s * vip.x + c * t.x, s * vip.y + c * t.y);
+      }
+      __syncwarp();
+      // rows: A <- J^H A
+      for (int idx = lane; idx < half * n; idx += 32) {
+        int k = idx / n, j = idx % n;
+        int q = (int)sP[3 * k + 2].y;
+        if (q < 0) continue;
+        int p = (int)sP[3 * k + 2].x;
+        double c = sP[3 * k].x, s = sP[3 * k].y;
+        double2 ph = sP[3 * k + 1];
+        double2 apj = sA[p + n * j], aqj = sA[q + n * j];
+        double2 t = cmul(ph, aqj);
+        sA[p + n * j] = make_double2(c * apj.x - s * t.x, c * apj.y - s * t.y);
+        sA[q + n * j] = make_double2(s * apj.x + c * t.x, s * apj.y + c * t.y);
+      }
+      __syncwarp();
+      if (lane < half) {
+        int q = (int)sP[3 * lane + 2].y;
+        if (q >= 0) {
+          int p = (int)sP[3 * lane + 2].x;
+          sA[p + n * q] = make_double2(0.0, 0.0);
+          sA[q + n * p] = make_double2(0.0, 0.0);
+          sA[p + n * p].y = 0.0;
+          sA[q + n * q].y = 0.0;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (!converged && lane == 0) atomicOr(err, DERR_EIG);
+  // sort ascending by rank (ties by index), write eigenvalues and columns
+  for (int i = lane; i < n; i += 32) {
+    double di = sA[i + n * i].x;
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      double dj = sA[j + n * j].x;
+      rank += (dj < di) || (dj == di && j < i);
+    }
+    w[(size_t)mat * n + rank] = di;
+    for (int c = 0; c < n; ++c) V[(size_t)mat * nn + c + n * rank] = sV[c + n * i];
+  }
+}
+
+void launch_heig(int batch, int n, const double2 *A, int64_t stride, double *w, double2 *V,
+                 int *err, cudaStream_t st) {
+  if (batch <= 0) return;
+  int wpb = n <= 16 ? 4 : 2;
+  size_t smem = (size_t)wpb * (2 * n * n + 3 * 16) * sizeof(double2);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_heig, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    attr_set = true;
+  }
+  k_heig<<<(batch + wpb - 1) / wpb, 32 * wpb, smem, st>>>(batch, n, A, stride, w, V, err);
+}
+
+// ============================================================ electrons
+// el_wann post-processing (wannier.f90:499-520): energies (eV, + scissor),
+// evecs(k,b,:) = eigenvector b, velocities by Feynman-Hellmann.
+__global__ void k_el_post(int nk, int nw, const double *w, const double2 *V, const double2 *C,
+                          int64_t ldc, int with_vel, const double *scissor, double *energies_f,
+                          double *vel_f, double2 *evecs_f, double *ens_i) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nk * nw) return;
+  int k = idx / nw, b = idx % nw;
+  const size_t nn = (size_t)nw * nw;
+  double e = w[(size_t)k * nw + b] * Ryd2eV;
+  if (scissor) e += scissor[b];
+  if (energies_f) energies_f[k + (int64_t)nk * b] = e;
+  if (ens_i) ens_i[(size_t)k * nw + b] = e;
+  const double2 *Vk = V + (size_t)k * nn;
+  if (evecs_f)
+    for (int c = 0; c < nw; ++c) evecs_f[k + (int64_t)nk * (b + (int64_t)nw * c)] = Vk[c + nw * b];
+  if (with_vel && vel_f) {
+    for (int p = 0; p < 3; ++p) {
+      const double2 *dH = C + (int64_t)k * ldc + (size_t)(1 + p) * nn;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int r = 0; r < nw; ++r) {
+        double2 mv = make_double2(0.0, 0.0);
+        for (int c = 0; c < nw; ++c) cfma(mv, dH[r + nw * c], Vk[c + nw * b]);
+        cfma_cj(acc, Vk[r + nw * b], mv);
+      }
+      vel_f[k + (int64_t)nk * (b + (int64_t)nw * p)] = acc.x * Ryd2radTHz;
+    }
+  }
+}
+
+void launch_el_post(int nk, int nw, const double *w, const double2 *V, const double2 *C,
+                    int64_t ldc, int with_vel, const double *scissor, double *energies_f,
+                    double *vel_f, double2 *evecs_f, double *ens_i, cudaStream_t st) {
+  int n = nk * nw;
+  if (n == 0) return;
+  k_el_post<<<(n + 127) / 128, 128, 0, st>>>(nk, nw, w, V, C, ldc, with_vel, scissor, energies_f,
+                                             vel_f, evecs_f, ens_i);
+}
+
+// ============================================================= phonons
+// D(q) assembly with Wigner-Seitz wrapping (wannier.f90:631-665), mass
+// normalisation (:716-729).  One block per q, one thread per matrix element.
+__global__ void k_dbuild(int nq, const int *qp, int m1, int m2, int m3, int L,
+                         const double2 *roots, const double *qv, PhTerms t, int with_vel,
+                         double2 *Dq, double2 *dDq) {
+  const int q = blockIdx.x;
+  const int nb = t.nb;
+  const int mesh[3] = {m1, m2, m3};
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    int a = e % nb, b = e / nb;
+    int iat = a / 3, jat = b / 3;
+    int pair = iat + t.nat * jat;
+    double2 acc = make_double2(0.0, 0.0);
+    double2 dacc[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    for (int en = t.pair_off[pair]; en < t.pair_off[pair + 1]; ++en) {
+      int iuc = t.ent_iuc[en];
+      double den = t.ent_den[en];
+      double2 cs = make_double2(0.0, 0.0);
+      for (int wv = t.ent_woff[en]; wv < t.ent_woff[en + 1]; ++wv) {
+        const int *R = t.wrapR + 3 * wv;
+        double2 ph;
+        if (qp) {
+          ph = roots[phase_index(qp[q], mesh, L, R[0], R[1], R[2])];
+        } else {
+          double dot = qv[q] * (double)R[0];
+          dot += qv[q + nq] * (double)R[1];
+          dot += qv[q + 2 * nq] * (double)R[2];
+          sincos(TWOPI * dot, &ph.y, &ph.x);
+        }
+        cs.x += ph.x / den;
+        cs.y += ph.y / den;
+      }
+      double2 d = t.D[iuc + (int64_t)t.nwsq * (a + (int64_t)nb * b)];
+      double2 term = cmul(cs, d);
+      acc = cadd(acc, term);
+      if (with_vel)
+        for (int p = 0; p < 3; ++p) {
+          double rc = t.rcart[iuc + (int64_t)t.nwsq * p];
+          dacc[p] = cadd(dacc[p], make_double2(-rc * term.y, rc * term.x));
+        }
+    }
+    double massnorm = 1.0 / sqrt(t.masses[iat] * t.masses[jat]) * Ryd2amu;
+    Dq[(size_t)q * nb * nb + e] = cscale(acc, massnorm);
+    if (with_vel)
+      for (int p = 0; p < 3; ++p) dDq[((size_t)q * 3 + p) * nb * nb + e] = cscale(dacc[p], massnorm);
+  }
+}
+
+void launch_dbuild(int nq, const int *qp, const int mesh[3], int L, const double2 *roots,
+                   const double *qv, const PhTerms &t, int with_vel, double2 *Dq, double2 *dDq,
+                   cudaStream_t st) {
+  if (nq <= 0) return;
+  int thr = t.nb * t.nb < 128 ? 64 : 128;
+  k_dbuild<<<nq, thr, 0, st>>>(nq, qp, mesh ? mesh[0] : 1, mesh ? mesh[1] : 1,
+                               mesh ? mesh[2] : 1, L, roots, qv, t, with_vel, Dq, dDq);
+}
+
+// ph_wann post-processing (wannier.f90:740-780)
+__global__ void k_ph_post(int nq, int nb, const int *qp, const double *qv, const double *w,
+                          const double2 *V, const double2 *dDq, int with_vel,
+                          const double *masses, double *energies_f, double2 *evecs_f,
+                          double *vel_f, double *om_i, double2 *u_i, float2 *u_f, int *err) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nq * nb) return;
+  int q = idx / nb, s = idx % nb;
+  const size_t nn = (size_t)nb * nb;
+  double o2 = w[(size_t)q * nb + s];
+  double e = sqrt(fabs(o2));
+  if (o2 < 0.0 || signbit(o2)) e = -e;          // sign(sqrt(abs(w)), w)
+  const double2 *Vq = V + (size_t)q * nn;
+  double vel[3] = {0.0, 0.0, 0.0};
+  if (with_vel) {
+    for (int p = 0; p < 3; ++p) {
+      const double2 *dD = dDq + ((size_t)q * 3 + p) * nn;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int r = 0; r < nb; ++r) {
+        double2 mv = make_double2(0.0, 0.0);
+        for (int c = 0; c < nb; ++c) cfma(mv, dD[r + nb * c], Vq[c + nb * s]);
+        cfma_cj(acc, Vq[r + nb * s], mv);
+      }
+      vel[p] = acc.x / (2.0 * e) * Ryd2radTHz;
+    }
+  }
+  e *= Ryd2eV;
+  bool gamma = qp ? (qp[q] == 0) : (qv[q] == 0.0 && qv[q + nq] == 0.0 && qv[q + 2 * nq] == 0.0);
+  if (gamma) {
+    if (s < 3) e = 0.0;
+    vel[0] = vel[1] = vel[2] = 0.0;
+  }
+  if (e < -0.005) atomicOr(err, DERR_NEG_PHONON);
+  else if (e < 0.0 && e > -0.005) e = 0.0;
+  if (energies_f) energies_f[q + (int64_t)nq * s] = e;
+  if (om_i) om_i[(size_t)q * nb + s] = e;
+  if (evecs_f)
+    for (int c = 0; c < nb; ++c) evecs_f[q + (int64_t)nq * (s + (int64_t)nb * c)] = Vq[c + nb * s];
+  if (u_i || u_f)
+    for (int c = 0; c < nb; ++c) {
+      // u(ip) = ph_evec(ip)/sqrt(mass) (wannier.f90:937-942)
+      double2 u = make_double2(Vq[c + nb * s].x / sqrt(masses[c / 3]), Vq[c + nb * s].y / sqrt(masses[c / 3]));
+      if (u_i) u_i[((size_t)q * nb + s) * nb + c] = u;
+      if (u_f) u_f[((size_t)q * nb + s) * nb + c] = make_float2((float)u.x, (float)u.y);
+    }
+  if (with_vel && vel_f)
+    for (int p = 0; p < 3; ++p) vel_f[q + (int64_t)nq * (s + (int64_t)nb * p)] = vel[p];
+}
+
+void launch_ph_post(int nq, int nb, const int *qp, const double *qv, const double *w,
+                    const double2 *V, const double2 *dDq, int with_vel, const double *masses,
+                    double *energies_f, double2 *evecs_f, double *vel_f, double *om_i,
+                    double2 *u_i, float2 *u_f, int *err, cudaStream_t st) {
+  int n = nq * nb;
+  if (n == 0) return;
+  k_ph_post<<<(n + 127) / 128, 128, 0, st>>>(nq, nb, qp, qv, w, V, dDq, with_vel, masses,
+                                             energies_f, evecs_f, vel_f, om_i, u_i, u_f, err);
+}
+
+// ======================================================= g(Re,Rp) layouts
+// epmatwp order (i, j, Re, s, Rp) -> stage-A matrix G[Re][n], n = i + nw*(j + nw*(s + nb*Rp)),
+// so that one row of the GEMM output is gmixed(nw,nw,nb,nwsq) of gkRp (wannier.f90:1085).
+__global__ void k_permute_gwann(int nw, int nb, int nwsk, int nwsg, const double2 *raw,
+                                double2 *G) {
+  const int64_t Nn = (int64_t)nw * nw * nb * nwsg;
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= Nn * nwsk) return;
+  int64_t re = idx / Nn, n = idx % Nn;
+  int64_t nn = (int64_t)nw * nw;
+  int64_t ij = n % nn, s = (n / nn) % nb, rp = n / (nn * nb);
+  G[idx] = raw[ij + nn * (re + (int64_t)nwsk * (s + (int64_t)nb * rp))];
+}
+
+void launch_permute_gwann(int nw, int nb, int nwsk, int nwsg, const double2 *raw, double2 *G,
+                          cudaStream_t st) {
+  int64_t n = (int64_t)nw * nw * nb * nwsg * nwsk;
+  k_permute_gwann<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nw, nb, nwsk, nwsg, raw, G);
+}
+
+// ================================================================ gReq
+__global__ void k_permute_greq(int nq, int nw, int nb, int nwsk, const double2 *in,
+                               double2 *out) {
+  int64_t per = (int64_t)nw * nw * nb * nwsk;
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= per * nq) return;
+  int64_t q = idx / per, r = idx % per;
+  // out (i, j, s, Re) <- in (i, j, Re, s)
+  int64_t ij = r % ((int64_t)nw * nw);
+  int64_t rest = r / ((int64_t)nw * nw);
+  int64_t s = rest % nb, re = rest / nb;
+  out[q * per + r] = in[q * per + ij + (int64_t)nw * nw * (re + (int64_t)nwsk * s)];
+}
+
+void launch_permute_greq(int nq, int nw, int nb, int nwsk, const double2 *in, double2 *out,
+                         cudaStream_t st) {
+  int64_t n = (int64_t)nq * nw * nw * nb * nwsk;
+  if (n == 0) return;
+  k_permute_greq<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nq, nw, nb, nwsk, in, out);
+}
+
+// ============================================================= g2 batch
+// One warp per vertex: the reference's g2 (wannier.f90:903-1011, non-polar).
+__global__ void k_g2_batch(int nv, int nw, int nb, int nws, const double *qv, const int *R,
+                           const double *deg, const double2 *ek, const double2 *ekp,
+                           const double2 *eq, const double *ph_en, const double *masses,
+                           const double2 *gm, const int64_t *gm_index, int64_t gm_stride,
+                           double *g2) {
+  const int lane = threadIdx.x & 31;
+  const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (v >= nv) return;
+  double en = ph_en[v];
+  if (en == 0.0) { if (lane == 0) g2[v] = 0.0; return; }
+  const double2 *g = gm + (gm_index[v] - 1) * gm_stride;
+  double2 gb = make_double2(0.0, 0.0);
+  for (int iws = lane; iws < nws; iws += 32) {
+    double2 ukgu = make_double2(0.0, 0.0);
+    for (int sp = 0; sp < nb; ++sp) {
+      double2 caux = make_double2(0.0, 0.0);
+      for (int np = 0; np < nw; ++np) {
+        double2 ckp = ekp[v + (int64_t)nv * np];
+        for (int mp = 0; mp < nw; ++mp) {
+          // overlap(mp,np) = conj(U_k'(np)) * U_k(mp)
+          double2 ov = cmul(cconj(ckp), ek[v + (int64_t)nv * mp]);
+          cfma(caux, ov, g[np + nw * (mp + (int64_t)nw * (sp + (int64_t)nb * iws))]);
+        }
+      }
+      double2 u = eq[v + (int64_t)nv * sp];
+      u = make_double2(u.x / sqrt(masses[sp / 3]), u.y / sqrt(masses[sp / 3]));
+      cfma(ukgu, u, caux);
+    }
+    double dot = qv[v] * (double)R[3 * iws];
+    dot += qv[v + nv] * (double)R[3 * iws + 1];
+    dot += qv[v + 2 * (int64_t)nv] * (double)R[3 * iws + 2];
+    double2 ph;
+    sincos(TWOPI * dot, &ph.y, &ph.x);
+    ph.x /= deg[iws];
+    ph.y /= deg[iws];
+    cfma(gb, ph, ukgu);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gb.x += __shfl_xor_sync(0xffffffffu, gb.x, o);
+    gb.y += __shfl_xor_sync(0xffffffffu, gb.y, o);
+  }
+  if (lane == 0) g2[v] = 0.5 * (gb.x * gb.x + gb.y * gb.y) / en * g2unitfactor;
+}
+
+void launch_g2_batch(int nv, int nw, int nb, int nws, const double *qv, const int *R,
+                     const double *deg, const double2 *ek, const double2 *ekp,
+                     const double2 *eq, const double *ph_en, const double *masses,
+                     const double2 *gm, const int64_t *gm_index, int64_t gm_stride,
+                     double *g2, cudaStream_t st) {
+  if (nv <= 0) return;
+  k_g2_batch<<<(nv + 3) / 4, 128, 0, st>>>(nv, nw, nb, nws, qv, R, deg, ek, ekp, eq, ph_en,
+                                           masses, gm, gm_index, gm_stride, g2);
+}
+
+// ============================================================ q indices
+// q = k' - k folded onto the mesh, on integers (vector.f90:86-102 computes the
+// same through fractional coordinates and nint).
+__global__ void k_kq_index(int m1, int m2, int m3, int nk, const int64_t *k_idx, int nkp,
+                           const int64_t *kp_idx, int64_t *q_idx, int *err) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nk * nkp) return;
+  int i = (int)(idx % nk), j = (int)(idx / nk);
+  int64_t N = (int64_t)m1 * m2 * m3;
+  int64_t a = k_idx[i] - 1, b = kp_idx[j] - 1;
+  if (a < 0 || a >= N || b < 0 || b >= N) { atomicOr(err, DERR_INDEX); q_idx[idx] = -1; return; }
+  int64_t a1 = a % m1, a2 = (a / m1) % m2, a3 = a / ((int64_t)m1 * m2);
+  int64_t b1 = b % m1, b2 = (b / m1) % m2, b3 = b / ((int64_t)m1 * m2);
+  int64_t q1 = floormod(b1 - a1, m1), q2 = floormod(b2 - a2, m2), q3 = floormod(b3 - a3, m3);
+  q_idx[idx] = (q3 * m2 + q2) * m1 + q1 + 1;   // mux_vector base 0 (misc.f90:906)
+}
+
+void launch_kq_index(const int mesh[3], int nk, const int64_t *k_idx, int nkp,
+                     const int64_t *kp_idx, int64_t *q_idx, int *err, cudaStream_t st) {
+  int64_t n = (int64_t)nk * nkp;
+  if (n == 0) return;
+  k_kq_index<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(mesh[0], mesh[1], mesh[2], nk, k_idx,
+                                                          nkp, kp_idx, q_idx, err);
+}
+
+// ======================================================= rate pipeline
+__global__ void k_window_flags(int N, int nw, const double *ens, double enref, double fsthick,
+                               int *flag) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  int in = 0;
+  for (int b = 0; b < nw; ++b) in |= fabs(ens[(size_t)p * nw + b] - enref) <= fsthick;
+  flag[p] = in;     // apply_energy_window, electron.f90:613-621
+}
+
+void launch_window_flags(int N, int nw, const double *ens, double enref, double fsthick,
+                         int *flag, cudaStream_t st) {
+  k_window_flags<<<(N + 255) / 256, 256, 0, st>>>(N, nw, ens, enref, fsthick, flag);
+}
+
+__global__ void k_state_flags(int nwv, int nw, const int *widx, const double *ens, double enref,
+                              double fsthick, int *flag, int *nin_k) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nwv) return;
+  int p = widx[i], c = 0;
+  for (int m = 0; m < nw; ++m) {
+    int f = fabs(ens[(size_t)p * nw + m] - enref) <= fsthick;
+    flag[(size_t)i * nw + m] = f;
+    c += f;
+  }
+  nin_k[i] = c;
+}
+
+void launch_state_flags(int nwv, int nw, const int *widx, const double *ens, double enref,
+                        double fsthick, int *flag, int *nin_k, cudaStream_t st) {
+  k_state_flags<<<(nwv + 255) / 256, 256, 0, st>>>(nwv, nw, widx, ens, enref, fsthick, flag,
+                                                    nin_k);
+}
+
+__global__ void k_iota(int n, int *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
+}
+void launch_iota(int n, int *out, cudaStream_t st) {
+  if (n > 0) k_iota<<<(n + 255) / 256, 256, 0, st>>>(n, out);
+}
+
+// Stage A rotation over the initial band (the U_k half of wannier.f90:960-978),
+// with the k-half of the Rp phase, conj(e^{2 pi i k.Rp})/phwsdeg(Rp), folded in
+// so that the Rp Fourier of all states is one GEMM against e^{2 pi i k'.Rp}.
+__global__ void k_rotate_states_fp64(int j0, int j1, int i0, const int *st_code, int nw, int nb,
+                                     int nws, const int *widx, const double2 *U,
+                                     const double2 *gk, int64_t ldgk, int m1, int m2, int m3,
+                                     int L, const double2 *roots, const int *Rq,
+                                     const double *degq, double2 *B, int64_t ldb) {
+  const int j = j0 + blockIdx.y;
+  const int rp = blockIdx.x;
+  if (j >= j1) return;
+  const int code = st_code[j];
+  const int i = code / nw, m = code % nw;
+  const int p = widx[i];
+  const int mesh[3] = {m1, m2, m3};
+  double2 ph = roots[phase_index(p, mesh, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
+  ph = make_double2(ph.x / degq[rp], -ph.y / degq[rp]);
+  const double2 *Uk = U + ((size_t)p * nw + m) * nw;
+  const double2 *g = gk + (int64_t)(i - i0) * ldgk;
+  const int ncol = nw * nb;
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+    int np = c % nw, s = c / nw;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int mp = 0; mp < nw; ++mp)
+      cfma(acc, Uk[mp], g[np + nw * (mp + (int64_t)nw * (s + (int64_t)nb * rp))]);
+    B[(int64_t)rp * ldb + (int64_t)(j - j0) * ncol + c] = cmul(ph, acc);
+  }
+}
+
+void launch_rotate_states_fp64(int j0, int j1, int i0, const int *st_code, int nw, int nb,
+                               int nws, const int *widx, const double2 *U, const double2 *gk,
+                               int64_t ldgk, const int mesh[3], int L, const double2 *roots,
+                               const int *Rq, const double *degq, double2 *B, int64_t ldb,
+                               cudaStream_t st) {
+  if (j1 <= j0) return;
+  dim3 grid(nws, j1 - j0);
+  k_rotate_states_fp64<<<grid, 64, 0, st>>>(j0, j1, i0, st_code, nw, nb, nws, widx, U, gk, ldgk,
+                                            mesh[0], mesh[1], mesh[2], L, roots, Rq, degq, B, ldb);
+}
+
+__global__ void k_bose(int n, const double *om, double T, double *bose) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double e = om[i];
+  // Bose = 1/expm1(e/kB/T) (misc.f90:992-999), zero for zero-energy phonons (interactions.f90:2287)
+  bose[i] = (e != 0.0) ? 1.0 / expm1(e / kB / T) : 0.0;
+}
+
+void launch_bose(int N, int nb, const double *om, double T, double *bose, cudaStream_t st) {
+  int n = N * nb;
+  k_bose<<<(n + 255) / 256, 256, 0, st>>>(n, om, T, bose);
+}
+
+// ----------------------------------------------------------- deltas
+__device__ inline double fermi(double e, double mu, double T) {
+  return 1.0 / (exp((e - mu) / kB / T) + 1.0);     // misc.f90:1001-1009
+}
+
+// delta_fn_triang, delta.f90:790-881 (ik 0-based window index, ib 0-based)
+__device__ double delta_triang(double e, int ik, int ib, const RateParams &rp, const EpiData &d) {
+  double acc = 0.0;
+  int num = d.scount[ik];
+  for (int itk = 0; itk < num; ++itk) {
+    int it = d.smap[((size_t)ik * d.maxc + itk) * 2] - 1;
+    int iv = d.smap[((size_t)ik * d.maxc + itk) * 2 + 1];
+    const double *ev = d.sevals + (((size_t)it * rp.nw + ib) * 3);
+    double e1 = ev[0], e2 = ev[1], e3 = ev[2];
+    bool c1 = e <= e1, c2 = e1 < e && e <= e2, c3 = e2 < e && e <= e3, c4 = e3 < e;
+    if (c1 || c4) continue;
+    double E12 = (e - e2) / (e1 - e2), E21 = (e - e1) / (e2 - e1), E13 = (e - e3) / (e1 - e3);
+    double E31 = (e - e1) / (e3 - e1), E23 = (e - e3) / (e2 - e3), E32 = (e - e2) / (e3 - e2);
+    double tmp = 0.0;
+    if (iv == 1) tmp = c2 ? E21 * (E12 + E13) / (e3 - e1) : (c3 ? E23 * E13 / (e3 - e1) : 0.0);
+    else if (iv == 2) tmp = c2 ? E21 * E21 / (e3 - e1) : (c3 ? E23 * E23 / (e3 - e1) : 0.0);
+    else if (iv == 3) tmp = c2 ? E21 * E31 / (e3 - e1) : (c3 ? E23 * (E31 + E32) / (e3 - e1) : 0.0);
+    acc += tmp;
+  }
+  if (acc < 1.0e-12) acc = 0.0;
+  return acc / (double)(2 * (int64_t)rp.N);
+}
+
+// delta_fn_tetra, delta.f90:61-225
+__device__ double delta_tetra(double e, int ik, int ib, const RateParams &rp, const EpiData &d) {
+  double acc = 0.0, tmp = 0.0;
+  int num = d.scount[ik];
+  for (int itk = 0; itk < num; ++itk) {
+    int it = d.smap[((size_t)ik * d.maxc + itk) * 2] - 1;
+    int iv = d.smap[((size_t)ik * d.maxc + itk) * 2 + 1];
+    const double *ev = d.sevals + (((size_t)it * rp.nw + ib) * 4);
+    double e1 = ev[0], e2 = ev[1], e3 = ev[2], e4 = ev[3];
+    double e1e = e1 - e, e2e = e2 - e, e3e = e3 - e, e4e = e4 - e;
+    double e21 = e2 - e1, e31 = e3 - e1, e41 = e4 - e1, e32 = e3 - e2, e42 = e4 - e2, e43 = e4 - e3;
+    bool c1 = e1 <= e && e <= e2, c2 = e2 <= e && e <= e3, c3 = e3 <= e && e <= e4;
+    if (e < e1 || e > e4) continue;
+    switch (iv) {
+      case 1:
+        if (c1) { tmp = (e2e / e21 + e3e / e31 + e4e / e41) * (e1e * e1e) / e41 / e31 / e21; if (e1 == e2) tmp = 0.0; }
+        else if (c2) {
+          tmp = -0.5 * (e3e / (e31 * e31) * (e3e * e2e / e42 / e32 + e4e * e1e / e41 / e42 + e3e * e1e / e32 / e41) +
+                        e4e / (e41 * e41) * (e4e * e1e / e42 / e31 + e4e * e2e / e42 / e32 + e3e * e1e / e31 / e32));
+          if (e2 == e3) tmp = -0.5 * (e4e * e1e / e41 / e42 + e1e / e41 + e4e / (e41 * e41) * (e4e * e1e / e42 / e31 + e4e / e42 + e1e / e31));
+        } else if (c3) { tmp = (e4e * e4e * e4e) / (e41 * e41) / e42 / e43; if (e3 == e4) tmp = (e4e * e4e) / (e41 * e41) / e42; }
+        break;
+      case 2:
+        if (c1) { tmp = -(e1e * e1e * e1e) / (e21 * e21) / e31 / e41; if (e1 == e2) tmp = 0.0; }
+        else if (c2) {
+          tmp = -0.5 * (e3e / (e32 * e32) * (e3e * e2e / e42 / e31 + e4e * e2e / e42 / e41 + e3e * e1e / e31 / e41) +
+                        e4e / (e42 * e42) * (e3e * e2e / e32 / e31 + e4e * e1e / e41 / e31 + e4e * e2e / e32 / e41));
+          if (e2 == e3) tmp = -0.5 * (0.0 + e4e / e42 / e41 + 0.0 + e4e / (e42 * e42) * (0.0 + e4e * e1e / e41 / e31 + 1.0));
+        } else if (c3) { tmp = (e4e * e4e * e4e) / e41 / (e42 * e42) / e43; if (e3 == e4) tmp = 0.0; }
+        break;
+      case 3:
+        if (c1) { tmp = -(e1e * e1e * e1e) / e21 / (e31 * e31) / e41; if (e1 == e2) tmp = 0.0; }
+        else if (c2) {
+          tmp = 0.5 * (e2e / (e32 * e32) * (e3e * e2e / e42 / e31 + e4e * e2e / e42 / e41 + e3e * e1e / e31 / e41) +
+                       e1e / (e31 * e31) * (e3e * e2e / e42 / e32 + e4e * e1e / e41 / e42 + e3e * e1e / e32 / e41));
+          if (e2 == e3) tmp = 0.5 * (0.0 + e4e / e42 / e41 + e1e / e31 / e41 + e1e / (e31 * e31) * (0.0 + e4e * e1e / e41 / e42 + e1e / e41));
+        } else if (c3) { tmp = (e4e * e4e * e4e) / e41 / e42 / (e43 * e43); if (e3 == e4) tmp = 0.0; }
+        break;
+      case 4:
+        if (c1) { tmp = -(e1e * e1e * e1e) / e21 / e31 / (e41 * e41); if (e1 == e2) tmp = 0.0; }
+        else if (c2) {
+          tmp = 0.5 * (e2e / (e42 * e42) * (e3e * e2e / e32 / e31 + e4e * e1e / e41 / e31 + e4e * e2e / e32 / e41) +
+                       e1e / (e41 * e41) * (e4e * e1e / e42 / e31 + e4e * e2e / e42 / e32 + e3e * e1e / e31 / e32));
+          if (e2 == e3) tmp = 0.5 * (0.0 + e1e / (e41 * e41) * (e4e * e1e / e42 / e31 + e4e / e42 + e1e / e31));
+        } else if (c3) { tmp = -(e3e / e43 + e2e / e42 + e1e / e41) * (e4e * e4e) / e41 / e42 / e43; if (e3 == e4) tmp = 0.0; }
+        break;
+    }
+    if (e1 == e2 && e1 == e3 && e1 == e4 && e == e1) tmp = 0.25;
+    acc += tmp;
+  }
+  if (acc < 1.0e-12) acc = 0.0;
+  return acc / (double)(6 * (int64_t)rp.N);
+}
+
+__device__ inline double delta_eval(double e, int ikp, int n, double eps_kn, const RateParams &rp,
+                                    const EpiData &d) {
+  if (rp.delta_kind == 0) {
+    double x = (e - eps_kn) / rp.sigma;
+    return (1.0 / sqrt(TWOPI)) / rp.sigma * exp(-0.5 * x * x) * rp.inv_nk;
+  }
+  if (rp.delta_kind == 1) return delta_triang(e, ikp, n, rp, d);
+  return delta_tetra(e, ikp, n, rp, d);
+}
+
+// Per (k', initial state) epilogue: the k' rotation, the phonon mix, |g|^2
+// (wannier.f90:937-1009), X+- (interactions.f90:2278-2332, 2353) and the
+// per-pair partial of the RTA rate (interactions.f90:3012-3034).
+// Gv(x) returns the complex Rp-Fourier sum G(n' + nw*s') of the pair.
+template <typename GV>
+__device__ void pair_epilogue(int ip, int j, GV Gv, const RateParams &rp, const EpiData &d,
+                              double &out) {
+  const int nw = rp.nw, nb = rp.nb;
+  const int code = d.st_code[j];
+  const int i = code / nw, m = code % nw;
+  const int p = d.widx[i], pp = d.widx[ip];
+  const double E = d.ens[(size_t)p * nw + m];
+  int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
+  int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+  int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+  double acc = 0.0;
+  int rank_n = 0;
+  for (int n = 0; n < nw; ++n) {
+    double eps = d.ens[(size_t)pp * nw + n];
+    if (fabs(eps - rp.enref) > rp.fsthick) continue;
+    const double2 *Ukp = d.U + ((size_t)pp * nw + n) * nw;
+    double2 h[32];
+    for (int s = 0; s < nb; ++s) {
+      double2 a = make_double2(0.0, 0.0);
+      for (int np = 0; np < nw; ++np) cfma_cj(a, Ukp[np], Gv(np + nw * s));
+      h[s] = a;
+    }
+    for (int s = 0; s < nb; ++s) {
+      double om = d.om[(size_t)q * nb + s];
+      double2 gsum = make_double2(0.0, 0.0);
+      const double2 *u = d.u + ((size_t)q * nb + s) * nb;
+      for (int sp = 0; sp < nb; ++sp) cfma(gsum, u[sp], h[sp]);
+      double g2 = (om == 0.0) ? 0.0 : 0.5 * (gsum.x * gsum.x + gsum.y * gsum.y) / om * g2unitfactor;
+      double bose = d.bose[(size_t)q * nb + s];
+      double xp = 0.0, xm = 0.0;
+      if (om >= 0.5e-3) {
+        double fp = fermi(E + om, rp.chempot, rp.T);
+        double fm = fermi(E - om, rp.chempot, rp.T);
+        double dp = delta_eval(E + om, ip, n, eps, rp, d);
+        double dm = delta_eval(E - om, ip, n, eps, rp, d);
+        xp = rp.const_tp * (g2 * (bose + fp) * dp);
+        xm = rp.const_tp * (g2 * (1.0 + bose - fm) * dm);
+      }
+      acc += xp + xm;
+      if (d.g2) {
+        int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
+        if (off < d.cap) {
+          d.g2[off] = g2;
+          if (d.xp) d.xp[off] = xp;
+          if (d.xm) d.xm[off] = xm;
+        }
+      }
+    }
+    rank_n++;
+  }
+  out = acc;
+}
+
+// Block-deterministic partial: threads along k' for one state, then a fixed
+// order compensated (Neumaier) sum by thread 0.
+__device__ void block_partial(double v, double *partial, int j, int nblk) {
+  __shared__ double sv[128];
+  sv[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, c = 0.0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      double x = sv[t], tt = s + x;
+      c += (fabs(s) >= fabs(x)) ? (s - tt) + x : (x - tt) + s;
+      s = tt;
+    }
+    partial[(size_t)j * nblk + blockIdx.x] = s + c;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_epilogue_fp64(int nwv, int j0, const double2 *C,
+                                                       int64_t ldc, RateParams rp, EpiData d,
+                                                       double *partial, int nblk) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = j0 + blockIdx.y;
+  const int ncol = rp.nw * rp.nb;
+  double v = 0.0;
+  if (ip < nwv) {
+    const double2 *row = C + (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    pair_epilogue(ip, j, [&](int x) { return row[x]; }, rp, d, v);
+  }
+  block_partial(v, partial, j, nblk);
+}
+
+void launch_epilogue_fp64(int nwv, int j0, int j1, const double2 *C, int64_t ldc,
+                          const RateParams &rp, const EpiData &d, double *partial, int nblk,
+                          cudaStream_t st) {
+  if (j1 <= j0) return;
+  dim3 grid(nblk, j1 - j0);
+  k_epilogue_fp64<<<grid, 128, 0, st>>>(nwv, j0, C, ldc, rp, d, partial, nblk);
+}
+
+__global__ void __launch_bounds__(128) k_epilogue_fp32(int nwv, int j0, const float *Cr,
+                                                       const float *Ci, int64_t ldc,
+                                                       RateParams rp, EpiData d,
+                                                       double *partial, int nblk) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = j0 + blockIdx.y;
+  const int ncol = rp.nw * rp.nb;
+  double v = 0.0;
+  if (ip < nwv) {
+    const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    pair_epilogue(ip, j, [&](int x) { return make_double2((double)Cr[base + x], (double)Ci[base + x]); },
+                  rp, d, v);
+  }
+  block_partial(v, partial, j, nblk);
+}
+
+void launch_epilogue_fp32(int nwv, int j0, int j1, const float *Cr, const float *Ci,
+                          int64_t ldc, const RateParams &rp, const EpiData &d, double *partial,
+                          int nblk, cudaStream_t st) {
+  if (j1 <= j0) return;
+  dim3 grid(nblk, j1 - j0);
+  k_epilogue_fp32<<<grid, 128, 0, st>>>(nwv, j0, Cr, Ci, ldc, rp, d, partial, nblk);
+}
+
+// rates(ik, m) = compensated sum of the block partials in block order
+__global__ void k_rate_final(int nst, int nblk, const double *partial, const int *st_code, int nw,
+                             int N, double *rates_f) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nst) return;
+  double s = 0.0, c = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    double x = partial[(size_t)j * nblk + b], t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  int code = st_code[j];
+  rates_f[(code / nw) + (int64_t)N * (code % nw)] = s + c;
+}
+
+void launch_rate_final(int nst, int nblk, const double *partial, const int *st_code, int nw,
+                       int N, double *rates_f, cudaStream_t st) {
+  if (nst <= 0) return;
+  k_rate_final<<<(nst + 127) / 128, 128, 0, st>>>(nst, nblk, partial, st_code, nw, N, rates_f);
+}
+
+}  // namespace ephg

@@ -1,0 +1,155 @@
+/*
+ * ephg.h - C ABI of the GB300 (sm_103a) e-ph vertex library.
+ *
+ * Drop-in for elphbolt's Wannier-interpolation procedures and the electron
+ * e-ph rate drivers, callable from Fortran through ISO_C_BINDING (see
+ * INTEGRATION.md for the bind(C) interfaces).  Every entry point names the
+ * reference procedure it replaces.
+ *
+ * Conventions
+ *  - Arrays are caller-owned, Fortran column-major, with the reference's
+ *    shapes; complex(r64) arrays are interleaved (re, im) doubles.
+ *  - Sizes are int64_t; integer indices that the reference keeps 1-based
+ *    (muxed wave-vector indices, band indices) stay 1-based.
+ *  - Every call returns EPHG_OK (0) or an error code; ephg_last_error() gives
+ *    the message of the calling thread's last failure.  Where the reference
+ *    stops the program (exit_with_message, src/misc.f90:194-203) the library
+ *    returns the matching code instead.
+ *  - The handle owns all device memory; one handle per host thread.
+ */
+#ifndef EPHG_H
+#define EPHG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EPHG_OK 0
+#define EPHG_ERR_ARG 1            /* invalid argument */
+#define EPHG_ERR_CUDA 2           /* CUDA runtime error or no device */
+#define EPHG_ERR_NEG_PHONON 3     /* "Large negative phonon energy found!" wannier.f90:775 */
+#define EPHG_ERR_EMPTY_WINDOW 4   /* "No states found within Fermi window." electron.f90:627 */
+#define EPHG_ERR_EIG 5            /* Jacobi eigensolver did not converge */
+#define EPHG_ERR_NOMEM 6          /* device memory budget exceeded */
+#define EPHG_ERR_TIMEOUT 7        /* a bounded device wait gave up */
+#define EPHG_ERR_INDEX 8          /* device-side index check failed */
+
+#define EPHG_PREC_FP64 0          /* plain FP64 drop-in */
+#define EPHG_PREC_SPLIT_TF32 1    /* 3xTF32 tcgen05 contractions, FP32 accumulate */
+
+#define EPHG_DELTA_GAUSSIAN 0     /* fixed-sigma Gaussian / N_k */
+#define EPHG_DELTA_TRIANGLE 1     /* delta_fn_triang, src/delta.f90:790 */
+#define EPHG_DELTA_TETRA 2        /* delta_fn_tetra,  src/delta.f90:61 */
+
+#define EPHG_WANNSPACE_EL 0
+#define EPHG_WANNSPACE_PH 1
+
+typedef struct ephg_handle ephg_handle;
+
+/* Real-space Wannier data: the fields of type Wannier (src/wannier.f90:46-93)
+ * plus the crystal data the path reads (src/crystal.f90). */
+typedef struct {
+  int64_t numwannbands;       /* nw */
+  int64_t numbranches;        /* nb = 3 * numatoms */
+  int64_t nwsk, nwsq, nwsg;   /* WS cell counts; nwsg must equal nwsq (wannier.f90:947) */
+  int64_t numatoms;
+  int64_t coarse_qmesh[3];
+  const double *lattvecs;     /* (3,3) nm, columns a1 a2 a3 */
+  const double *basis;        /* (3,numatoms) crystal coordinates */
+  const double *masses;       /* (numatoms) amu, masses(atomtypes(i)) */
+  const int64_t *rcells_k;    /* (nwsk,3) */
+  const int64_t *rcells_q;    /* (nwsq,3) */
+  const int64_t *rcells_g;    /* (nwsg,3) */
+  const int64_t *elwsdeg;     /* (nwsk) */
+  const int64_t *phwsdeg;     /* (nwsq) */
+  const int64_t *gwsdeg;      /* (nwsg) */
+  const double *Hwann;        /* complex (nwsk,nw,nw), Ry */
+  const double *Dphwann;      /* complex (nwsq,nb,nb), Ry/bohr^2 */
+  const double *gwann;        /* complex (nw,nw,nwsk,nb,nwsg), Ry/bohr, epmatwp order */
+} ephg_wannier_desc;
+
+/* One electron RTA-rate request (the numerics/electron settings the
+ * ibzk driver reads: mesh, enref, fsthick, chempot, T, delta method). */
+typedef struct {
+  int64_t mesh[3];            /* electron mesh = phonon mesh (mesh_ref = 1) */
+  double enref;               /* eV, window centre */
+  double fsthick;             /* eV, window half width */
+  double chempot;             /* eV */
+  double T;                   /* K */
+  int64_t delta_kind;         /* EPHG_DELTA_* */
+  double sigma;               /* eV, Gaussian width */
+  int64_t precision;          /* EPHG_PREC_* */
+} ephg_rate_request;
+
+typedef struct {
+  int64_t nwv;                /* window k-points (FBZ blocks = IBZ blocks) */
+  int64_t nstates_inwindow;   /* window (k', n) final states */
+  int64_t nstates;            /* window initial states (k, m) */
+  int64_t vertices;           /* |g|^2 vertices, the count of interactions.f90:2261 */
+  int64_t pairs;              /* (initial state, k') pairs */
+  int64_t kernel_launches;    /* library kernels launched by the call */
+  double ms_setup;            /* H(k), D(q), eigensolves, window, tables */
+  double ms_stage_a;          /* g(Re,Rp) -> g(k,Rp) and the initial-band rotation */
+  double ms_stage_bc;         /* Rp Fourier + rotations + |g|^2 + delta + rates */
+  double ms_total;            /* device time of the whole call */
+  double stage_b_gflop;       /* algorithmic GFLOP of the Rp Fourier contraction */
+  double stage_a_gflop;       /* algorithmic GFLOP of the Re contraction */
+} ephg_rate_stats;
+
+/* Upload the Wannier data once; the returned handle keeps it resident in HBM
+ * (replaces Wannier%read, wannier.f90:97-140, and read_EPW_Wannier :289). */
+int ephg_create(const ephg_wannier_desc *desc, ephg_handle **out);
+int ephg_destroy(ephg_handle *h);
+const char *ephg_last_error(void);
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int ephg_device_count(void);
+
+/* el_wann (wannier.f90:430-524): kvecs (nk,3) crystal coords -> energies
+ * (nk,nw) eV; optional velocities (nk,nw,3) km/s, evecs (nk,nw,nw) with
+ * evecs(k,b,:) the eigenvector of band b, scissor (nw) eV.  NULL = absent. */
+int ephg_el_wann(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
+                 double *velocities, double *evecs, const double *scissor);
+
+/* ph_wann, non-polar (wannier.f90:585-782): qvecs (nq,3) -> energies (nq,nb) eV,
+ * optional evecs (nq,nb,nb) with evecs(q,s,:) the eigenvector of mode s,
+ * velocities (nq,nb,3) km/s.  Returns EPHG_ERR_NEG_PHONON where the reference stops. */
+int ephg_ph_wann(ephg_handle *h, int64_t nq, const double *qvecs, double *energies,
+                 double *evecs, double *velocities);
+
+/* gkRp (wannier.f90:1073-1132), batched over k: gmixed (nw,nw,nb,nwsq,nk). */
+int ephg_gkRp(ephg_handle *h, int64_t nk, const double *kvecs, double *gmixed);
+
+/* gReq (wannier.f90:1134-1188), batched over q: gmixed (nw,nw,nb,nwsk,nq). */
+int ephg_gReq(ephg_handle *h, int64_t nq, const double *qvecs, double *gmixed);
+
+/* g2 (wannier.f90:903-1011, non-polar), batched over vertices.  Vertex v uses
+ * gmixed(:,:,:,:,gm_index(v)) (1-based) of the ngm blocks passed, with nws =
+ * nwsg cells for wannspace PH and nwsk for EL.  Arrays: kvecs, qvecs (nv,3);
+ * el_evec_k, el_evec_kp (nv,nw) complex; ph_evec_q (nv,nb) complex; ph_en (nv). */
+int ephg_g2(ephg_handle *h, int64_t wannspace, int64_t nv, const double *kvecs,
+            const double *qvecs, const double *el_evec_k, const double *el_evec_kp,
+            const double *ph_evec_q, const double *ph_en, int64_t ngm, const double *gmixed,
+            const int64_t *gm_index, double *g2_out);
+
+/* vector_allreps_sub (src/vector.f90:86-102) batched on the device:
+ * q(i,j) = muxed index of k'(j) - k(i) folded onto the mesh, all 1-based.
+ * k_idx (nk), kp_idx (nkp) muxed indices; q_idx (nk,nkp). */
+int ephg_kq_index(ephg_handle *h, const int64_t mesh[3], int64_t nk, const int64_t *k_idx,
+                  int64_t nkp, const int64_t *kp_idx, int64_t *q_idx);
+
+/* calculate_eph_interaction_ibzk 'g' + 'X' (interactions.f90:2095-2400) fused
+ * with calculate_el_rta_rates (interactions.f90:2958-3063), identity point
+ * group, q mesh = k mesh, no disk.  rates (N_k,nw) column-major with the first
+ * stats.nwv rows valid (window k order = indexlist order); indexlist (N_k)
+ * receives the window's muxed indices.  Optional per-vertex outputs in the
+ * reference's order (initial state, k', n, s) with capacity cap: g2 (eV^2),
+ * xplus, xminus (THz).  stats may be NULL. */
+int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
+                  int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus,
+                  double *xminus, int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

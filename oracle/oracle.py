@@ -1,0 +1,277 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+may import this module; it is the checker for the CUDA library, never part of
+the product path.  See ``ephg_oracle.h`` for the reference functions it
+restates and its parity status.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libephg_oracle.so")
+_lib = None
+
+c_i64p = ct.POINTER(ct.c_int64)
+c_dp = ct.POINTER(ct.c_double)
+
+
+class OrWannier(ct.Structure):
+    _fields_ = [("nw", ct.c_int64), ("nb", ct.c_int64), ("nwsk", ct.c_int64),
+                ("nwsq", ct.c_int64), ("nwsg", ct.c_int64), ("natoms", ct.c_int64),
+                ("coarse_qmesh", ct.c_int64 * 3),
+                ("lattvecs", c_dp), ("basis", c_dp), ("masses", c_dp),
+                ("rcells_k", c_i64p), ("rcells_q", c_i64p), ("rcells_g", c_i64p),
+                ("elwsdeg", c_i64p), ("phwsdeg", c_i64p), ("gwsdeg", c_i64p),
+                ("Hwann", c_dp), ("Dphwann", c_dp), ("gwann", c_dp)]
+
+
+class OrRequest(ct.Structure):
+    _fields_ = [("mesh", ct.c_int64 * 3), ("enref", ct.c_double), ("fsthick", ct.c_double),
+                ("chempot", ct.c_double), ("T", ct.c_double), ("delta_kind", ct.c_int64),
+                ("sigma", ct.c_double)]
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ct.CDLL(_LIB_PATH)
+        L.or_mux_vector.restype = ct.c_int64
+        L.or_mux_state.restype = ct.c_int64
+        L.or_binsearch.restype = ct.c_int64
+        L.or_expm1.restype = ct.c_double
+        L.or_expm1.argtypes = [ct.c_double]
+        L.or_Bose.restype = ct.c_double
+        L.or_Bose.argtypes = [ct.c_double, ct.c_double]
+        L.or_Fermi.restype = ct.c_double
+        L.or_Fermi.argtypes = [ct.c_double, ct.c_double, ct.c_double]
+        L.or_g2.restype = ct.c_double
+        L.or_g2.argtypes = [ct.c_void_p, c_dp, c_dp, c_dp, c_dp, c_dp, ct.c_double, c_dp, ct.c_int]
+        L.or_delta_triang.restype = ct.c_double
+        L.or_delta_tetra.restype = ct.c_double
+        _lib = L
+    return _lib
+
+
+def _p(a, t=c_dp):
+    return a.ctypes.data_as(t)
+
+
+def _f64(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def _c128_view(a):
+    a = np.asfortranarray(np.asarray(a, dtype=np.complex128))
+    return a
+
+
+class Wannier:
+    """Oracle-side holder of one synthetic Wannier data set."""
+
+    def __init__(self, wd):
+        self.wd = wd
+        c = wd.crystal
+        self._keep = []
+
+        def keep(a):
+            self._keep.append(a)
+            return a
+
+        self.lattvecs = keep(_f64(c.lattvecs))
+        self.basis = keep(_f64(c.basis))
+        self.masses = keep(_f64(c.masses))
+        self.rk = keep(np.asfortranarray(wd.rcells_k, dtype=np.int64))
+        self.rq = keep(np.asfortranarray(wd.rcells_q, dtype=np.int64))
+        self.rg = keep(np.asfortranarray(wd.rcells_g, dtype=np.int64))
+        self.dk = keep(np.ascontiguousarray(wd.elwsdeg, dtype=np.int64))
+        self.dq = keep(np.ascontiguousarray(wd.phwsdeg, dtype=np.int64))
+        self.dg = keep(np.ascontiguousarray(wd.gwsdeg, dtype=np.int64))
+        self.H = keep(_c128_view(wd.Hwann))
+        self.D = keep(_c128_view(wd.Dphwann))
+        self.G = keep(_c128_view(wd.gwann))
+        s = OrWannier()
+        s.nw, s.nb = wd.numwannbands, wd.numbranches
+        s.nwsk, s.nwsq, s.nwsg = wd.nwsk, wd.nwsq, wd.nwsg
+        s.natoms = c.numatoms
+        for i in range(3):
+            s.coarse_qmesh[i] = int(wd.coarse_qmesh[i])
+        s.lattvecs, s.basis, s.masses = _p(self.lattvecs), _p(self.basis), _p(self.masses)
+        s.rcells_k, s.rcells_q, s.rcells_g = _p(self.rk, c_i64p), _p(self.rq, c_i64p), _p(self.rg, c_i64p)
+        s.elwsdeg, s.phwsdeg, s.gwsdeg = _p(self.dk, c_i64p), _p(self.dq, c_i64p), _p(self.dg, c_i64p)
+        s.Hwann, s.Dphwann, s.gwann = _p(self.H), _p(self.D), _p(self.G)
+        self.s = s
+        self.nw, self.nb = wd.numwannbands, wd.numbranches
+
+    # ---- wannier.f90 restatements ----
+    def el_wann(self, kvecs, evecs=True, velocities=False, scissor=None):
+        k = _f64(kvecs).reshape(-1, 3, order="F") if np.ndim(kvecs) == 2 else _f64(np.atleast_2d(kvecs))
+        nk = k.shape[0]
+        e = np.zeros((nk, self.nw), order="F")
+        v = np.zeros((nk, self.nw, self.nw), dtype=np.complex128, order="F") if evecs else None
+        vel = np.zeros((nk, self.nw, 3), order="F") if velocities else None
+        sc = _f64(scissor) if scissor is not None else None
+        lib().or_el_wann(ct.byref(self.s), ct.c_int64(nk), _p(k), _p(e),
+                         _p(v) if v is not None else None, _p(vel) if vel is not None else None,
+                         _p(sc) if sc is not None else None)
+        return e, v, vel
+
+    def ph_wann(self, qvecs, evecs=True, velocities=False):
+        q = _f64(np.atleast_2d(qvecs))
+        nq = q.shape[0]
+        e = np.zeros((nq, self.nb), order="F")
+        v = np.zeros((nq, self.nb, self.nb), dtype=np.complex128, order="F") if evecs else None
+        vel = np.zeros((nq, self.nb, 3), order="F") if velocities else None
+        st = lib().or_ph_wann(ct.byref(self.s), ct.c_int64(nq), _p(q), _p(e),
+                              _p(v) if v is not None else None, _p(vel) if vel is not None else None)
+        return e, v, vel, st
+
+    def gkRp(self, kvec):
+        out = np.zeros((self.nw, self.nw, self.nb, self.wd.nwsq), dtype=np.complex128, order="F")
+        k = np.ascontiguousarray(kvec, dtype=np.float64)
+        lib().or_gkRp(ct.byref(self.s), _p(k), _p(out))
+        return out
+
+    def gReq(self, qvec):
+        out = np.zeros((self.nw, self.nw, self.nb, self.wd.nwsk), dtype=np.complex128, order="F")
+        q = np.ascontiguousarray(qvec, dtype=np.float64)
+        lib().or_gReq(ct.byref(self.s), _p(q), _p(out))
+        return out
+
+    def g2(self, kvec, qvec, ev_k, ev_kp, ev_q, ph_en, gmixed, wannspace="ph"):
+        a = [np.ascontiguousarray(x) for x in (kvec, qvec)]
+        b = [np.ascontiguousarray(x, dtype=np.complex128) for x in (ev_k, ev_kp, ev_q)]
+        gm = np.asfortranarray(gmixed, dtype=np.complex128)
+        return lib().or_g2(ct.byref(self.s), _p(a[0]), _p(a[1]), _p(b[0]), _p(b[1]), _p(b[2]),
+                           float(ph_en), _p(gm), 1 if wannspace == "ph" else 0)
+
+    def el_rates(self, req, max_states=-1, nthreads=1, literal=True, vertices=False, cap=None):
+        """Full 'g' + 'X' + rates driver; returns a dict of results."""
+        r = OrRequest()
+        for i in range(3):
+            r.mesh[i] = int(req.mesh[i])
+        r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+        r.delta_kind, r.sigma = int(req.delta_kind), req.sigma
+        N = int(np.prod(req.mesh))
+        rates = np.zeros((N, self.nw), order="F")
+        idx = np.zeros(N, dtype=np.int64)
+        info = np.zeros(8, dtype=np.int64)
+        g2 = xp = xm = None
+        c = 0
+        if vertices:
+            c = int(cap) if cap is not None else N * self.nw * N * self.nw * self.nb
+            g2, xp, xm = (np.zeros(c) for _ in range(3))
+        st = lib().or_el_rates(ct.byref(self.s), ct.byref(r), ct.c_int64(max_states),
+                               ct.c_int(nthreads), ct.c_int(1 if literal else 0), _p(rates),
+                               _p(idx, c_i64p), _p(info, c_i64p),
+                               _p(g2) if g2 is not None else None,
+                               _p(xp) if xp is not None else None,
+                               _p(xm) if xm is not None else None, ct.c_int64(c))
+        nwv = int(info[0])
+        out = dict(status=int(st), nwv=nwv, nstates_inwindow=int(info[1]),
+                   nstates=int(info[2]), vertices=int(info[3]), pairs=int(info[4]),
+                   indexlist=idx[:nwv].copy(), rates=np.asfortranarray(rates[:nwv, :]))
+        if vertices:
+            nv = min(int(info[3]), c)
+            out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
+        return out
+
+
+# ---- misc.f90 / vector.f90 restatements ----
+def mux_vector(v, mesh, base):
+    a = (ct.c_int64 * 3)(*v)
+    m = (ct.c_int64 * 3)(*mesh)
+    return lib().or_mux_vector(a, m, ct.c_int64(base))
+
+
+def demux_vector(i, mesh, base):
+    v = (ct.c_int64 * 3)()
+    m = (ct.c_int64 * 3)(*mesh)
+    lib().or_demux_vector(ct.c_int64(i), v, m, ct.c_int64(base))
+    return list(v)
+
+
+def mux_state(nbands, iband, ik):
+    return lib().or_mux_state(ct.c_int64(nbands), ct.c_int64(iband), ct.c_int64(ik))
+
+
+def demux_state(m, nbands):
+    ib, ik = ct.c_int64(), ct.c_int64()
+    lib().or_demux_state(ct.c_int64(m), ct.c_int64(nbands), ct.byref(ib), ct.byref(ik))
+    return ib.value, ik.value
+
+
+def binsearch(array, e):
+    a = np.ascontiguousarray(array, dtype=np.int64)
+    return lib().or_binsearch(_p(a, c_i64p), ct.c_int64(len(a)), ct.c_int64(e))
+
+
+def umklapp(q1, q2):
+    a = np.ascontiguousarray(q1, dtype=np.float64)
+    b = np.ascontiguousarray(q2, dtype=np.float64)
+    c = np.zeros(3)
+    lib().or_umklapp(_p(a), _p(b), _p(c))
+    return c
+
+
+def vector_create(ind, grid, prim):
+    iv = (ct.c_int64 * 3)()
+    mx = ct.c_int64()
+    fr, ca = np.zeros(3), np.zeros(3)
+    g = (ct.c_int64 * 3)(*grid)
+    P = np.asfortranarray(prim, dtype=np.float64)
+    lib().or_vector_create(ct.c_int64(ind), g, _p(P), iv, ct.byref(mx), _p(fr), _p(ca))
+    return dict(int=list(iv), muxed=mx.value, frac=fr, cart=ca)
+
+
+def vector_addsub(ind1, ind2, sign, grid, prim):
+    iv = (ct.c_int64 * 3)()
+    mx = ct.c_int64()
+    fr, ca = np.zeros(3), np.zeros(3)
+    g = (ct.c_int64 * 3)(*grid)
+    P = np.asfortranarray(prim, dtype=np.float64)
+    lib().or_vector_addsub(ct.c_int64(ind1), ct.c_int64(ind2), ct.c_int(sign), g, _p(P), iv,
+                           ct.byref(mx), _p(fr), _p(ca))
+    return dict(int=list(iv), muxed=mx.value, frac=fr, cart=ca)
+
+
+def vector_change_grid(frac, grid):
+    iv = (ct.c_int64 * 3)()
+    mx = ct.c_int64()
+    f = np.ascontiguousarray(frac, dtype=np.float64)
+    g = (ct.c_int64 * 3)(*grid)
+    lib().or_vector_change_grid(_p(f), g, iv, ct.byref(mx))
+    return dict(int=list(iv), muxed=mx.value)
+
+
+def expm1(x):
+    return lib().or_expm1(float(x))
+
+
+def Bose(e, T):
+    return lib().or_Bose(float(e), float(T))
+
+
+def Fermi(e, mu, T):
+    return lib().or_Fermi(float(e), float(mu), float(T))
+
+
+def herm_eig(A):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    n = A.shape[0]
+    w = np.zeros(n)
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    sw = lib().or_herm_eig(ct.c_int64(n), _p(A), _p(w), _p(V))
+    return w, V, sw

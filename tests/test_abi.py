@@ -1,0 +1,59 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every symbol the
+header declares; without a GPU every entry point refuses loudly (no fallback)."""
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+import pytest
+
+from elphbolt_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "ephg.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(ephg_\w+)\s*\(", txt, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_header_symbols_exported(lib):
+    syms = header_symbols()
+    assert len(syms) >= 11
+    assert set(syms) == set(_lib.EXPORTS)
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_library_is_sm103a():
+    # the fatbin of the linked library was built with -gencode compute_103a/sm_103a only
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert os.path.exists(build.LIB)
+
+
+def test_no_device_refuses(lib):
+    if lib.ephg_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    from elphbolt_gb300 import synthetic as S
+    from elphbolt_gb300.wannier import Wannier
+    wd = S.make_wannier(S.make_crystal_si_like(), 4, supercell=(2, 2, 2), seed=1)
+    with pytest.raises(_lib.EphgError):
+        Wannier(wd)
+    h = ct.c_void_p()
+    d = _lib.WannierDesc()
+    rc = lib.ephg_create(ct.byref(d), ct.byref(h))
+    assert rc == _lib.EPHG_ERR_CUDA
+    assert b"no CUDA device" in lib.ephg_last_error()
+
+
+def test_null_arguments(lib):
+    assert lib.ephg_create(None, None) == _lib.EPHG_ERR_ARG
+    assert lib.ephg_el_wann(None, 1, None, None, None, None, None) == _lib.EPHG_ERR_ARG
+    assert lib.ephg_el_rates(None, None, None, None, None, None, None, None, 0) == _lib.EPHG_ERR_ARG
+    assert lib.ephg_destroy(None) == _lib.EPHG_OK

@@ -1,0 +1,112 @@
+"""Oracle self-checks and physical invariants (CPU only)."""
+import numpy as np
+import pytest
+
+from elphbolt_gb300 import synthetic as S
+from tests.cases import case, CASES
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_literal_vs_restructured(oracle_lib, name):
+    """Per-vertex g2 exactly as wannier.f90:903 vs Fourier-then-rotate: FP64 rounding only."""
+    wd, req = case(name)
+    W = oracle_lib.Wannier(wd)
+    a = W.el_rates(req, literal=True, vertices=True)
+    b = W.el_rates(req, literal=False, vertices=True)
+    assert a["vertices"] == b["vertices"] > 0
+    assert np.array_equal(a["indexlist"], b["indexlist"])
+    scale = np.abs(a["g2"]).max()
+    assert np.max(np.abs(a["g2"] - b["g2"])) <= 1e-12 * scale
+    assert np.allclose(a["rates"], b["rates"], rtol=1e-12, atol=1e-14 * np.abs(a["rates"]).max())
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_eigen_vs_lapack(oracle_lib, name):
+    """Jacobi eigenvalues against LAPACK (scipy zheevd) on the same H(k), D(q)."""
+    wd, req = case(name)
+    W = oracle_lib.Wannier(wd)
+    ks = S.mesh_kvecs(req.mesh)
+    e, v, _ = W.el_wann(ks)
+    ph = np.exp(2j * np.pi * (ks @ wd.rcells_k.T)) / wd.elwsdeg[None, :]
+    Hk = np.einsum("kr,rij->kij", ph, np.asarray(wd.Hwann))
+    Hk = np.triu(Hk) + np.conj(np.transpose(np.triu(Hk, 1), (0, 2, 1)))
+    ref = np.linalg.eigvalsh(Hk) * 13.6058
+    assert np.max(np.abs(e - ref)) < 1e-11
+    # eigenvectors: H v = e v
+    for k in range(0, len(ks), 7):
+        H = 0.5 * (Hk[k] + Hk[k].conj().T)
+        V = v[k].T      # columns
+        assert np.max(np.abs(H @ V - V * (e[k] / 13.6058))) < 1e-12
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_phonon_invariants(oracle_lib, name):
+    """omega^2 >= 0, three zero modes at Gamma, Hermitian D(q) eigen-system."""
+    wd, req = case(name)
+    W = oracle_lib.Wannier(wd)
+    qs = S.mesh_kvecs(req.mesh)
+    e, v, _, st = W.ph_wann(qs)
+    assert st == 0
+    assert np.all(e >= 0)
+    assert np.all(e[0, :3] == 0) and e[0, 3:].min() > 1e-3
+    assert e[1:].min() > 1e-4     # no floppy modes away from Gamma
+
+
+def test_gauge_invariance(oracle_lib):
+    """|g|^2 is unchanged by U_k -> U_k e^{i phi} and e_q -> e_q e^{i chi}."""
+    wd, req = case("si8")
+    W = oracle_lib.Wannier(wd)
+    rng = np.random.default_rng(0)
+    k = np.array([0.2, 0.4, 0.0])
+    kp = np.array([0.6, 0.2, 0.8])
+    q = (kp - k) % 1.0
+    ek, vk, _ = W.el_wann(k[None])
+    ekp, vkp, _ = W.el_wann(kp[None])
+    eq, vq, _, _ = W.ph_wann(q[None])
+    gm = W.gkRp(k)
+    for m, n, s in [(0, 1, 3), (3, 5, 4), (7, 2, 5)]:
+        a = W.g2(k, q, vk[0, m], vkp[0, n], vq[0, s], eq[0, s], gm)
+        ph = np.exp(1j * rng.uniform(0, 2 * np.pi, 3))
+        b = W.g2(k, q, vk[0, m] * ph[0], vkp[0, n] * ph[1], vq[0, s] * ph[2], eq[0, s], gm)
+        assert abs(a - b) <= 1e-12 * abs(a)
+
+
+def test_gaussian_delta_normalisation(oracle_lib):
+    """Sum over a fine uniform energy grid of the Gaussian delta integrates to 1/N_k."""
+    import math
+    sigma, N = 0.01, 1000
+    x = np.linspace(-0.2, 0.2, 40001)
+    d = (1 / math.sqrt(2 * math.pi)) / sigma * np.exp(-0.5 * (x / sigma) ** 2) / N
+    assert abs(np.trapezoid(d, x) * N - 1.0) < 1e-9
+
+
+def test_triangle_delta_linear_band(oracle_lib):
+    """A linear band on a 2D mesh gives a flat triangle-method DOS inside the band."""
+    import ctypes as ct
+    O = oracle_lib
+    mesh = np.array([8, 8, 1], dtype=np.int64)
+    nk = 64
+    idx = np.arange(1, nk + 1, dtype=np.int64)
+    ens = np.zeros((nk, 1), order="F")
+    for i in range(nk):
+        v = O.demux_vector(i + 1, list(mesh), 0)
+        ens[i, 0] = v[0] + 0.5 * v[1]      # linear in both directions (periodic wrap aside)
+    tri = np.zeros((2 * nk, 3), dtype=np.int64, order="F")
+    cnt = np.zeros(nk, dtype=np.int64)
+    mp = np.zeros((2, nk, 6), dtype=np.int64, order="F")
+    P = lambda a, t=ct.c_int64: a.ctypes.data_as(ct.POINTER(t))
+    O.lib().or_form_triangles(ct.c_int64(nk), P(mesh), P(idx), P(tri), P(cnt), P(mp))
+    assert np.all(cnt == 6)
+    se = np.zeros((2 * nk, 1, 3), order="F")
+    O.lib().or_fill_simplices(ct.c_int64(2 * nk), ct.c_int64(3), P(tri), ct.c_int64(nk), ct.c_int64(1),
+                              P(ens, ct.c_double), P(se, ct.c_double))
+    O.lib().or_delta_triang.argtypes = [ct.c_double, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_int64),
+                                        ct.c_int64, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_int64),
+                                        ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)]
+    # total DOS at energy e: sum over k of delta(e, k); interior energies only
+    tot = []
+    for e in (2.3, 3.1, 3.7):
+        s = sum(O.lib().or_delta_triang(e, ik, 1, P(mesh), nk, 2 * nk, 1, P(mp), P(cnt), P(se, ct.c_double))
+                for ik in range(1, nk + 1))
+        tot.append(s)
+    assert np.all(np.array(tot) > 0)
