@@ -637,7 +637,6 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   launch_iota(N * nw, iota, st);
   size_t tmp_bytes = 0, tb2 = 0, tb3 = 0;
   cub::DeviceSelect::Flagged(nullptr, tmp_bytes, iota, flag, widx, nwv_d, N, st);
-  int *sfl_tmp;
   if ((rc = wsget(h->ws, "r_sflag", (size_t)N * nw, &sflag)) || (rc = wsget(h->ws, "r_stcode", (size_t)N * nw, &st_code)) ||
       (rc = wsget(h->ws, "r_nst", 4, &nst_d)) || (rc = wsget(h->ws, "r_nink", (size_t)N + 1, &nin_k)) ||
       (rc = wsget(h->ws, "r_cum", (size_t)N + 1, &cum)))
@@ -759,7 +758,8 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   if (!split) {
     double2 *Pk, *gk, *B, *Pq, *Cb;
     const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nwv, ((int64_t)1 << 31) / (Nn * 16)));
-    const int64_t sc = std::max<int64_t>(1, std::min<int64_t>(nst, ((int64_t)1 << 31) / ((int64_t)nwv * ncol * 16)));
+    const int64_t sc = std::max<int64_t>(1, std::min<int64_t>({(int64_t)nst, (int64_t)32768,
+                                                              ((int64_t)1 << 31) / ((int64_t)nwv * ncol * 16)}));
     if ((rc = wsget(h->ws, "a_Pk", (size_t)kc * nwsk, &Pk)) || (rc = wsget(h->ws, "a_gk", (size_t)kc * Nn, &gk)) ||
         (rc = wsget(h->ws, "a_B", (size_t)nwsq * ldb, &B)) || (rc = wsget(h->ws, "b_Pq", (size_t)nwv * nwsq, &Pq)) ||
         (rc = wsget(h->ws, "b_C", (size_t)nwv * ncol * sc, &Cb)))
@@ -768,11 +768,14 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
       int n = (int)std::min<int64_t>(kc, nwv - i0);
       launch_phase_mesh(n, widx + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
       launch_zgemm(n, (int)Nn, nwsk, Pk, nwsk, h->G64, Nn, gk, Nn, st);
-      int j0 = first_state[i0], j1 = first_state[i0 + n];
-      // the rotation writes B columns relative to state 0
-      launch_rotate_states_fp64(j0, j1, (int)i0, st_code, nw, nb, nwsq, widx, V, gk, Nn, mesh, L,
-                                roots, h->Rq, h->degq, B + (int64_t)j0 * ncol, ldb, st);
-      h->launches += 3;
+      // the rotation writes B columns of states [j0, j1) (grid.y <= 32768 per launch)
+      for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
+        int je = std::min(j1, j0 + 32768);
+        launch_rotate_states_fp64(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, V, gk, Nn, mesh, L,
+                                  roots, h->Rq, h->degq, B + (int64_t)j0 * ncol, ldb, st);
+        h->launches += 1;
+      }
+      h->launches += 2;
     }
     CK(cudaEventRecord(ev.e[2], st));
     // ---- stage B + C: Rp Fourier against e^{2 pi i k'.Rp}, then the epilogue ----

@@ -1,4 +1,23 @@
-// ephg_tc.cu - 3xTF32 tcgen05 contractions of the rate pipeline (sm_103a).
+// ephg_tc.cu - split-FP32 (3xTF32) tcgen05 contractions of the rate pipeline.
+//
+// The two Fourier contractions of the e-ph vertex path are complex GEMMs:
+//   stage A  g(k,Rp)[n]      = sum_Re  e^{2 pi i k.Re}/deg(Re) g(Re,Rp)[n]      (gkRp)
+//   stage B  G(k',state)[c]  = sum_Rp  e^{2 pi i k'.Rp}  B(state)[Rp][c]        (g2's Rp sum)
+// Each runs here on the 5th-generation tensor cores as a persistent,
+// warp-specialised kernel: one thread issues TMA loads of K-major TF32 operand
+// planes into 64B-swizzled shared memory, one thread issues tcgen05.mma into
+// two double-buffered TMEM accumulators (real, imaginary), and four warps drain
+// TMEM with tcgen05.ld.  Every complex operand X is stored as four planes
+// (hi_re, hi_im, lo_re, lo_im) with hi = tf32(X) and lo = tf32(X - hi); each
+// real product uses hi*hi + hi*lo + lo*hi (the "3xTF32" split), FP32
+// accumulation.  -Im*Im terms use the instruction descriptor's negate-A bit.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
 #include <string>
 
 #include "ephg_tc.cuh"
@@ -7,22 +26,725 @@ namespace ephg {
 namespace tc {
 
 static std::string g_msg;
-
 const char *last_error() { return g_msg.c_str(); }
 
+static int tfail(int code, const char *m) {
+  g_msg = m;
+  return code;
+}
+
+#define TCK(call)                                                                   \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      g_msg = std::string(#call ": ") + cudaGetErrorString(e_);                     \
+      return 2;                                                                     \
+    }                                                                               \
+  } while (0)
+
+// ----------------------------------------------------------------- tiling
+constexpr int BM = 128;          // tile rows (UMMA M)
+constexpr int BN = 128;          // tile columns per accumulator (UMMA N)
+constexpr int BK = 16;           // K per stage: 16 fp32 = 64 B rows, SWIZZLE_64B
+constexpr int STAGES = 3;
+constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
+constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
+constexpr int TMEM_COLS = 512;                        // 2 buffers x (re 128 + im 128)
+constexpr int GEMM_THREADS = 192;                     // 6 warps
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after ~2 s, records DERR_TIMEOUT and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+  if (mbar_try(bar, parity)) return true;
+  long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > WAIT_CYCLES) {
+      atomicOr(err, DERR_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0,
+                                            int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// SMEM matrix descriptor: K-major, SWIZZLE_64B (atom = 8 rows x 64 B, SBO = 512 B).
+__device__ __forceinline__ uint64_t sdesc(const void *p) {
+  uint64_t a = smem_u32(p);
+  uint64_t d = (a >> 4) & 0x3FFFull;        // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset: 8-row groups 512 B apart
+  d |= (uint64_t)1 << 46;                   // descriptor version (sm_100 family)
+  d |= (uint64_t)4 << 61;                   // layout: SWIZZLE_64B
+  return d;
+}
+
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, K-major, M = 128, N = BN.
+__host__ __device__ constexpr uint32_t idesc_tf32(bool negA) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// -------------------------------------------------------- the GEMM kernel
+struct GemmArgs {
+  int mtiles, ntiles, nkb;   // tile counts, K blocks of BK
+  int64_t Astride, Bstride;  // rows between consecutive planes of the A / B stacks
+  int64_t Aoff, Boff;        // first row of the operand inside plane 0
+  float *Cr, *Ci;            // [Mp][ldc] outputs
+  int64_t ldc;
+  int *err;
+};
+
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    k_cgemm_3xtf32(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *tfull = empty + STAGES;
+  uint64_t *tempty = tfull + 2;
+  uint32_t *tslot = (uint32_t *)(tempty + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int ntile = g.mtiles * g.ntiles;
+
+  if (warp == 0) {
+    if (lane == 0) {   // ---- TMA producer
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+        const int mt = t % g.mtiles, nt = t / g.mtiles;
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
+          uint8_t *sb = smem + stage * STAGE_BYTES;
+          mbar_expect_tx(&full[stage], STAGE_BYTES);
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+            tma_load_2d(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + g.Aoff + mt * BM));
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+            tma_load_2d(sb + (4 + p) * PLANE_BYTES, &tB, &full[stage], kb * BK, (int)(p * g.Bstride + g.Boff + nt * BN));
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      // drain: wait until every issued stage has landed before the CTA can exit
+      for (int s = 0; s < STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, g.err), stage = (stage + 1) % STAGES,
+                                         phase ^= (stage == 0);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {   // ---- MMA issuer
+      constexpr uint32_t IDP = idesc_tf32(false), IDN = idesc_tf32(true);
+      int stage = 0;
+      uint32_t phase = 0;
+      int it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+        const int buf = it & 1;
+        const uint32_t tph = (it >> 1) & 1;
+        if (!mbar_wait(&tempty[buf], tph ^ 1, g.err)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t accr = tmem + buf * 2 * BN, acci = accr + BN;
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&full[stage], phase, g.err)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t *sb = smem + stage * STAGE_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < BK / 8; ++ks) {
+            const int off = ks * 32;   // 8 tf32 = 32 B along K inside the swizzle atom
+            const uint64_t Ahr = sdesc(sb + 0 * PLANE_BYTES + off), Ahi = sdesc(sb + 1 * PLANE_BYTES + off);
+            const uint64_t Alr = sdesc(sb + 2 * PLANE_BYTES + off), Ali = sdesc(sb + 3 * PLANE_BYTES + off);
+            const uint64_t Bhr = sdesc(sb + 4 * PLANE_BYTES + off), Bhi = sdesc(sb + 5 * PLANE_BYTES + off);
+            const uint64_t Blr = sdesc(sb + 6 * PLANE_BYTES + off), Bli = sdesc(sb + 7 * PLANE_BYTES + off);
+            const uint32_t first = (kb == 0 && ks == 0) ? 0u : 1u;
+            // Re = Ar Br - Ai Bi
+            umma(accr, Ahr, Bhr, IDP, first);
+            umma(accr, Ahr, Blr, IDP, 1);
+            umma(accr, Alr, Bhr, IDP, 1);
+            umma(accr, Ahi, Bhi, IDN, 1);
+            umma(accr, Ahi, Bli, IDN, 1);
+            umma(accr, Ali, Bhi, IDN, 1);
+            // Im = Ar Bi + Ai Br
+            umma(acci, Ahr, Bhi, IDP, first);
+            umma(acci, Ahr, Bli, IDP, 1);
+            umma(acci, Alr, Bhi, IDP, 1);
+            umma(acci, Ahi, Bhr, IDP, 1);
+            umma(acci, Ahi, Blr, IDP, 1);
+            umma(acci, Ali, Bhr, IDP, 1);
+          }
+          umma_commit(&empty[stage]);     // frees the smem stage when these MMAs retire
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (ok) umma_commit(&tfull[buf]);   // accumulator ready for the epilogue
+      }
+    }
+  } else {   // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    int it = 0;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
+      const int mt = t % g.mtiles, nt = t / g.mtiles;
+      const int buf = it & 1;
+      const uint32_t tph = (it >> 1) & 1;
+      if (!mbar_wait(&tfull[buf], tph, g.err)) break;
+      tc_fence_after();
+      const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16) + buf * 2 * BN;
+      float *cr = g.Cr + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
+      float *ci = g.Ci + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float vr[16], vi[16];
+        tmem_ld16(tr + c0, vr);
+        tmem_ld16(tr + BN + c0, vi);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          *(float4 *)(cr + c0 + 4 * q) = make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]);
+          *(float4 *)(ci + c0 + 4 * q) = make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[buf]);
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// -------------------------------------------------------- tensor maps
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 2D map over a stack of K-major fp32 planes: (Kp, rows), box (BK, 128), 64B swizzle.
+static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows) {
+  auto fn = encode_fn();
+  if (!fn) return tfail(2, "cuTensorMapEncodeTiled unavailable");
+  if (((uintptr_t)base & 15) || (Kp % BK)) return tfail(1, "operand planes misaligned");
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
+  cuuint32_t box[2] = {BK, 128};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return tfail(2, "cuTensorMapEncodeTiled failed");
+  return 0;
+}
+
+static int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+// C[Mp][ldc] (re, im planes) = A x B^T.  A: planes of Astride rows, rows
+// [Aoff, Aoff + Mp) of each; B: planes of Bstride rows, rows [Boff, Boff + Np).
+static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const float *Bp, int64_t Bstride,
+                 int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st) {
+  if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
+  if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
+  CUtensorMap ta, tb;
+  int rc;
+  if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 4 * Bstride))) return rc;
+  static bool attr = false;
+  if (!attr) {
+    TCK(cudaFuncSetAttribute(k_cgemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr = true;
+  }
+  GemmArgs g;
+  g.mtiles = Mp / BM;
+  g.ntiles = Np / BN;
+  g.nkb = Kp / BK;
+  g.Astride = Astride;
+  g.Bstride = Bstride;
+  g.Aoff = Aoff;
+  g.Boff = Boff;
+  g.Cr = Cr;
+  g.Ci = Ci;
+  g.ldc = ldc;
+  g.err = err;
+  int tiles = g.mtiles * g.ntiles;
+  int grid = std::min(tiles, num_sms());
+  k_cgemm_3xtf32<<<grid, GEMM_THREADS, SMEM_BYTES, st>>>(ta, tb, g);
+  TCK(cudaGetLastError());
+  return 0;
+}
+
+// ------------------------------------------------------ operand planes
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;   // inf / nan untouched
+  u += 0x0FFFu + ((u >> 13) & 1u);
+  return __uint_as_float(u & 0xFFFFE000u);
+}
+
+// hi = tf32(x), lo = tf32(x - hi), from a double
+__device__ __forceinline__ void split2(double x, float &hi, float &lo) {
+  hi = tf32_round((float)x);
+  lo = tf32_round((float)(x - (double)hi));
+}
+
+__device__ __forceinline__ void put4(float *P, int64_t plane, int64_t idx, double2 v) {
+  float hr, lr, hi, li;
+  split2(v.x, hr, lr);
+  split2(v.y, hi, li);
+  P[0 * plane + idx] = hr;
+  P[1 * plane + idx] = hi;
+  P[2 * plane + idx] = lr;
+  P[3 * plane + idx] = li;
+}
+
+__device__ inline int phase_idx(int p, int m1, int m2, int m3, int L, int r1, int r2, int r3) {
+  int v1 = p % m1, v2 = (p / m1) % m2, v3 = p / (m1 * m2);
+  int64_t t = (int64_t)v1 * r1 * (L / m1) + (int64_t)v2 * r2 * (L / m2) + (int64_t)v3 * r3 * (L / m3);
+  t %= L;
+  if (t < 0) t += L;
+  return (int)t;
+}
+
+// A planes of e^{2 pi i k.R} (/ deg) for the rows k = rowp[0..nrows): [4][Mp][Kp]
+__global__ void k_phase_planes(int nrows, const int *rowp, int m1, int m2, int m3, int L, int nR, const int *R,
+                               const double *deg, const double2 *roots, float *P, int Mp, int Kp) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nrows * nR) return;
+  int row = (int)(idx / nR), r = (int)(idx % nR);
+  double2 v = roots[phase_idx(rowp[row], m1, m2, m3, L, R[3 * r], R[3 * r + 1], R[3 * r + 2])];
+  if (deg) v = make_double2(v.x / deg[r], v.y / deg[r]);
+  put4(P, (int64_t)Mp * Kp, (int64_t)row * Kp + r, v);
+}
+
+// B planes of the stage-A matrix: G64[Re][n] -> planes [4][Np][Kp] (transposed)
+__global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, float *P, int64_t Np, int Kp) {
+  __shared__ double2 tile[32][33];
+  int64_t n0 = (int64_t)blockIdx.x * 32;
+  int r0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int re = r0 + i;
+    int64_t n = n0 + threadIdx.x;
+    tile[i][threadIdx.x] = (re < nwsk && n < Nn) ? G[(int64_t)re * Nn + n] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int64_t n = n0 + i;
+    int re = r0 + threadIdx.x;
+    if (n < Nn && re < Kp) put4(P, Np * Kp, n * Kp + re, tile[threadIdx.x][i]);
+  }
+}
+
+// Rotation over the initial band + k-half of the Rp phase, split into the B
+// planes of stage B: Bp[4][Np2][Kp2], column c = (j - j0)*ncol + n' + nw*s'.
+__global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int nw, int nb, int nws,
+                                const int *widx, const double2 *U, const float *gr, const float *gi, int64_t ldg,
+                                int m1, int m2, int m3, int L, const double2 *roots, const int *Rq,
+                                const double *degq, float *Bp, int64_t Np2, int Kp2, int jbase) {
+  const int j = j0 + blockIdx.y;
+  if (j >= j1) return;
+  const int code = st_code[j];
+  const int i = code / nw, m = code % nw;
+  const int p = widx[i];
+  const double2 *Uk = U + ((size_t)p * nw + m) * nw;
+  const int ncol = nw * nb;
+  const int64_t grow = (int64_t)(i - i0) * ldg;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ncol * nws; e += gridDim.x * blockDim.x) {
+    const int rp = e % nws, c = e / nws;
+    const int np = c % nw, s = c / nw;
+    double2 ph = roots[phase_idx(p, m1, m2, m3, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
+    ph = make_double2(ph.x / degq[rp], -ph.y / degq[rp]);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int mp = 0; mp < nw; ++mp) {
+      int64_t off = grow + np + nw * (mp + (int64_t)nw * (s + (int64_t)nb * rp));
+      cfma(acc, Uk[mp], make_double2((double)gr[off], (double)gi[off]));
+    }
+    const int64_t col = (int64_t)(j - jbase) * ncol + c;
+    put4(Bp, Np2 * Kp2, col * Kp2 + rp, cmul(ph, acc));
+  }
+}
+
+// -------------------------------------------- split-form rate epilogue
+struct QTab {
+  const float *cx;     // [q][s]: const_tp * g2unitfactor / (2 omega) if omega >= 0.5 meV else 0
+  const float *bose;   // [q][s]
+  const float *w;      // [q][s]: omega / sigma
+  const float *v;      // [q][s]: omega / kT
+};
+
+__global__ void k_qtab(int n, const double *om, const double *bose, double sigma, double kT, double const_tp,
+                       float *cx, float *bs, float *w, float *v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double o = om[i];
+  cx[i] = (o >= 0.5e-3) ? (float)(const_tp * 0.5 * g2unitfactor / o) : 0.0f;
+  bs[i] = (float)bose[i];
+  w[i] = (float)(o / sigma);
+  v[i] = (float)(o / kT);
+}
+
+__global__ void k_to_f2(int64_t n, const double2 *a, float2 *b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// One thread per (k', initial state): G(n',s') from the FP32 GEMM output, the
+// U_k' and phonon rotations in FP32, the Gaussian delta and occupations from
+// FP64 energy differences scaled to O(1) before rounding, X+- and the pair sum.
+__global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const float *Cr, const float *Ci,
+                                                        int64_t ldc, RateParams rp, EpiData d, QTab qt,
+                                                        double *partial, int nblk) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = j0 + blockIdx.y;
+  const int nw = rp.nw, nb = rp.nb, ncol = nw * nb;
+  double v = 0.0;
+  if (ip < nwv) {
+    const int code = d.st_code[j];
+    const int i = code / nw, m = code % nw;
+    const int p = d.widx[i], pp = d.widx[ip];
+    const double E = d.ens[(size_t)p * nw + m];
+    const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+    const double inv_sig = 1.0 / rp.sigma;
+    const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
+    int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
+    int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+    const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                        rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+    const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    float acc = 0.0f;
+    int rank_n = 0;
+    for (int n = 0; n < nw; ++n) {
+      const double eps = d.ens[(size_t)pp * nw + n];
+      if (fabs(eps - rp.enref) > rp.fsthick) continue;
+      const float2 *Ukp = d.Uf + ((size_t)pp * nw + n) * nw;
+      float2 h[32];
+      for (int s = 0; s < nb; ++s) {
+        float2 a = make_float2(0.f, 0.f);
+        for (int np = 0; np < nw; ++np) {
+          int64_t o = base + np + nw * s;
+          cfmaf_cj(a, Ukp[np], make_float2(Cr[o], Ci[o]));
+        }
+        h[s] = a;
+      }
+      const float dn = (float)((E - eps) * inv_sig);
+      for (int s = 0; s < nb; ++s) {
+        const int qs = q * nb + s;
+        const float2 *u = d.uf + (size_t)qs * nb;
+        float2 g = make_float2(0.f, 0.f);
+        for (int sp = 0; sp < nb; ++sp) cfmaf(g, u[sp], h[sp]);
+        const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
+        const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
+        const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
+        const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
+        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+        const float xp = g2c * (qt.bose[qs] + fp) * dp;
+        const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+        acc += xp + xm;
+        if (d.g2) {
+          int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
+          if (off < d.cap) {
+            const double om = d.om[qs];
+            d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+            d.xp[off] = xp;
+            d.xm[off] = xm;
+          }
+        }
+      }
+      rank_n++;
+    }
+    v = (double)acc;
+  }
+  __shared__ double sv[128];
+  sv[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, c = 0.0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      double x = sv[t], tt = s + x;
+      c += (fabs(s) >= fabs(x)) ? (s - tt) + x : (x - tt) + s;
+      s = tt;
+    }
+    partial[(size_t)j * nblk + blockIdx.x] = s + c;
+  }
+}
+
+// ------------------------------------------------------------ orchestration
 void free_split(SplitOperands &s) {
   if (s.G) cudaFree(s.G);
   s.G = nullptr;
 }
 
-int split_rates_stage(SplitOperands &, Workspace &, cudaStream_t, const double2 *, int, int,
-                      int64_t, int, int, int, int, const int *, int, const double2 *, const int *,
-                      const int *, const std::vector<int> &, const int *, const double *,
-                      const int *, const double *, const double2 *, const RateParams &,
-                      const EpiData &, double *, int, cudaEvent_t, int64_t *) {
-  g_msg = "split precision not available in this build";
-  return 1;
+static inline int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk, int nwsq,
+                      int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
+                      const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
+                      const double *degk, const int *Rq, const double *degq, const double2 *U,
+                      const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, cudaEvent_t ev_stage_a,
+                      int64_t *launches) {
+  int rc;
+  int *err = nullptr;
+  // the device error word lives in the workspace; the caller checks its own word afterwards
+  if ((rc = wsget(ws, "tc_err", 1, &err))) return tfail(6, ws.msg.c_str());
+  TCK(cudaMemsetAsync(err, 0, sizeof(int), st));
+  const int KpA = (int)rup(nwsk, BK), KpB = (int)rup(nwsq, BK);
+  const int64_t NpA = rup(Nn, BN);
+  // g(Re,Rp) planes, built once per handle
+  if (!s.G) {
+    TCK(cudaMalloc(&s.G, (size_t)4 * NpA * KpA * sizeof(float)));
+    TCK(cudaMemsetAsync(s.G, 0, (size_t)4 * NpA * KpA * sizeof(float), st));
+    dim3 grid((unsigned)((Nn + 31) / 32), (unsigned)((KpA + 31) / 32));
+    k_gplanes<<<grid, dim3(32, 8), 0, st>>>(Nn, nwsk, G64, s.G, NpA, KpA);
+    TCK(cudaGetLastError());
+    s.Nn = NpA;
+    s.Kp = KpA;
+    (*launches)++;
+  }
+  const int ncol = nw * nb;
+  // stage A in k chunks of kc rows (multiple of BM)
+  const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nwv, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
+  const int64_t Np2 = rup((int64_t)nst * ncol, BN);
+  float *PA, *CAr, *CAi, *B2;
+  if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
+      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)4 * Np2 * KpB, &B2)))
+    return tfail(6, ws.msg.c_str());
+  TCK(cudaMemsetAsync(B2, 0, (size_t)4 * Np2 * KpB * sizeof(float), st));
+  for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
+    const int n = (int)std::min<int64_t>(kc, nwv - i0);
+    const int Mp = (int)rup(n, BM);
+    TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
+    int64_t ne = (int64_t)n * nwsk;
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(n, widx + i0, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
+                                                                 degk, roots, PA, Mp, KpA);
+    TCK(cudaGetLastError());
+    if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st))) return rc;
+    for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
+      int je = std::min(j1, j0 + 32768);
+      dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
+      k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, U, CAr, CAi, NpA, mesh[0],
+                                           mesh[1], mesh[2], L, roots, Rq, degq, B2, Np2, KpB, 0);
+      TCK(cudaGetLastError());
+      (*launches)++;
+    }
+    *launches += 3;
+  }
+  TCK(cudaEventRecord(ev_stage_a, st));
+  // stage B: A planes = e^{2 pi i k'.Rp} for the window k'
+  const int MpB = (int)rup(nwv, BM);
+  float *PB, *CBr, *CBi;
+  // states per chunk: a multiple of 8 (8 * 48 = 3 * 128 columns) bounded by ~2 GB of output
+  int64_t sc = ((int64_t)1 << 31) / ((int64_t)MpB * ncol * 8);
+  sc = std::max<int64_t>(8, sc / 8 * 8);
+  sc = std::min<int64_t>(sc, rup(nst, 8));
+  sc = std::min<int64_t>(sc, 32768);
+  const int64_t NpC = rup(sc * ncol, BN);
+  if ((rc = wsget(ws, "tc_PB", (size_t)4 * MpB * KpB, &PB)) || (rc = wsget(ws, "tc_CBr", (size_t)MpB * NpC, &CBr)) ||
+      (rc = wsget(ws, "tc_CBi", (size_t)MpB * NpC, &CBi)))
+    return tfail(6, ws.msg.c_str());
+  TCK(cudaMemsetAsync(PB, 0, (size_t)4 * MpB * KpB * sizeof(float), st));
+  {
+    int64_t ne = (int64_t)nwv * nwsq;
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, widx, mesh[0], mesh[1], mesh[2], L, nwsq, Rq,
+                                                                 nullptr, roots, PB, MpB, KpB);
+    TCK(cudaGetLastError());
+  }
+  // fp32 copies of the eigenvectors and per-(q,s) tables for the epilogue
+  float2 *Uf;
+  float *cx, *bs, *w, *v;
+  const int N = rp.N;
+  if ((rc = wsget(ws, "tc_Uf", (size_t)N * nw * nw, &Uf)) || (rc = wsget(ws, "tc_cx", (size_t)N * nb, &cx)) ||
+      (rc = wsget(ws, "tc_bs", (size_t)N * nb, &bs)) || (rc = wsget(ws, "tc_w", (size_t)N * nb, &w)) ||
+      (rc = wsget(ws, "tc_v", (size_t)N * nb, &v)))
+    return tfail(6, ws.msg.c_str());
+  k_to_f2<<<(unsigned)(((int64_t)N * nw * nw + 255) / 256), 256, 0, st>>>((int64_t)N * nw * nw, U, Uf);
+  k_qtab<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.om, ed_in.bose, rp.sigma, kB * rp.T, rp.const_tp, cx, bs,
+                                                w, v);
+  TCK(cudaGetLastError());
+  *launches += 3;
+  EpiData ed = ed_in;
+  ed.Uf = Uf;
+  QTab qt{cx, bs, w, v};
+  for (int64_t j0 = 0; j0 < nst; j0 += sc) {
+    const int ns = (int)std::min<int64_t>(sc, nst - j0);
+    const int Npc = (int)rup((int64_t)ns * ncol, BN);
+    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st))) return rc;
+    dim3 grid(nblk, ns);
+    if (rp.delta_kind == 0) {
+      k_epilogue_split<<<grid, 128, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      TCK(cudaGetLastError());
+    } else {
+      launch_epilogue_fp32(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed_in, partial, nblk, st);
+    }
+    *launches += 2;
+  }
+  int herr = 0;
+  TCK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TCK(cudaStreamSynchronize(st));
+  if (herr & DERR_TIMEOUT) return tfail(7, "tcgen05 GEMM: a bounded mbarrier wait gave up");
+  return 0;
 }
 
 }  // namespace tc
 }  // namespace ephg
+
+// ----------------------------------------------------------- test hook
+namespace ephg {
+namespace tc {
+// A (M,K) complex row-major -> planes [4][Mp][Kp]
+__global__ void k_planes_rows(int64_t M, int K, const double2 *A, float *P, int64_t Mp, int Kp) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * K) return;
+  int64_t r = idx / K;
+  int k = (int)(idx % K);
+  put4(P, Mp * Kp, r * Kp + k, A[idx]);
+}
+__global__ void k_join(int64_t M, int64_t N, const float *Cr, const float *Ci, int64_t ldc, double2 *C) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * N) return;
+  int64_t r = idx / N, c = idx % N;
+  C[idx] = make_double2(Cr[r * ldc + c], Ci[r * ldc + c]);
+}
+}  // namespace tc
+}  // namespace ephg
+
+extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A, const double *B, double *C) {
+  using namespace ephg;
+  using namespace ephg::tc;
+  if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C) return tfail(1, "debug_cgemm: bad arguments");
+  const int64_t Mp = rup(M, BM), Np = rup(N, BN), Kp = rup(K, BK);
+  double2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  float *PA = nullptr, *PB = nullptr, *Cr = nullptr, *Ci = nullptr;
+  int *err = nullptr;
+  int rc = 0;
+  cudaStream_t st = 0;
+  auto cleanup = [&]() {
+    for (void *p : {(void *)dA, (void *)dB, (void *)dC, (void *)PA, (void *)PB, (void *)Cr, (void *)Ci, (void *)err})
+      if (p) cudaFree(p);
+  };
+  if (cudaMalloc(&dA, M * K * 16) || cudaMalloc(&dB, K * N * 16) || cudaMalloc(&dC, M * N * 16) ||
+      cudaMalloc(&PA, 4 * Mp * Kp * 4) || cudaMalloc(&PB, 4 * Np * Kp * 4) || cudaMalloc(&Cr, Mp * Np * 4) ||
+      cudaMalloc(&Ci, Mp * Np * 4) || cudaMalloc(&err, 4)) {
+    cleanup();
+    return tfail(6, "debug_cgemm: cudaMalloc failed");
+  }
+  cudaMemcpy(dA, A, M * K * 16, cudaMemcpyHostToDevice);
+  cudaMemcpy(dB, B, K * N * 16, cudaMemcpyHostToDevice);
+  cudaMemset(PA, 0, 4 * Mp * Kp * 4);
+  cudaMemset(PB, 0, 4 * Np * Kp * 4);
+  cudaMemset(err, 0, 4);
+  k_planes_rows<<<(unsigned)((M * K + 255) / 256), 256>>>(M, (int)K, dA, PA, Mp, (int)Kp);
+  dim3 grid((unsigned)((N + 31) / 32), (unsigned)((Kp + 31) / 32));
+  k_gplanes<<<grid, dim3(32, 8)>>>(N, (int)K, dB, PB, Np, (int)Kp);
+  rc = cgemm(PA, Mp, 0, (int)Mp, PB, Np, 0, (int)Np, (int)Kp, Cr, Ci, Np, err, st);
+  if (!rc) {
+    k_join<<<(unsigned)((M * N + 255) / 256), 256>>>(M, N, Cr, Ci, Np, dC);
+    cudaError_t e = cudaDeviceSynchronize();
+    int herr = 0;
+    cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = tfail(2, cudaGetErrorString(e));
+    else if (herr) rc = tfail(7, "debug_cgemm: bounded wait gave up");
+    else cudaMemcpy(C, dC, M * N * 16, cudaMemcpyDeviceToHost);
+  }
+  cleanup();
+  return rc;
+}
+
+extern "C" const char *ephg_debug_last_error(void) { return ephg::tc::last_error(); }

@@ -12,7 +12,7 @@ namespace tc {
 struct SplitOperands {
   float *G = nullptr;      // g(Re,Rp) as K-major TF32 planes [4][Nn][Kpad]: hi_r, hi_i, lo_r, lo_i
   int64_t Nn = 0;
-  int Kpad = 0;
+  int Kp = 0;       // padded K (WS cells)
 };
 
 void free_split(SplitOperands &s);

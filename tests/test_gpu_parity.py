@@ -66,7 +66,9 @@ def test_ph_wann(W_cache, oracle_lib, name):
     nz = eo > 1e-3
     ov = np.abs(np.einsum("kbc,kbc->kb", np.conj(evo), ev))
     assert np.max(np.abs(ov[nz] - 1)) < 1e-8
-    assert np.max(np.abs(v[1:] - vo[1:])) < 1e-7 * np.abs(vo).max()
+    # (in a 2^3 supercell every wrap set is symmetric and the reference's
+    # unwrapped-R velocity formula cancels to ~0, hence the absolute floor)
+    assert np.max(np.abs(v[1:] - vo[1:])) < 1e-7 * max(np.abs(vo).max(), 1e-3)
 
 
 @pytest.mark.parametrize("name", CASES)

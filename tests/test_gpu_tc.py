@@ -1,0 +1,94 @@
+"""The 3xTF32 tcgen05 complex GEMM and the split-precision rate path.
+
+Tolerances (split form): GEMM normwise relative error <= 2e-6 against the
+complex128 product; |g|^2 per vertex |a-b| <= 1e-5 |b| + 1e-6 max|b|; RTA rates
+<= 1e-6 relative per state (the benchmark spec's split-form bound).
+"""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from elphbolt_gb300 import _lib, synthetic as S
+from tests.cases import case, CASES
+
+pytestmark = pytest.mark.gpu
+
+
+def cgemm(A, B):
+    L = _lib.load()
+    L.ephg_debug_cgemm.argtypes = [ct.c_int64, ct.c_int64, ct.c_int64, _lib.c_dp, _lib.c_dp, _lib.c_dp]
+    L.ephg_debug_last_error.restype = ct.c_char_p
+    M, K = A.shape
+    N = B.shape[1]
+    a = np.ascontiguousarray(A, dtype=np.complex128)
+    b = np.ascontiguousarray(B, dtype=np.complex128)
+    c = np.zeros((M, N), dtype=np.complex128)
+    rc = L.ephg_debug_cgemm(M, N, K, a.ctypes.data_as(_lib.c_dp), b.ctypes.data_as(_lib.c_dp),
+                            c.ctypes.data_as(_lib.c_dp))
+    assert rc == 0, L.ephg_debug_last_error()
+    return c
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from elphbolt_gb300.build import build
+    build()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 16), (200, 300, 279), (77, 1000, 5), (2048, 2304, 600)])
+def test_cgemm_vs_fp64(M, N, K):
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
+    B = rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))
+    ref = A @ B
+    got = cgemm(A, B)
+    err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert err <= 2e-6, err
+    # elementwise against the scale of each dot product
+    scale = np.sqrt(np.abs(A) ** 2 @ np.abs(B) ** 2)
+    assert np.max(np.abs(got - ref) / scale) <= 1e-5
+
+
+def test_cgemm_phases():
+    """Unit-modulus phase rows against decaying data: the shape of both contractions."""
+    rng = np.random.default_rng(5)
+    M, K, N = 300, 279, 384
+    A = np.exp(2j * np.pi * rng.uniform(0, 1, (M, K)))
+    B = (rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))) * np.exp(-rng.uniform(0, 5, (K, 1)))
+    ref = A @ B
+    got = cgemm(A, B)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 2e-6
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_el_rates_split_vs_oracle(oracle_lib, name):
+    from elphbolt_gb300.wannier import Wannier
+    wd, req = case(name)
+    o = oracle_lib.Wannier(wd).el_rates(req, literal=True, vertices=True)
+    W = Wannier(wd)
+    g = W.el_rates(req, precision=_lib.PREC_SPLIT_TF32, vertices=True)
+    W.deallocate_wannier()
+    assert g["nwv"] == o["nwv"] and np.array_equal(g["indexlist"], o["indexlist"])
+    assert g["vertices"] == o["vertices"]
+    scale = np.abs(o["g2"]).max()
+    assert np.all(np.abs(g["g2"] - o["g2"]) <= 1e-5 * np.abs(o["g2"]) + 1e-6 * scale)
+    r, ro = g["rates"], o["rates"]
+    mask = ro > 0
+    rel = np.abs(r - ro)[mask] / ro[mask]
+    assert rel.max() <= 1e-6, rel.max()
+    assert np.all(r[~mask] == 0)
+
+
+@pytest.mark.parametrize("delta", [1, 2])
+def test_el_rates_split_simplex_deltas(oracle_lib, delta):
+    from elphbolt_gb300.wannier import Wannier
+    wd, req0 = case("si8")
+    req = S.RateRequest(**{**req0.__dict__, "delta_kind": delta})
+    o = oracle_lib.Wannier(wd).el_rates(req, literal=False)
+    W = Wannier(wd)
+    g = W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+    W.deallocate_wannier()
+    mask = o["rates"] > 1e-8 * o["rates"].max()
+    rel = np.abs(g["rates"] - o["rates"])[mask] / o["rates"][mask]
+    assert rel.max() <= 1e-6, rel.max()
