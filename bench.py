@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Benchmark of the e-ph vertex path: |g|^2 vertices/s of RTA-rate requests.
+
+Workload (the one the metric is quoted on): synthetic diamond-Si-like fcc
+2-atom crystal, a = 5.43 A, 28 amu, nw = 8 Wannier bands, nb = 6 modes, Re and
+Rp Wigner-Seitz sets of a 6x6x6 supercell (279 cells each), 24^3 k = q mesh,
+window +-0.5 eV around mu = mid-gap + 0.6 eV, Gaussian delta sigma = 10 meV,
+T = 300 K.  A step is one full RTA-rate request (H(k) and D(q) set-up and
+eigensolves, g(Re,Rp) -> g(k,Rp), the Rp Fourier, rotations, |g|^2, delta x
+occupations, compensated rate sums) in the split-FP32 (3xTF32) tcgen05 form.
+
+Our arm: ``value`` is vertices/s with the Wannier data resident in HBM, from
+the library's CUDA events on its launch stream; ``e2e`` is the same metric for
+the one-shot drop-in through the C ABI from pinned host buffers (create ->
+rates -> destroy, every host<->device copy inside the timed region).
+``--impl reference``: the reference algorithm on the host cores (the CPU
+restatement of the reference path, literal per-vertex g2, OpenMP over k').
+
+Multi-GPU: the path runs as independent replicas, one per rank (no
+collective on the data path); value is the whole job's vertices / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "|g|^2 vertices/s (split-FP32 3xTF32 tcgen05, RTA rates within 1e-6 of FP64)"
+UNIT = "vertices/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks not sampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        loaded = [x for x in sm if mx and x > 0.3 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def workload():
+    from elphbolt_gb300 import synthetic as S
+    wd = S.si_like()                                   # seed 20260101, 6^3 WS supercell
+    req = S.si_like_request(wd, (24, 24, 24))          # 24^3, +-0.5 eV at mid-gap+0.6 eV, 10 meV
+    return wd, req
+
+
+def config_dict(wd, req, stats=None):
+    c = {"workload": "Si-like fcc 2-atom, nwann 8, nmodes 6, %d Re / %d Rp WS cells (6^3), 24^3 k=q mesh, "
+                     "window +-0.5 eV at mid-gap+0.6 eV, Gaussian delta 10 meV, T 300 K" % (wd.nwsk, wd.nwsq),
+         "mesh": list(req.mesh), "nwann": wd.numwannbands, "nmodes": wd.numbranches,
+         "n_ws_re": wd.nwsk, "n_ws_rp": wd.nwsq, "precision": "split-FP32 (3xTF32, FP32 accumulate)",
+         "l2_policy": "inputs larger than L2 (g(Re,Rp) TF32 planes 494 MB, stage-B operand planes 2.9 GB)"}
+    if stats:
+        c.update({"window_k": stats["nwv"], "initial_states": stats["nstates"], "vertices_per_step": stats["vertices"]})
+    return c
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def traffic_per_gflop():
+    """DRAM bytes per algorithmic GFLOP of the stage-B contraction, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "cgemm_stageB_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_alg_gflop")
+        except Exception:
+            return None
+    return None
+
+
+def cpu_sample(wd, req, seconds_target=20.0, states=None):
+    """The CPU oracle (literal per-vertex g2) on a bounded sample of initial states."""
+    from oracle import oracle as O
+    ncores = os.cpu_count() or 1
+    W = O.Wannier(wd)
+    t0 = time.time()
+    R = O.RatesRun(W, req, nthreads=ncores)
+    t_setup = time.time() - t0
+    # calibrate: one state, then enough states for ~seconds_target
+    a = R.run(0, 1)
+    per_state_s = a["us_loop"] * 1e-6
+    n = states or max(1, min(64, int(seconds_target / max(per_state_s, 1e-3))))
+    b = R.run(1, n)
+    R.close()
+    v = b["vertices"]
+    t = b["us_loop"] * 1e-6
+    return dict(value=v / t, cores=ncores, states=n, vertices=v, seconds=t, setup_s=t_setup,
+                nstates_total=a["nstates_inwindow"])
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    wd, req = workload()
+    from oracle import oracle as O
+    O.build()
+    ncores = os.cpu_count() or 1
+    W = O.Wannier(wd)
+    t0 = time.time()
+    R = O.RatesRun(W, req, nthreads=ncores)
+    t_setup = time.time() - t0
+    a = R.run(0, 1)
+    per_state_s = max(a["us_loop"] * 1e-6, 1e-3)
+    budget = 150.0 / max(1, args.steps + args.warmup)       # whole run within a few minutes
+    n = max(1, int(budget / per_state_s))
+    s0 = 1
+    for _ in range(args.warmup):
+        R.run(s0, n)
+        s0 += n
+    tt, vv = 0.0, 0
+    for _ in range(args.steps):
+        b = R.run(s0, n)
+        s0 += n
+        tt += b["us_loop"] * 1e-6
+        vv += b["vertices"]
+    R.close()
+    val = vv / tt
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tt / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": config_dict(wd, req),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": "%d steps x %d initial states of %d (literal per-vertex g2, OpenMP over k'); "
+                                       "set-up %.1f s excluded" % (args.steps, n, a["nstates_inwindow"], t_setup)},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    from elphbolt_gb300 import _lib, build
+    build.build()
+    from elphbolt_gb300.wannier import Wannier
+    import ctypes as ct
+
+    dev = 0
+    torch.cuda.set_device(dev)
+    group = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        group = dist
+    wd, req = workload()
+    W = Wannier(wd)
+    prec = _lib.PREC_SPLIT_TF32
+    for _ in range(args.warmup):
+        out = W.el_rates(req, precision=prec)
+    # ---- timed region: value ----
+    if group:
+        group.barrier()
+    torch.cuda.synchronize()
+    dev_ms, launches, gemm_ms, gemm_n, wall0 = [], 0, 0.0, 0, time.time()
+    with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
+        for _ in range(args.steps):
+            out = W.el_rates(req, precision=prec)
+            st = out["stats"]
+            dev_ms.append(st["ms_total"])
+            launches += st["kernel_launches"]
+            gemm_ms += st["ms_gemm_b"]
+            gemm_n += st["gemm_b_launches"]
+        torch.cuda.synchronize()
+        wall = time.time() - wall0
+    if group:
+        group.barrier()
+    total_ms = float(sum(dev_ms))
+    if group:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        group.all_reduce(t, op=group.ReduceOp.MAX)
+        total_ms = float(t.item())
+    st = out["stats"]
+    vertices = st["vertices"]
+    value = ws * args.steps * vertices / (total_ms * 1e-3)
+    split_rates = out["rates"]
+    # ---- e2e: one-shot drop-in through the C ABI from pinned host buffers ----
+    e2e = e2e_measure(wd, req, prec, max(1, min(args.steps, 3)))
+    # ---- FP64 plain drop-in on the same request (one step) ----
+    f = W.el_rates(req, precision=_lib.PREC_FP64)
+    fst = f["stats"]
+    fp64_value = fst["vertices"] / (fst["ms_total"] * 1e-3)
+    ref = f["rates"]
+    mask = ref > 0
+    rate_err = float(np.max(np.abs(split_rates[mask] - ref[mask]) / ref[mask])) if mask.any() else None
+    W.deallocate_wannier()
+    if rank != 0:
+        return 0
+    # ---- roofline of the dominant kernel (stage-B 3xTF32 contraction) ----
+    bf16, hbm, src = peaks()
+    achieved = st["stage_b_gflop"] / (st["ms_gemm_b"] * 1e-3) / 1e3          # TFLOP/s algorithmic
+    peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
+    tpg = traffic_per_gflop()
+    cpu = cpu_sample(wd, req)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (3xTF32 contractions) + f64 (eigensolves, sums)",
+            "data": "synthetic (seeded, reference units and layouts)",
+            "config": config_dict(wd, req, st),
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak,
+                         "traffic": (tpg * st["stage_b_gflop"] / max(1, st["gemm_b_launches"])) if tpg else None,
+                         "kernel": "k_cgemm_3xtf32 (stage B, Rp Fourier)",
+                         "peak_source": "%s bf16 %.1f TFLOP/s / 2 (TF32) / 3 (split), of %s" % (src, bf16, src),
+                         "launches_per_step": st["gemm_b_launches"],
+                         "ms_per_launch": st["ms_gemm_b"] / max(1, st["gemm_b_launches"])},
+            "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                             "sample": "%d initial states of %d, %d vertices in %.1f s (literal per-vertex g2, "
+                                       "OpenMP over k'); set-up %.1f s excluded" % (
+                                           cpu["states"], cpu["nstates_total"], cpu["vertices"], cpu["seconds"],
+                                           cpu["setup_s"])},
+            "fp64_dropin": {"value": fp64_value, "unit": UNIT, "ms_per_step": fst["ms_total"],
+                            "split_speedup": value / ws / fp64_value},
+            "error_vs_fp64": {"rates_max_rel": rate_err},
+            "stage_ms": {"setup": st["ms_setup"], "stage_a": st["ms_stage_a"], "stage_bc": st["ms_stage_bc"],
+                         "gemm_a": st["ms_gemm_a"], "gemm_b": st["ms_gemm_b"]},
+            "wall_s": wall,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def e2e_measure(wd, req, prec, steps):
+    """create -> el_rates -> destroy through the C ABI, inputs in pinned host memory."""
+    import ctypes as ct
+    import numpy as np
+    import torch
+    from elphbolt_gb300 import _lib
+    L = _lib.load()
+    c = wd.crystal
+
+    def pin(a, dtype):
+        t = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(np.asarray(a, dtype=dtype)).ravel(order="F")))
+        return t.pin_memory()
+
+    arrs = {k: pin(v, d) for k, v, d in [
+        ("lat", c.lattvecs, np.float64), ("bas", c.basis, np.float64), ("mas", c.masses, np.float64),
+        ("rk", wd.rcells_k, np.int64), ("rq", wd.rcells_q, np.int64), ("rg", wd.rcells_g, np.int64),
+        ("dk", wd.elwsdeg, np.int64), ("dq", wd.phwsdeg, np.int64), ("dg", wd.gwsdeg, np.int64),
+        ("H", np.asfortranarray(wd.Hwann), np.complex128),
+        ("D", np.asfortranarray(wd.Dphwann), np.complex128), ("G", np.asfortranarray(wd.gwann), np.complex128)]}
+    d = _lib.WannierDesc()
+    d.numwannbands, d.numbranches = wd.numwannbands, wd.numbranches
+    d.nwsk, d.nwsq, d.nwsg, d.numatoms = wd.nwsk, wd.nwsq, wd.nwsg, c.numatoms
+    for i in range(3):
+        d.coarse_qmesh[i] = int(wd.coarse_qmesh[i])
+    dp = lambda t: ct.cast(t.data_ptr(), _lib.c_dp)
+    ip = lambda t: ct.cast(t.data_ptr(), _lib.c_i64p)
+    d.lattvecs, d.basis, d.masses = dp(arrs["lat"]), dp(arrs["bas"]), dp(arrs["mas"])
+    d.rcells_k, d.rcells_q, d.rcells_g = ip(arrs["rk"]), ip(arrs["rq"]), ip(arrs["rg"])
+    d.elwsdeg, d.phwsdeg, d.gwsdeg = ip(arrs["dk"]), ip(arrs["dq"]), ip(arrs["dg"])
+    d.Hwann, d.Dphwann, d.gwann = dp(arrs["H"]), dp(arrs["D"]), dp(arrs["G"])
+    r = _lib.RateRequest()
+    for i in range(3):
+        r.mesh[i] = int(req.mesh[i])
+    r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+    r.delta_kind, r.sigma, r.precision = int(req.delta_kind), float(req.sigma), int(prec)
+    N = int(np.prod(req.mesh))
+    rates = torch.zeros(N * wd.numwannbands, dtype=torch.float64).pin_memory()
+    idx = torch.zeros(N, dtype=torch.int64).pin_memory()
+    stats = _lib.RateStats()
+    h2d = sum(t.numel() * t.element_size() for t in arrs.values())
+    d2h = rates.numel() * 8 + idx.numel() * 8
+    vert = 0
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(steps):
+        h = ct.c_void_p()
+        _lib.check(L.ephg_create(ct.byref(d), ct.byref(h)))
+        _lib.check(L.ephg_el_rates(h, ct.byref(r), dp(rates), ip(idx), ct.byref(stats), None, None, None, 0))
+        _lib.check(L.ephg_destroy(h))
+        vert += stats.vertices
+    torch.cuda.synchronize()
+    t = time.time() - t0
+    return {"value": vert / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "steps": steps, "ms_per_step": 1e3 * t / steps,
+            "flow": "ephg_create (upload from pinned host) + ephg_el_rates (host rates out) + ephg_destroy"}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1 and args.impl == "ours":
+        # one GPU per rank: each replica sees only its own device
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

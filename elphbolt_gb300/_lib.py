@@ -61,7 +61,9 @@ class RateStats(ct.Structure):
                 ("vertices", ct.c_int64), ("pairs", ct.c_int64), ("kernel_launches", ct.c_int64),
                 ("ms_setup", ct.c_double), ("ms_stage_a", ct.c_double),
                 ("ms_stage_bc", ct.c_double), ("ms_total", ct.c_double),
-                ("stage_b_gflop", ct.c_double), ("stage_a_gflop", ct.c_double)]
+                ("stage_b_gflop", ct.c_double), ("stage_a_gflop", ct.c_double),
+                ("ms_gemm_a", ct.c_double), ("ms_gemm_b", ct.c_double),
+                ("gemm_a_launches", ct.c_int64), ("gemm_b_launches", ct.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

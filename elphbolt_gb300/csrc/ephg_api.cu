@@ -113,9 +113,11 @@ struct ephg_handle {
   double *ent_den = nullptr, *rcartq = nullptr;
   double2 *D = nullptr;
   PhTerms terms;
+  int *kposk = nullptr, *kposq = nullptr;   // split-form contraction order (far cells first)
   int *err = nullptr;        // device error word
   Workspace ws;
   tc::SplitOperands split;   // split-TF32 operand planes (lazy)
+  LaunchTimer timer_a, timer_b;   // device time of the contraction launches of the last request
   int64_t launches = 0;
 };
 
@@ -164,7 +166,7 @@ int ephg_destroy(ephg_handle *h) {
   if (!h) return EPHG_OK;
   void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->graw, h->G64,
                   h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_den,
-                  h->rcartq, h->D, h->err};
+                  h->rcartq, h->D, h->err, h->kposk, h->kposq};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   h->ws.release();
@@ -312,6 +314,27 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
     h->terms.nwsq = nwsq;
     h->terms.nb = nb;
     h->terms.nat = h->nat;
+  }
+  // contraction order of the split form: cells by decreasing |R| (ties by index),
+  // so that the decaying Wannier-space terms are summed smallest first
+  {
+    auto order = [&](const std::vector<int> &r, int n) {
+      std::vector<double> len(n);
+      for (int i = 0; i < n; ++i) {
+        double c[3];
+        for (int d = 0; d < 3; ++d)
+          c[d] = h->lattvecs[d] * r[3 * i] + h->lattvecs[d + 3] * r[3 * i + 1] + h->lattvecs[d + 6] * r[3 * i + 2];
+        len[i] = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      }
+      std::vector<int> idx(n), pos(n);
+      for (int i = 0; i < n; ++i) idx[i] = i;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return len[a] > len[b]; });
+      for (int p = 0; p < n; ++p) pos[idx[p]] = p;
+      return pos;
+    };
+    std::vector<int> pk = order(rk, nwsk), pq = order(rq, nwsq);
+    if ((rc = upload(&h->kposk, pk.data(), pk.size(), h->st)) || (rc = upload(&h->kposq, pq.data(), pq.size(), h->st)))
+      return bail(rc);
   }
   if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaMalloc err"));
   if (cudaMemsetAsync(h->err, 0, sizeof(int), h->st) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "memset"));
@@ -612,6 +635,8 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   int rc;
   int64_t launches0 = h->launches;
   EvTimer ev;
+  h->timer_a.reset();
+  h->timer_b.reset();
   CK(cudaEventRecord(ev.e[0], st));
   // ---- set-up: electrons on the full mesh (el_wann, electron.f90:364) ----
   double2 *roots, *P, *Hk, *V, *Dq, *Vq, *u;
@@ -767,7 +792,9 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
       int n = (int)std::min<int64_t>(kc, nwv - i0);
       launch_phase_mesh(n, widx + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
+      h->timer_a.begin(st);
       launch_zgemm(n, (int)Nn, nwsk, Pk, nwsk, h->G64, Nn, gk, Nn, st);
+      h->timer_a.end(st);
       // the rotation writes B columns of states [j0, j1) (grid.y <= 32768 per launch)
       for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
         int je = std::min(j1, j0 + 32768);
@@ -783,14 +810,17 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     h->launches += 1;
     for (int64_t j0 = 0; j0 < nst; j0 += sc) {
       int ns = (int)std::min<int64_t>(sc, nst - j0);
+      h->timer_b.begin(st);
       launch_zgemm(nwv, ns * ncol, nwsq, Pq, nwsq, B + j0 * ncol, ldb, Cb, (int64_t)ns * ncol, st);
+      h->timer_b.end(st);
       launch_epilogue_fp64(nwv, (int)j0, (int)j0 + ns, Cb, (int64_t)ns * ncol, rp, ed, partial, nblk, st);
       h->launches += 2;
     }
   } else {
     rc = tc::split_rates_stage(h->split, h->ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
-                               mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->Rq,
-                               h->degq, V, rp, ed, partial, nblk, ev.e[2], &h->launches);
+                               mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->kposk,
+                               h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk, ev.e[2],
+                               &h->launches, &h->timer_a, &h->timer_b);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
   }
   CKL();
@@ -825,6 +855,10 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     stats->ms_total = t03;
     stats->stage_a_gflop = 8.0 * (double)nwv * nwsk * (double)Nn * 1e-9;
     stats->stage_b_gflop = 8.0 * (double)nwv * nwsq * (double)ncol * nst * 1e-9;
+    stats->ms_gemm_a = h->timer_a.total_ms();
+    stats->ms_gemm_b = h->timer_b.total_ms();
+    stats->gemm_a_launches = h->timer_a.n;
+    stats->gemm_b_launches = h->timer_b.n;
   }
   return EPHG_OK;
 }

@@ -11,6 +11,17 @@
 // (hi_re, hi_im, lo_re, lo_im) with hi = tf32(X) and lo = tf32(X - hi); each
 // real product uses hi*hi + hi*lo + lo*hi (the "3xTF32" split), FP32
 // accumulation.  -Im*Im terms use the instruction descriptor's negate-A bit.
+//
+// Accuracy.  The tensor core's FP32 accumulation truncates toward zero, so a
+// long chain of MMAs into one accumulator drifts low (measured: -6e-6 relative
+// on a 279-term complex dot product with the largest terms first).  Two
+// measures keep the chain short: the hi*lo + lo*hi correction products go to
+// their own accumulators (2^-11 smaller, so their truncation is negligible), the
+// two chains being added in the CUDA cores with round-to-nearest; the
+// contraction index is ordered by decreasing |R|, i.e. by increasing size of
+// the decaying Wannier-space terms, so the main accumulator is small while most
+// truncations happen; and the last K block (the nearest cells, the largest
+// terms) is accumulated in the short correction chain.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -49,7 +60,7 @@ constexpr int BK = 16;           // K per stage: 16 fp32 = 64 B rows, SWIZZLE_64
 constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
 constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
-constexpr int TMEM_COLS = 512;                        // 2 buffers x (re 128 + im 128)
+constexpr int TMEM_COLS = 512;                        // main re, main im, corr re, corr im (128 each)
 constexpr int GEMM_THREADS = 192;                     // 6 warps
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
@@ -224,12 +235,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       uint32_t phase = 0;
       int it = 0;
       bool ok = true;
+      const uint32_t mr = tmem, mi = tmem + BN, cr = tmem + 2 * BN, ci = tmem + 3 * BN;
       for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
-        const int buf = it & 1;
-        const uint32_t tph = (it >> 1) & 1;
-        if (!mbar_wait(&tempty[buf], tph ^ 1, g.err)) { ok = false; break; }
+        if (!mbar_wait(&tempty[0], (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t accr = tmem + buf * 2 * BN, acci = accr + BN;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&full[stage], phase, g.err)) { ok = false; break; }
           tc_fence_after();
@@ -241,26 +250,31 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             const uint64_t Alr = sdesc(sb + 2 * PLANE_BYTES + off), Ali = sdesc(sb + 3 * PLANE_BYTES + off);
             const uint64_t Bhr = sdesc(sb + 4 * PLANE_BYTES + off), Bhi = sdesc(sb + 5 * PLANE_BYTES + off);
             const uint64_t Blr = sdesc(sb + 6 * PLANE_BYTES + off), Bli = sdesc(sb + 7 * PLANE_BYTES + off);
-            const uint32_t first = (kb == 0 && ks == 0) ? 0u : 1u;
-            // Re = Ar Br - Ai Bi
-            umma(accr, Ahr, Bhr, IDP, first);
-            umma(accr, Ahr, Blr, IDP, 1);
-            umma(accr, Alr, Bhr, IDP, 1);
-            umma(accr, Ahi, Bhi, IDN, 1);
-            umma(accr, Ahi, Bli, IDN, 1);
-            umma(accr, Ali, Bhi, IDN, 1);
-            // Im = Ar Bi + Ai Br
-            umma(acci, Ahr, Bhi, IDP, first);
-            umma(acci, Ahr, Bli, IDP, 1);
-            umma(acci, Alr, Bhi, IDP, 1);
-            umma(acci, Ahi, Bhr, IDP, 1);
-            umma(acci, Ahi, Blr, IDP, 1);
-            umma(acci, Ali, Bhr, IDP, 1);
+            const uint32_t acc = (kb == 0 && ks == 0) ? 0u : 1u;
+            // corrections: hi*lo + lo*hi
+            umma(cr, Ahr, Blr, IDP, acc);
+            umma(cr, Alr, Bhr, IDP, 1);
+            umma(cr, Ahi, Bli, IDN, 1);
+            umma(cr, Ali, Bhi, IDN, 1);
+            umma(ci, Ahr, Bli, IDP, acc);
+            umma(ci, Alr, Bhi, IDP, 1);
+            umma(ci, Ahi, Blr, IDP, 1);
+            umma(ci, Ali, Bhr, IDP, 1);
+            // main: Re = Ar Br - Ai Bi, Im = Ar Bi + Ai Br (hi parts).  The last K
+            // block holds the nearest cells, the largest terms: they go to the
+            // short correction chain instead of the long main chain.
+            const bool nearblk = (kb == g.nkb - 1) && g.nkb > 1;
+            const uint32_t dr = nearblk ? cr : mr, di = nearblk ? ci : mi;
+            const uint32_t am = nearblk ? 1u : acc;
+            umma(dr, Ahr, Bhr, IDP, am);
+            umma(dr, Ahi, Bhi, IDN, 1);
+            umma(di, Ahr, Bhi, IDP, am);
+            umma(di, Ahi, Bhr, IDP, 1);
           }
           umma_commit(&empty[stage]);     // frees the smem stage when these MMAs retire
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
-        if (ok) umma_commit(&tfull[buf]);   // accumulator ready for the epilogue
+        if (ok) umma_commit(&tfull[0]);   // accumulators ready for the epilogue
       }
     }
   } else {   // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4
@@ -269,18 +283,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     int it = 0;
     for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
       const int mt = t % g.mtiles, nt = t / g.mtiles;
-      const int buf = it & 1;
-      const uint32_t tph = (it >> 1) & 1;
-      if (!mbar_wait(&tfull[buf], tph, g.err)) break;
+      if (!mbar_wait(&tfull[0], it & 1, g.err)) break;
       tc_fence_after();
-      const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16) + buf * 2 * BN;
+      const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
       float *cr = g.Cr + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
       float *ci = g.Ci + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 16) {
-        float vr[16], vi[16];
+        float vr[16], vi[16], wr[16], wi[16];
         tmem_ld16(tr + c0, vr);
         tmem_ld16(tr + BN + c0, vi);
+        tmem_ld16(tr + 2 * BN + c0, wr);
+        tmem_ld16(tr + 3 * BN + c0, wi);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          vr[q] += wr[q];
+          vi[q] += wi[q];
+        }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           *(float4 *)(cr + c0 + 4 * q) = make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]);
@@ -288,7 +307,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
       }
       tc_fence_before();
-      mbar_arrive(&tempty[buf]);
+      mbar_arrive(&tempty[0]);
     }
   }
   __syncthreads();
@@ -405,18 +424,20 @@ __device__ inline int phase_idx(int p, int m1, int m2, int m3, int L, int r1, in
 }
 
 // A planes of e^{2 pi i k.R} (/ deg) for the rows k = rowp[0..nrows): [4][Mp][Kp]
+// (column of cell r = kpos[r]: the contraction order, far cells first)
 __global__ void k_phase_planes(int nrows, const int *rowp, int m1, int m2, int m3, int L, int nR, const int *R,
-                               const double *deg, const double2 *roots, float *P, int Mp, int Kp) {
+                               const double *deg, const int *kpos, const double2 *roots, float *P, int Mp, int Kp) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)nrows * nR) return;
   int row = (int)(idx / nR), r = (int)(idx % nR);
   double2 v = roots[phase_idx(rowp[row], m1, m2, m3, L, R[3 * r], R[3 * r + 1], R[3 * r + 2])];
   if (deg) v = make_double2(v.x / deg[r], v.y / deg[r]);
-  put4(P, (int64_t)Mp * Kp, (int64_t)row * Kp + r, v);
+  put4(P, (int64_t)Mp * Kp, (int64_t)row * Kp + kpos[r], v);
 }
 
-// B planes of the stage-A matrix: G64[Re][n] -> planes [4][Np][Kp] (transposed)
-__global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, float *P, int64_t Np, int Kp) {
+// B planes of the stage-A matrix: G64[Re][n] -> planes [4][Np][Kp] (transposed,
+// column of Re = kpos[Re], or Re itself when kpos is null)
+__global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, const int *kpos, float *P, int64_t Np, int Kp) {
   __shared__ double2 tile[32][33];
   int64_t n0 = (int64_t)blockIdx.x * 32;
   int r0 = blockIdx.y * 32;
@@ -429,7 +450,7 @@ __global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, float *P, int6
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     int64_t n = n0 + i;
     int re = r0 + threadIdx.x;
-    if (n < Nn && re < Kp) put4(P, Np * Kp, n * Kp + re, tile[threadIdx.x][i]);
+    if (n < Nn && re < nwsk) put4(P, Np * Kp, n * Kp + (kpos ? kpos[re] : re), tile[threadIdx.x][i]);
   }
 }
 
@@ -438,7 +459,7 @@ __global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, float *P, int6
 __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int nw, int nb, int nws,
                                 const int *widx, const double2 *U, const float *gr, const float *gi, int64_t ldg,
                                 int m1, int m2, int m3, int L, const double2 *roots, const int *Rq,
-                                const double *degq, float *Bp, int64_t Np2, int Kp2, int jbase) {
+                                const double *degq, const int *kpos, float *Bp, int64_t Np2, int Kp2, int jbase) {
   const int j = j0 + blockIdx.y;
   if (j >= j1) return;
   const int code = st_code[j];
@@ -458,7 +479,7 @@ __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int 
       cfma(acc, Uk[mp], make_double2((double)gr[off], (double)gi[off]));
     }
     const int64_t col = (int64_t)(j - jbase) * ncol + c;
-    put4(Bp, Np2 * Kp2, col * Kp2 + rp, cmul(ph, acc));
+    put4(Bp, Np2 * Kp2, col * Kp2 + kpos[rp], cmul(ph, acc));
   }
 }
 
@@ -577,9 +598,9 @@ static inline int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk, int nwsq,
                       int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
                       const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
-                      const double *degk, const int *Rq, const double *degq, const double2 *U,
-                      const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, cudaEvent_t ev_stage_a,
-                      int64_t *launches) {
+                      const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
+                      const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk,
+                      cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
   int rc;
   int *err = nullptr;
   // the device error word lives in the workspace; the caller checks its own word afterwards
@@ -592,7 +613,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     TCK(cudaMalloc(&s.G, (size_t)4 * NpA * KpA * sizeof(float)));
     TCK(cudaMemsetAsync(s.G, 0, (size_t)4 * NpA * KpA * sizeof(float), st));
     dim3 grid((unsigned)((Nn + 31) / 32), (unsigned)((KpA + 31) / 32));
-    k_gplanes<<<grid, dim3(32, 8), 0, st>>>(Nn, nwsk, G64, s.G, NpA, KpA);
+    k_gplanes<<<grid, dim3(32, 8), 0, st>>>(Nn, nwsk, G64, kposA, s.G, NpA, KpA);
     TCK(cudaGetLastError());
     s.Nn = NpA;
     s.Kp = KpA;
@@ -613,14 +634,16 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
     int64_t ne = (int64_t)n * nwsk;
     k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(n, widx + i0, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
-                                                                 degk, roots, PA, Mp, KpA);
+                                                                 degk, kposA, roots, PA, Mp, KpA);
     TCK(cudaGetLastError());
+    tA->begin(st);
     if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st))) return rc;
+    tA->end(st);
     for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
       int je = std::min(j1, j0 + 32768);
       dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
       k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, U, CAr, CAi, NpA, mesh[0],
-                                           mesh[1], mesh[2], L, roots, Rq, degq, B2, Np2, KpB, 0);
+                                           mesh[1], mesh[2], L, roots, Rq, degq, kposB, B2, Np2, KpB, 0);
       TCK(cudaGetLastError());
       (*launches)++;
     }
@@ -643,7 +666,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   {
     int64_t ne = (int64_t)nwv * nwsq;
     k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, widx, mesh[0], mesh[1], mesh[2], L, nwsq, Rq,
-                                                                 nullptr, roots, PB, MpB, KpB);
+                                                                 nullptr, kposB, roots, PB, MpB, KpB);
     TCK(cudaGetLastError());
   }
   // fp32 copies of the eigenvectors and per-(q,s) tables for the epilogue
@@ -665,7 +688,9 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
+    tB->begin(st);
     if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st))) return rc;
+    tB->end(st);
     dim3 grid(nblk, ns);
     if (rp.delta_kind == 0) {
       k_epilogue_split<<<grid, 128, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
@@ -732,7 +757,7 @@ extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A
   cudaMemset(err, 0, 4);
   k_planes_rows<<<(unsigned)((M * K + 255) / 256), 256>>>(M, (int)K, dA, PA, Mp, (int)Kp);
   dim3 grid((unsigned)((N + 31) / 32), (unsigned)((Kp + 31) / 32));
-  k_gplanes<<<grid, dim3(32, 8)>>>(N, (int)K, dB, PB, Np, (int)Kp);
+  k_gplanes<<<grid, dim3(32, 8)>>>(N, (int)K, dB, nullptr, PB, Np, (int)Kp);
   rc = cgemm(PA, Mp, 0, (int)Mp, PB, Np, 0, (int)Np, (int)Kp, Cr, Ci, Np, err, st);
   if (!rc) {
     k_join<<<(unsigned)((M * N + 255) / 256), 256>>>(M, N, Cr, Ci, Np, dC);

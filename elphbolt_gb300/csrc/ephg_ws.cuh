@@ -6,6 +6,7 @@
 #include <map>
 #include <string>
 #include <utility>
+#include <vector>
 
 namespace ephg {
 
@@ -52,5 +53,39 @@ int wsget(Workspace &ws, const char *name, size_t count, T **out) {
   *out = (T *)p;
   return rc;
 }
+
+// Device-time accumulator for a family of kernel launches: mark() before and
+// after each launch on the launching stream, total_ms() after a stream sync.
+struct LaunchTimer {
+  std::vector<cudaEvent_t> ev;
+  size_t used = 0;
+  int n = 0;
+  void reset() { used = 0; n = 0; }
+  void mark(cudaStream_t st) {
+    if (used == ev.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev.push_back(e);
+    }
+    cudaEventRecord(ev[used++], st);
+  }
+  void begin(cudaStream_t st) { mark(st); }
+  void end(cudaStream_t st) {
+    mark(st);
+    ++n;
+  }
+  double total_ms() const {
+    double t = 0;
+    for (size_t i = 0; i + 1 < used; i += 2) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      t += ms;
+    }
+    return t;
+  }
+  ~LaunchTimer() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
 
 }  // namespace ephg

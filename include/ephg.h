@@ -95,6 +95,10 @@ typedef struct {
   double ms_total;            /* device time of the whole call */
   double stage_b_gflop;       /* algorithmic GFLOP of the Rp Fourier contraction */
   double stage_a_gflop;       /* algorithmic GFLOP of the Re contraction */
+  double ms_gemm_a;           /* summed device time of the stage-A contraction launches */
+  double ms_gemm_b;           /* summed device time of the stage-B contraction launches */
+  int64_t gemm_a_launches;
+  int64_t gemm_b_launches;
 } ephg_rate_stats;
 
 /* Upload the Wannier data once; the returned handle keeps it resident in HBM

@@ -12,9 +12,16 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+
+static double wall_us(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec * 1e6 + ts.tv_nsec * 1e-3;
+}
 
 typedef double complex cplx;
 
@@ -740,15 +747,30 @@ static double delta_eval(const delta_ctx *c, double e, int64_t ikp, int64_t n) {
  * group (IBZ blocks = FBZ blocks), q on the electron mesh (mesh_ref = 1) and no
  * disk: |g|^2, X+- and rates are formed state by state in memory.
  */
-int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
-                int nthreads, int literal, double *rates, int64_t *indexlist,
-                int64_t *info, double *g2out, double *xpout, double *xmout, int64_t cap) {
-  const int64_t nw = w->nw, nb = w->nb, nwsq = w->nwsq;
+struct or_rates_ctx {
+  const or_wannier *w;
+  or_request req;
+  int64_t N, nwv, nin, status, us_setup;
+  int64_t *indexlist;
+  double *kfull, *ens_full, *kw, *ens, *evecs, *phe, *phv;
+  int64_t *simplex, *scount, *smap;
+  double *se;
+  delta_ctx dc;
+};
+
+/* Set-up of the ibzk driver: FBZ energies, window, window eigenvectors,
+ * phonons on the q mesh, simplices (electron.f90:321-595, phonon.f90:159-230). */
+or_rates_ctx *or_rates_setup(const or_wannier *w, const or_request *req, int nthreads) {
+  const int64_t nw = w->nw, nb = w->nb;
   const int64_t *mesh = req->mesh;
   const int64_t N = mesh[0] * mesh[1] * mesh[2];
-  const double const_tp = TWOPI / HBAR_EVPS;
-  const double g2unitfactor = RYD2EV * RYD2EV * RYD2EV * RYD2AMU;
-  for (int i = 0; i < 8; ++i) info[i] = 0;
+  or_rates_ctx *cx = (or_rates_ctx *)calloc(1, sizeof(or_rates_ctx));
+  cx->w = w;
+  cx->req = *req;
+  cx->N = N;
+  double t_start = wall_us();
+  int64_t *indexlist = (int64_t *)malloc(sizeof(int64_t) * (N > 0 ? N : 1));
+  cx->indexlist = indexlist;
   /* 1. FBZ wave vectors (crystal.f90:377-408) and energies */
   double *kfull = (double *)malloc(sizeof(double) * N * 3);
   for (int64_t i = 1; i <= N; ++i) {
@@ -765,8 +787,10 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
     for (int64_t b = 0; b < nw; ++b) if (fabs(ens_full[ik + N * b] - req->enref) <= req->fsthick) in = 1;
     if (in) indexlist[nwv++] = ik + 1;
   }
-  info[0] = nwv;
-  if (nwv == 0) { info[5] = 2; free(kfull); free(ens_full); return 2; }
+  cx->nwv = nwv;
+  cx->kfull = kfull;
+  cx->ens_full = ens_full;
+  if (nwv == 0) { cx->status = 2; return cx; }
   /* 3. window quantities: wave vectors, energies, eigenvectors */
   double *kw = (double *)malloc(sizeof(double) * nwv * 3);
   for (int64_t i = 0; i < nwv; ++i)
@@ -777,7 +801,10 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
   int64_t nin = 0;
   for (int64_t i = 0; i < nwv; ++i)
     for (int64_t b = 0; b < nw; ++b) if (fabs(ens[i + nwv * b] - req->enref) <= req->fsthick) nin++;
-  info[1] = nin;
+  cx->nin = nin;
+  cx->kw = kw;
+  cx->ens = ens;
+  cx->evecs = evecs;
   /* 4. phonons on the full q mesh (phonon.f90:208-214, q mesh = k mesh) */
   double *phe = (double *)malloc(sizeof(double) * N * nb);
   double *phv = (double *)malloc(sizeof(double) * 2 * N * nb * nb);
@@ -807,7 +834,9 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
       free(q); free(e); free(v);
     }
   }
-  if (phs) info[5] = 1;
+  cx->phe = phe;
+  cx->phv = phv;
+  if (phs) cx->status = 1;
   /* 5. simplices for the triangle / tetrahedron deltas */
   delta_ctx dc;
   memset(&dc, 0, sizeof dc);
@@ -828,6 +857,45 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
     or_fill_simplices(dc.nsimplex, nv, simplex, nwv, nw, ens, se);
     dc.map = smap; dc.count = scount; dc.se = se;
   }
+  cx->simplex = simplex;
+  cx->scount = scount;
+  cx->smap = smap;
+  cx->se = se;
+  cx->dc = dc;
+  cx->us_setup = (int64_t)(wall_us() - t_start);
+  return cx;
+}
+
+void or_rates_free(or_rates_ctx *cx) {
+  if (!cx) return;
+  free(cx->indexlist); free(cx->kfull); free(cx->ens_full); free(cx->kw); free(cx->ens);
+  free(cx->evecs); free(cx->phe); free(cx->phv); free(cx->simplex); free(cx->scount);
+  free(cx->smap); free(cx->se);
+  free(cx);
+}
+
+/* The per-state part of the ibzk driver ('g' + 'X', interactions.f90:2169-2400)
+ * and the rate sums (interactions.f90:3001-3034) for the in-window initial
+ * states of rank [state_begin, state_begin + nstates) (nstates < 0: all). */
+int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nthreads,
+                 int literal, double *rates, int64_t *indexlist, int64_t *info,
+                 double *g2out, double *xpout, double *xmout, int64_t cap) {
+  const or_wannier *w = cx->w;
+  const or_request *req = &cx->req;
+  const int64_t nw = w->nw, nb = w->nb, nwsq = w->nwsq;
+  const int64_t *mesh = req->mesh;
+  const int64_t N = cx->N, nwv = cx->nwv, nin = cx->nin;
+  const double const_tp = TWOPI / HBAR_EVPS;
+  const double g2unitfactor = RYD2EV * RYD2EV * RYD2EV * RYD2AMU;
+  const double *kw = cx->kw, *ens = cx->ens, *evecs = cx->evecs, *phe = cx->phe, *phv = cx->phv;
+  const delta_ctx dc = cx->dc;
+  for (int i = 0; i < 8; ++i) info[i] = 0;
+  info[0] = nwv;
+  info[1] = nin;
+  info[5] = cx->status;
+  info[6] = cx->us_setup;
+  for (int64_t i = 0; i < nwv; ++i) indexlist[i] = cx->indexlist[i];
+  if (cx->status == 2) return 2;
   /* 6. in-window initial states in istate order, optionally truncated */
   int64_t nst_all = nwv * nw;
   int64_t *rank = (int64_t *)malloc(sizeof(int64_t) * nst_all);
@@ -837,33 +905,42 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
     or_demux_state(istate, nw, &m, &ik);
     rank[istate - 1] = -1;
     if (fabs(ens[(ik - 1) + nwv * (m - 1)] - req->enref) > req->fsthick) continue;
-    if (max_states >= 0 && nsel >= max_states) continue;
-    rank[istate - 1] = nsel++;
+    int64_t k = nsel++;
+    if (k < state_begin || (nstates >= 0 && k >= state_begin + nstates)) continue;
+    rank[istate - 1] = k - state_begin;
   }
+  nsel = 0;
+  for (int64_t i = 0; i < nst_all; ++i) nsel += rank[i] >= 0;
   info[2] = nsel;
   int64_t per_state = nin * nb;     /* count per initial state: same for every state */
   info[3] = nsel * per_state;
   info[4] = nsel * nwv;
   for (int64_t i = 0; i < N * nw; ++i) rates[i] = 0.0;
-  /* 7. per IBZ k: gkRp, then its in-window states (parallel over k) */
+  double t_loop = wall_us();
+  /* 7. per IBZ k (serial, as one image walks its states): gkRp, then for each
+   *    in-window state the k' loop, split over OpenMP threads; X+- are stored per
+   *    vertex and summed in the reference's order afterwards. */
   int nt = nthreads > 0 ? nthreads : 1;
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+  int64_t *koff = (int64_t *)malloc(sizeof(int64_t) * (nwv + 1));   /* first vertex of k' */
+  koff[0] = 0;
+  for (int64_t ikp = 1; ikp <= nwv; ++ikp) {
+    int64_t c = 0;
+    for (int64_t n = 1; n <= nw; ++n) c += fabs(ens[(ikp - 1) + nwv * (n - 1)] - req->enref) <= req->fsthick;
+    koff[ikp] = koff[ikp - 1] + c * nb;
+  }
+  const int64_t gsz = nw * nw * nb * nwsq;
+  double *gk = (double *)malloc(sizeof(double) * 2 * gsz);
+  double *xp = (double *)malloc(sizeof(double) * (per_state > 0 ? per_state : 1));
+  double *xm = (double *)malloc(sizeof(double) * (per_state > 0 ? per_state : 1));
+  double *g2l = (double *)malloc(sizeof(double) * (per_state > 0 ? per_state : 1));
+  cplx *gkm = (cplx *)malloc(sizeof(cplx) * nw * nb * nwsq);   /* restructured form */
+  double *evk = (double *)malloc(sizeof(double) * 2 * nw);
   for (int64_t ik = 1; ik <= nwv; ++ik) {
     int any = 0;
     for (int64_t m = 1; m <= nw; ++m) if (rank[(ik - 1) * nw + m - 1] >= 0) any = 1;
     if (!any) continue;
-    const int64_t gsz = nw * nw * nb * nwsq;
-    double *gk = (double *)malloc(sizeof(double) * 2 * gsz);
     double kv[3] = {kw[ik - 1], kw[(ik - 1) + nwv], kw[(ik - 1) + 2 * nwv]};
     or_gkRp(w, kv, gk);
-    double *evk = (double *)malloc(sizeof(double) * 2 * nw);
-    double *evkp = (double *)malloc(sizeof(double) * 2 * nw);
-    double *evq = (double *)malloc(sizeof(double) * 2 * nb);
-    double *xp = (double *)malloc(sizeof(double) * per_state);
-    double *xm = (double *)malloc(sizeof(double) * per_state);
-    double *g2l = (double *)malloc(sizeof(double) * per_state);
-    cplx *gkm = (cplx *)malloc(sizeof(cplx) * nw * nb * nwsq);   /* restructured form */
-    cplx *ph = (cplx *)malloc(sizeof(cplx) * nwsq);
     for (int64_t m = 1; m <= nw; ++m) {
       int64_t istate = (ik - 1) * nw + m;
       int64_t r = rank[istate - 1];
@@ -884,91 +961,107 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
               gkm[np + nw * (s + nb * rp)] = a;
             }
       }
-      int64_t cnt = 0;
-      int64_t kint[3];
-      or_demux_vector(indexlist[ik - 1], kint, mesh, 0);
-      for (int64_t ikp = 1; ikp <= nwv; ++ikp) {
-        /* q = k' - k on the electron mesh (vector.f90:86-102), ph mesh = el mesh */
-        int64_t qi[3], qmux;
-        double qf[3], qc[3];
-        double prim[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-        or_vector_addsub(indexlist[ikp - 1], indexlist[ik - 1], -1, mesh, prim, qi, &qmux, qf, qc);
-        int64_t iq = qmux;   /* change_grid to the same mesh keeps the index */
-        double qv[3] = {qf[0], qf[1], qf[2]};
-        if (!literal) {
-          for (int64_t rp = 0; rp < nwsq; ++rp) {
-            double dot = 0.0;
-            for (int d = 0; d < 3; ++d) dot += qv[d] * (double)w->rcells_q[rp + nwsq * d];
-            ph[rp] = expi(TWOPI * dot) / (double)w->phwsdeg[rp];
-          }
-        }
-        for (int64_t n = 1; n <= nw; ++n) {
-          if (fabs(ens[(ikp - 1) + nwv * (n - 1)] - req->enref) > req->fsthick) continue;
-          for (int64_t c = 0; c < nw; ++c) {
-            evkp[2 * c] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c))];
-            evkp[2 * c + 1] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c)) + 1];
-          }
-          cplx hs[64];
+#pragma omp parallel num_threads(nt)
+      {
+        double *evkp = (double *)malloc(sizeof(double) * 2 * nw);
+        double *evq = (double *)malloc(sizeof(double) * 2 * nb);
+        cplx *ph = (cplx *)malloc(sizeof(cplx) * nwsq);
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t ikp = 1; ikp <= nwv; ++ikp) {
+          /* q = k' - k on the electron mesh (vector.f90:86-102), ph mesh = el mesh */
+          int64_t qi[3], qmux;
+          double qf[3], qc[3];
+          double prim[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+          or_vector_addsub(indexlist[ikp - 1], indexlist[ik - 1], -1, mesh, prim, qi, &qmux, qf, qc);
+          int64_t iq = qmux;   /* change_grid to the same mesh keeps the index */
+          double qv[3] = {qf[0], qf[1], qf[2]};
           if (!literal) {
-            /* h(s') = sum_Rp phase * sum_n' conj(U_k'[n][n']) gkm(n', s', Rp) */
-            for (int64_t s = 0; s < nb; ++s) hs[s] = 0.0;
-            for (int64_t rp = 0; rp < nwsq; ++rp)
-              for (int64_t s = 0; s < nb; ++s) {
-                cplx a = 0.0;
-                for (int64_t np = 0; np < nw; ++np) a += conj(cget(evkp, np)) * gkm[np + nw * (s + nb * rp)];
-                hs[s] += ph[rp] * a;
-              }
+            for (int64_t rp = 0; rp < nwsq; ++rp) {
+              double dot = 0.0;
+              for (int d = 0; d < 3; ++d) dot += qv[d] * (double)w->rcells_q[rp + nwsq * d];
+              ph[rp] = expi(TWOPI * dot) / (double)w->phwsdeg[rp];
+            }
           }
-          for (int64_t s = 1; s <= nb; ++s) {
-            double en_ph = phe[(iq - 1) + N * (s - 1)];
-            for (int64_t c = 0; c < nb; ++c) {
-              evq[2 * c] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c))];
-              evq[2 * c + 1] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c)) + 1];
+          int64_t cnt = koff[ikp - 1];
+          for (int64_t n = 1; n <= nw; ++n) {
+            if (fabs(ens[(ikp - 1) + nwv * (n - 1)] - req->enref) > req->fsthick) continue;
+            for (int64_t c = 0; c < nw; ++c) {
+              evkp[2 * c] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c))];
+              evkp[2 * c + 1] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c)) + 1];
             }
-            double g2;
-            if (literal) {
-              g2 = or_g2(w, kv, qv, evk, evkp, evq, en_ph, gk, 1);
-            } else if (en_ph == 0) {
-              g2 = 0.0;
-            } else {
-              cplx gb = 0.0;
-              for (int64_t sp = 0; sp < nb; ++sp) gb += cget(evq, sp) / sqrt(w->masses[sp / 3]) * hs[sp];
-              g2 = 0.5 * creal(gb * conj(gb)) / en_ph * g2unitfactor;
+            cplx hs[64];
+            if (!literal) {
+              /* h(s') = sum_Rp phase * sum_n' conj(U_k'[n][n']) gkm(n', s', Rp) */
+              for (int64_t s = 0; s < nb; ++s) hs[s] = 0.0;
+              for (int64_t rp = 0; rp < nwsq; ++rp)
+                for (int64_t s = 0; s < nb; ++s) {
+                  cplx a = 0.0;
+                  for (int64_t np = 0; np < nw; ++np) a += conj(cget(evkp, np)) * gkm[np + nw * (s + nb * rp)];
+                  hs[s] += ph[rp] * a;
+                }
             }
-            /* 'X' (:2278-2332) */
-            double bosefac = (en_ph != 0.0) ? or_Bose(en_ph, req->T) : 0.0;
-            double fp = or_Fermi(en_el + en_ph, req->chempot, req->T);
-            double fm = or_Fermi(en_el - en_ph, req->chempot, req->T);
-            double dp = delta_eval(&dc, en_el + en_ph, ikp, n);
-            double dm = delta_eval(&dc, en_el - en_ph, ikp, n);
-            double xplus = 0.0, xminus = 0.0;
-            if (en_ph >= 0.5e-3) {
-              xplus = g2 * (bosefac + fp) * dp;
-              xminus = g2 * (1.0 + bosefac - fm) * dm;
+            for (int64_t s = 1; s <= nb; ++s) {
+              double en_ph = phe[(iq - 1) + N * (s - 1)];
+              for (int64_t c = 0; c < nb; ++c) {
+                evq[2 * c] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c))];
+                evq[2 * c + 1] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c)) + 1];
+              }
+              double g2;
+              if (literal) {
+                g2 = or_g2(w, kv, qv, evk, evkp, evq, en_ph, gk, 1);
+              } else if (en_ph == 0) {
+                g2 = 0.0;
+              } else {
+                cplx gb = 0.0;
+                for (int64_t sp = 0; sp < nb; ++sp) gb += cget(evq, sp) / sqrt(w->masses[sp / 3]) * hs[sp];
+                g2 = 0.5 * creal(gb * conj(gb)) / en_ph * g2unitfactor;
+              }
+              /* 'X' (:2278-2332) */
+              double bosefac = (en_ph != 0.0) ? or_Bose(en_ph, req->T) : 0.0;
+              double fp = or_Fermi(en_el + en_ph, req->chempot, req->T);
+              double fm = or_Fermi(en_el - en_ph, req->chempot, req->T);
+              double dp = delta_eval(&dc, en_el + en_ph, ikp, n);
+              double dm = delta_eval(&dc, en_el - en_ph, ikp, n);
+              double xplus = 0.0, xminus = 0.0;
+              if (en_ph >= 0.5e-3) {
+                xplus = g2 * (bosefac + fp) * dp;
+                xminus = g2 * (1.0 + bosefac - fm) * dm;
+              }
+              g2l[cnt] = g2;
+              xp[cnt] = const_tp * xplus;
+              xm[cnt] = const_tp * xminus;
+              cnt++;
             }
-            g2l[cnt] = g2;
-            xp[cnt] = const_tp * xplus;
-            xm[cnt] = const_tp * xminus;
-            cnt++;
           }
         }
+        free(evkp); free(evq); free(ph);
       }
       /* rates: sum X+ then X- in order (:3012-3034) */
       double acc = 0.0;
-      for (int64_t i = 0; i < cnt; ++i) acc += xp[i];
-      for (int64_t i = 0; i < cnt; ++i) acc += xm[i];
+      for (int64_t i = 0; i < per_state; ++i) acc += xp[i];
+      for (int64_t i = 0; i < per_state; ++i) acc += xm[i];
       rates[(ik - 1) + N * (m - 1)] = acc;
       int64_t off = r * per_state;
-      for (int64_t i = 0; i < cnt; ++i)
+      for (int64_t i = 0; i < per_state; ++i)
         if (off + i < cap) {
           if (g2out) g2out[off + i] = g2l[i];
           if (xpout) xpout[off + i] = xp[i];
           if (xmout) xmout[off + i] = xm[i];
         }
     }
-    free(gk); free(evk); free(evkp); free(evq); free(xp); free(xm); free(g2l); free(gkm); free(ph);
   }
-  free(kfull); free(ens_full); free(kw); free(ens); free(evecs); free(phe); free(phv); free(rank);
-  free(simplex); free(scount); free(smap); free(se);
+  free(gk); free(xp); free(xm); free(g2l); free(gkm); free(evk); free(koff);
+  info[7] = (int64_t)(wall_us() - t_loop);
+  free(rank);
   return (int)info[5];
+}
+
+int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
+                int nthreads, int literal, double *rates, int64_t *indexlist,
+                int64_t *info, double *g2out, double *xpout, double *xmout, int64_t cap) {
+  or_rates_ctx *cx = or_rates_setup(w, req, nthreads);
+  int rc = or_rates_run(cx, 0, max_states, nthreads, literal, rates, indexlist, info, g2out, xpout,
+                        xmout, cap);
+  or_rates_free(cx);
+  return rc;
 }

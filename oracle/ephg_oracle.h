@@ -119,6 +119,8 @@ double or_delta_tetra(double e, int64_t ik, int64_t ib, const int64_t mesh[3], i
  * info[3]  vertices    total count increments (interactions.f90:2261)
  * info[4]  pairs       (initial state, k') pairs
  * info[5]  status      0 ok, 1 large negative phonon energy, 2 empty window
+ * info[6]  microseconds of set-up (meshes, eigensolves, phonons, simplices)
+ * info[7]  microseconds of the per-state loop (gkRp + |g|^2 + X + rates)
  * rates:      (N_k, nw) column-major, first info[0] rows valid (IBZ block order)
  * indexlist:  (N_k) muxed 1-based indices of the window k-points
  * g2/xp/xm:   optional per-vertex lists in the reference's order, capacity cap
@@ -131,6 +133,17 @@ double or_delta_tetra(double e, int64_t ik, int64_t ib, const int64_t mesh[3], i
 int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
                 int nthreads, int literal, double *rates, int64_t *indexlist,
                 int64_t *info, double *g2, double *xp, double *xm, int64_t cap);
+
+/* The same driver split in two, so that a timed sample of states does not
+ * repeat the set-up: or_rates_setup (steps up to the simplices), then
+ * or_rates_run on the in-window states of rank [state_begin, state_begin +
+ * nstates) (nstates < 0: all), or_rates_free.  Arguments as above. */
+typedef struct or_rates_ctx or_rates_ctx;
+or_rates_ctx *or_rates_setup(const or_wannier *w, const or_request *req, int nthreads);
+int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nthreads,
+                 int literal, double *rates, int64_t *indexlist, int64_t *info,
+                 double *g2, double *xp, double *xm, int64_t cap);
+void or_rates_free(or_rates_ctx *cx);
 
 #ifdef __cplusplus
 }

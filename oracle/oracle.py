@@ -182,7 +182,8 @@ class Wannier:
         nwv = int(info[0])
         out = dict(status=int(st), nwv=nwv, nstates_inwindow=int(info[1]),
                    nstates=int(info[2]), vertices=int(info[3]), pairs=int(info[4]),
-                   indexlist=idx[:nwv].copy(), rates=np.asfortranarray(rates[:nwv, :]))
+                   indexlist=idx[:nwv].copy(), rates=np.asfortranarray(rates[:nwv, :]),
+                   us_setup=int(info[6]), us_loop=int(info[7]))
         if vertices:
             nv = min(int(info[3]), c)
             out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
@@ -275,3 +276,49 @@ def herm_eig(A):
     V = np.zeros((n, n), dtype=np.complex128, order="F")
     sw = lib().or_herm_eig(ct.c_int64(n), _p(A), _p(w), _p(V))
     return w, V, sw
+
+
+class RatesRun:
+    """The oracle's rate driver with its set-up done once (or_rates_setup), so
+    that a timed sample of initial states (or_rates_run) excludes it."""
+
+    def __init__(self, W, req, nthreads=1):
+        L = lib()
+        L.or_rates_setup.restype = ct.c_void_p
+        L.or_rates_setup.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int]
+        L.or_rates_run.argtypes = [ct.c_void_p, ct.c_int64, ct.c_int64, ct.c_int, ct.c_int, c_dp, c_i64p,
+                                   c_i64p, c_dp, c_dp, c_dp, ct.c_int64]
+        L.or_rates_free.argtypes = [ct.c_void_p]
+        self.W = W
+        r = OrRequest()
+        for i in range(3):
+            r.mesh[i] = int(req.mesh[i])
+        r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+        r.delta_kind, r.sigma = int(req.delta_kind), req.sigma
+        self.r = r
+        self.N = int(np.prod(req.mesh))
+        self.nthreads = nthreads
+        self.ctx = L.or_rates_setup(ct.byref(W.s), ct.byref(r), nthreads)
+
+    def run(self, state_begin, nstates, literal=True):
+        N, nw = self.N, self.W.nw
+        rates = np.zeros((N, nw), order="F")
+        idx = np.zeros(N, dtype=np.int64)
+        info = np.zeros(8, dtype=np.int64)
+        lib().or_rates_run(self.ctx, state_begin, nstates, self.nthreads, 1 if literal else 0, _p(rates),
+                           _p(idx, c_i64p), _p(info, c_i64p), None, None, None, 0)
+        nwv = int(info[0])
+        return dict(nwv=nwv, nstates_inwindow=int(info[1]), nstates=int(info[2]), vertices=int(info[3]),
+                    status=int(info[5]), us_setup=int(info[6]), us_loop=int(info[7]),
+                    rates=np.asfortranarray(rates[:nwv]), indexlist=idx[:nwv].copy())
+
+    def close(self):
+        if self.ctx:
+            lib().or_rates_free(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
