@@ -16,12 +16,15 @@
 #include "ephg_kernels.cuh"
 #include "ephg_tc.cuh"
 #include "ephg_ws.cuh"
+#include "ephg_handle.cuh"
 
 using namespace ephg;
 
+#define fail ephg::api_fail
+
 static thread_local std::string g_err;
 
-static int fail(int code, const char *fmt, ...) {
+int ephg::api_fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -93,33 +96,6 @@ std::vector<int> ws_wrap(const double lvec[9], const double vl[3], double eps) {
 
 }  // namespace
 
-struct ephg_handle {
-  int device = 0;
-  cudaStream_t st = nullptr;
-  int nw = 0, nb = 0, nwsk = 0, nwsq = 0, nwsg = 0, nat = 0;
-  int cq[3] = {0, 0, 0};
-  double lattvecs[9];
-  std::vector<double> masses_h;
-  int64_t Nn = 0;   // nw*nw*nb*nwsg, the stage-A row length
-  // resident device data
-  int *Rk = nullptr, *Rq = nullptr, *Rg = nullptr;         // (n,3) int
-  double *degk = nullptr, *degq = nullptr, *degg = nullptr;
-  double2 *Hext = nullptr;   // [Re][4*nw*nw]: H, i rx H, i ry H, i rz H
-  double2 *graw = nullptr;   // epmatwp order (i,j,Re,s,Rp)
-  double2 *G64 = nullptr;    // stage-A matrix [Re][Nn]
-  double *masses = nullptr;
-  // phonon wrap terms
-  int *pair_off = nullptr, *ent_iuc = nullptr, *ent_woff = nullptr, *wrapR = nullptr;
-  double *ent_den = nullptr, *rcartq = nullptr;
-  double2 *D = nullptr;
-  PhTerms terms;
-  int *kposk = nullptr, *kposq = nullptr;   // split-form contraction order (far cells first)
-  int *err = nullptr;        // device error word
-  Workspace ws;
-  tc::SplitOperands split;   // split-TF32 operand planes (lazy)
-  LaunchTimer timer_a, timer_b;   // device time of the contraction launches of the last request
-  int64_t launches = 0;
-};
 
 static int read_err(ephg_handle *h, int *word) {
   CK(cudaMemcpyAsync(word, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -128,7 +104,7 @@ static int read_err(ephg_handle *h, int *word) {
   return EPHG_OK;
 }
 
-static int check_err(ephg_handle *h) {
+int ephg::api_check_err(ephg_handle *h) {
   int w = 0;
   int rc = read_err(h, &w);
   if (rc) return rc;
@@ -380,7 +356,7 @@ int ephg_el_wann(ephg_handle *h, int64_t nk, const double *kvecs, double *energi
   CK(cudaMemcpyAsync(energies, ens, (size_t)nk * nw * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   if (evecs) CK(cudaMemcpyAsync(evecs, ev, (size_t)nk * nn * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
   if (with_vel) CK(cudaMemcpyAsync(velocities, vel, (size_t)nk * nw * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 // ------------------------------------------------------------- ph_wann
@@ -415,7 +391,7 @@ int ephg_ph_wann(ephg_handle *h, int64_t nq, const double *qvecs, double *energi
   CK(cudaMemcpyAsync(energies, ens, (size_t)nq * nb * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   if (evecs) CK(cudaMemcpyAsync(evecs, ev, (size_t)nq * nn * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
   if (with_vel) CK(cudaMemcpyAsync(velocities, vel, (size_t)nq * nb * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 // ---------------------------------------------------------------- gkRp
@@ -444,7 +420,7 @@ int ephg_gkRp(ephg_handle *h, int64_t nk, const double *kvecs, double *gmixed) {
                        cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
   }
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 // ---------------------------------------------------------------- gReq
@@ -476,7 +452,7 @@ int ephg_gReq(ephg_handle *h, int64_t nq, const double *qvecs, double *gmixed) {
                        cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
   }
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 // ------------------------------------------------------------------ g2
@@ -517,7 +493,7 @@ int ephg_g2(ephg_handle *h, int64_t wannspace, int64_t nv, const double *kvecs,
   h->launches += 1;
   CKL();
   CK(cudaMemcpyAsync(g2_out, out, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 // ------------------------------------------------------------ kq index
@@ -539,7 +515,7 @@ int ephg_kq_index(ephg_handle *h, const int64_t mesh[3], int64_t nk, const int64
   h->launches += 1;
   CKL();
   CK(cudaMemcpyAsync(q_idx, q, (size_t)nk * nkp * sizeof(int64_t), cudaMemcpyDeviceToHost, h->st));
-  return check_err(h);
+  return ephg::api_check_err(h);
 }
 
 }  // extern "C"
@@ -677,7 +653,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   int nwv = 0;
   CK(cudaMemcpyAsync(&nwv, nwv_d, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if ((rc = check_err(h))) return rc;
+  if ((rc = ephg::api_check_err(h))) return rc;
   if (nwv == 0) return fail(EPHG_ERR_EMPTY_WINDOW, "No states found within Fermi window.");
   // ---- phonons on the q mesh (phonon.f90:208-214) ----
   launch_dbuild(N, iota, mesh, L, roots, nullptr, h->terms, 0, Dq, nullptr, st);
@@ -702,7 +678,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   std::vector<int> widx_h(nwv), code_h;
   CK(cudaMemcpyAsync(widx_h.data(), widx, nwv * sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if ((rc = check_err(h))) return rc;
+  if ((rc = ephg::api_check_err(h))) return rc;
   code_h.resize(nst);
   CK(cudaMemcpyAsync(code_h.data(), st_code, nst * sizeof(int), cudaMemcpyDeviceToHost, st));
   // simplices for triangle / tetrahedron deltas
@@ -836,7 +812,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     if (xplus) CK(cudaMemcpy(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
     if (xminus) CK(cudaMemcpy(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
   }
-  if ((rc = check_err(h))) return rc;
+  if ((rc = ephg::api_check_err(h))) return rc;
   if (stats) {
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
     cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);

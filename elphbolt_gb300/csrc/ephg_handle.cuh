@@ -1,0 +1,45 @@
+// ephg_handle.cuh - the library handle (internal; the C ABI sees an opaque pointer).
+#pragma once
+#include <vector>
+
+#include "../../include/ephg.h"
+#include "ephg_kernels.cuh"
+#include "ephg_tc.cuh"
+#include "ephg_ws.cuh"
+
+// Resident Wannier data of one crystal on one device, its stream, workspace
+// and error word.
+struct ephg_handle {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int nw = 0, nb = 0, nwsk = 0, nwsq = 0, nwsg = 0, nat = 0;
+  int cq[3] = {0, 0, 0};
+  double lattvecs[9];
+  std::vector<double> masses_h;
+  int64_t Nn = 0;   // nw*nw*nb*nwsg, the stage-A row length
+  // resident device data
+  int *Rk = nullptr, *Rq = nullptr, *Rg = nullptr;         // (n,3) int
+  double *degk = nullptr, *degq = nullptr, *degg = nullptr;
+  double2 *Hext = nullptr;   // [Re][4*nw*nw]: H, i rx H, i ry H, i rz H
+  double2 *graw = nullptr;   // epmatwp order (i,j,Re,s,Rp)
+  double2 *G64 = nullptr;    // stage-A matrix [Re][Nn]
+  double *masses = nullptr;
+  // phonon wrap terms
+  int *pair_off = nullptr, *ent_iuc = nullptr, *ent_woff = nullptr, *wrapR = nullptr;
+  double *ent_den = nullptr, *rcartq = nullptr;
+  double2 *D = nullptr;
+  ephg::PhTerms terms;
+  int *kposk = nullptr, *kposq = nullptr;   // split-form contraction order (far cells first)
+  int *err = nullptr;        // device error word
+  ephg::Workspace ws;
+  ephg::tc::SplitOperands split;   // split-TF32 operand planes (lazy)
+  ephg::LaunchTimer timer_a, timer_b;   // device time of the contraction launches of the last request
+  int64_t launches = 0;
+};
+
+namespace ephg {
+// record a failure message for ephg_last_error() and return code
+int api_fail(int code, const char *fmt, ...);
+// read, clear and translate the handle's device error word
+int api_check_err(ephg_handle *h);
+}  // namespace ephg
