@@ -31,7 +31,8 @@ c_dp = ct.POINTER(ct.c_double)
 
 # every symbol include/ephg.h declares
 EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count", "ephg_el_wann",
-           "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates"]
+           "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates",
+           "ephg_el_wann_noalloc"]
 
 
 class EphgError(RuntimeError):
@@ -95,6 +96,7 @@ def load(path: str = LIB_PATH):
     L.ephg_kq_index.argtypes = [vp, c_i64p, ct.c_int64, c_i64p, ct.c_int64, c_i64p, c_i64p]
     L.ephg_el_rates.argtypes = [vp, ct.POINTER(RateRequest), c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, c_dp, ct.c_int64]
+    L.ephg_el_wann_noalloc.argtypes = [vp, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ct.c_int
     L.ephg_last_error.restype = ct.c_char_p

@@ -153,6 +153,26 @@ int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus,
                   double *xminus, int64_t cap);
 
+/* el_wann without any device allocation.  No counterpart in the reference:
+ * it serves callers that cannot allocate device memory where they need the
+ * electrons -- a host code handing over buffers it already owns on the device
+ * (OpenACC or CUDA Fortran arrays, or system memory the GPU reaches over the
+ * Grace C2C link), a process whose device memory is fixed by another
+ * framework's pool, or a time-critical loop that must not pay cudaMalloc's
+ * implicit synchronisation.  kvecs (nk,3) is read and energies (nk,nw) and
+ * evecs (nk,nw,nw, nullable) written through the caller's device-accessible
+ * pointers, in the layouts of ephg_el_wann (no velocities, no scissor).  The
+ * scratch is one fixed array of EPHG_NOALLOC_SCRATCH_BYTES inside the library
+ * (every GPU that loads the library holds it until exit); requests that need
+ * more are refused with EPHG_ERR_ARG and the largest nk that fits in the
+ * message.  The first call on a device resolves the array's address (set-up,
+ * once per device), so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  The handle's device must be
+ * current; the call returns after the handle's stream has finished. */
+#define EPHG_NOALLOC_SCRATCH_BYTES (16ull << 20)
+int ephg_el_wann_noalloc(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
+                         double *evecs);
+
 #ifdef __cplusplus
 }
 #endif
