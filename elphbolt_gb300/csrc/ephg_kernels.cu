@@ -341,22 +341,33 @@ void launch_el_post(int nk, int nw, const double *w, const double2 *V, const dou
 
 // ============================================================= phonons
 // D(q) assembly with Wigner-Seitz wrapping (wannier.f90:631-665), mass
-// normalisation (:716-729).  One block per q, one thread per matrix element.
-__global__ void k_dbuild(int nq, const int *qp, int m1, int m2, int m3, int L,
-                         const double2 *roots, const double *qv, PhTerms t, int with_vel,
-                         double2 *Dq, double2 *dDq) {
+// normalisation (:716-729).  One block per q.  The wrapped phase sum of each
+// (atom pair, WS cell), sum_w e^{2 pi i q.(R + w N_c)} / (deg * nwrap), is
+// formed once into shared memory (chunks of DB_CHUNK cells) and then each
+// thread contracts it with D(R) for its matrix elements.
+constexpr int DB_CHUNK = 64;
+
+__global__ void __launch_bounds__(128) k_dbuild(int nq, const int *qp, int m1, int m2, int m3, int L,
+                                                const double2 *roots, const double *qv, PhTerms t, int with_vel,
+                                                double2 *Dq, double2 *dDq) {
+  extern __shared__ double2 dsm[];   // [npair][DB_CHUNK] phase sums
   const int q = blockIdx.x;
-  const int nb = t.nb;
+  const int nb = t.nb, nwsq = t.nwsq, npair = t.npair;
   const int mesh[3] = {m1, m2, m3};
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int a = e % nb, b = e / nb;
-    int iat = a / 3, jat = b / 3;
-    int pair = iat + t.nat * jat;
-    double2 acc = make_double2(0.0, 0.0);
-    double2 dacc[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-    for (int en = t.pair_off[pair]; en < t.pair_off[pair + 1]; ++en) {
-      int iuc = t.ent_iuc[en];
-      double den = t.ent_den[en];
+  const int ne = nb * nb;
+  // each thread owns up to DB_U matrix elements (nb <= 32 gives <= 1024 elements)
+  constexpr int DB_U = 8;
+  double2 acc[DB_U], dacc[DB_U][3];
+  for (int u = 0; u < DB_U; ++u) {
+    acc[u] = make_double2(0.0, 0.0);
+    for (int p = 0; p < 3; ++p) dacc[u][p] = make_double2(0.0, 0.0);
+  }
+  for (int c0 = 0; c0 < nwsq; c0 += DB_CHUNK) {
+    const int nc = min(DB_CHUNK, nwsq - c0);
+    __syncthreads();
+    for (int w = threadIdx.x; w < npair * nc; w += blockDim.x) {
+      const int pair = w / nc, iuc = c0 + w % nc;
+      const int en = t.pair_off[pair] + iuc;     // entries are (pair, cell) in cell order
       double2 cs = make_double2(0.0, 0.0);
       for (int wv = t.ent_woff[en]; wv < t.ent_woff[en + 1]; ++wv) {
         const int *R = t.wrapR + 3 * wv;
@@ -369,22 +380,40 @@ __global__ void k_dbuild(int nq, const int *qp, int m1, int m2, int m3, int L,
           dot += qv[q + 2 * nq] * (double)R[2];
           sincos(TWOPI * dot, &ph.y, &ph.x);
         }
-        cs.x += ph.x / den;
-        cs.y += ph.y / den;
+        cs.x += ph.x;
+        cs.y += ph.y;
       }
-      double2 d = t.D[iuc + (int64_t)t.nwsq * (a + (int64_t)nb * b)];
-      double2 term = cmul(cs, d);
-      acc = cadd(acc, term);
-      if (with_vel)
-        for (int p = 0; p < 3; ++p) {
-          double rc = t.rcart[iuc + (int64_t)t.nwsq * p];
-          dacc[p] = cadd(dacc[p], make_double2(-rc * term.y, rc * term.x));
-        }
+      const double den = t.ent_den[en];
+      dsm[pair * DB_CHUNK + (iuc - c0)] = make_double2(cs.x / den, cs.y / den);
     }
-    double massnorm = 1.0 / sqrt(t.masses[iat] * t.masses[jat]) * Ryd2amu;
-    Dq[(size_t)q * nb * nb + e] = cscale(acc, massnorm);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < DB_U; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      if (e >= ne) break;
+      const int a = e % nb, b = e / nb;
+      const int pair = (a / 3) + t.nat * (b / 3);
+      for (int k = 0; k < nc; ++k) {
+        const int iuc = c0 + k;
+        const double2 term = cmul(dsm[pair * DB_CHUNK + k], t.D[iuc + (int64_t)nwsq * (a + (int64_t)nb * b)]);
+        acc[u] = cadd(acc[u], term);
+        if (with_vel)
+          for (int p = 0; p < 3; ++p) {
+            const double rc = t.rcart[iuc + (int64_t)nwsq * p];
+            dacc[u][p] = cadd(dacc[u][p], make_double2(-rc * term.y, rc * term.x));
+          }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < DB_U; ++u) {
+    const int e = threadIdx.x + u * blockDim.x;
+    if (e >= ne) break;
+    const int a = e % nb, b = e / nb;
+    const double massnorm = 1.0 / sqrt(t.masses[a / 3] * t.masses[b / 3]) * Ryd2amu;
+    Dq[(size_t)q * ne + e] = cscale(acc[u], massnorm);
     if (with_vel)
-      for (int p = 0; p < 3; ++p) dDq[((size_t)q * 3 + p) * nb * nb + e] = cscale(dacc[p], massnorm);
+      for (int p = 0; p < 3; ++p) dDq[((size_t)q * 3 + p) * ne + e] = cscale(dacc[u][p], massnorm);
   }
 }
 
@@ -392,9 +421,14 @@ void launch_dbuild(int nq, const int *qp, const int mesh[3], int L, const double
                    const double *qv, const PhTerms &t, int with_vel, double2 *Dq, double2 *dDq,
                    cudaStream_t st) {
   if (nq <= 0) return;
-  int thr = t.nb * t.nb < 128 ? 64 : 128;
-  k_dbuild<<<nq, thr, 0, st>>>(nq, qp, mesh ? mesh[0] : 1, mesh ? mesh[1] : 1,
-                               mesh ? mesh[2] : 1, L, roots, qv, t, with_vel, Dq, dDq);
+  const size_t smem = (size_t)t.npair * DB_CHUNK * sizeof(double2);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_dbuild, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    attr = true;
+  }
+  k_dbuild<<<nq, 128, smem, st>>>(nq, qp, mesh ? mesh[0] : 1, mesh ? mesh[1] : 1, mesh ? mesh[2] : 1, L, roots, qv,
+                                  t, with_vel, Dq, dDq);
 }
 
 // ph_wann post-processing (wannier.f90:740-780)

@@ -483,6 +483,75 @@ __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int 
   }
 }
 
+// Stage-A rotation, one block per window k: the block loads g(k,Rp) for KT
+// contraction positions at a time (coalesced rows of nw*nw*nb values), rotates
+// over the initial band for every in-window state of k, applies the k-half of
+// the Rp phase and writes KT consecutive K positions of each operand row, so
+// that both the reads and the split-plane writes are whole sectors.
+// kinv[kp] = Rp cell at contraction position kp (-1 for padding).
+constexpr int ROT_KT = 8;
+
+__global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state, int nw, int nb, const int *st_code,
+                                                  const int *widx, const double2 *U, const float *gr, const float *gi,
+                                                  int64_t ldg, int m1, int m2, int m3, int L, const double2 *roots,
+                                                  const int *Rq, const double *degq, const int *kinv, int Kp2,
+                                                  float *Bp, int64_t Np2) {
+  extern __shared__ unsigned char rsm[];
+  const int i = i0 + blockIdx.x;
+  const int j0 = first_state[i], j1 = first_state[i + 1];
+  const int nsk = j1 - j0;
+  if (nsk <= 0) return;
+  const int p = widx[i];
+  const int per = nw * nw * nb, ncol = nw * nb;
+  float2 *sg = (float2 *)rsm;                                   // [ROT_KT][per]
+  float2 *sU = (float2 *)(rsm + ((sizeof(float2) * ROT_KT * per + 15) & ~(size_t)15));  // [nsk][nw]
+  float2 *sph = sU + nsk * nw;                                  // [ROT_KT]
+  for (int t = threadIdx.x; t < nsk * nw; t += blockDim.x) {
+    int js = t / nw, mp = t % nw;
+    int m = st_code[j0 + js] % nw;
+    double2 u = U[((size_t)p * nw + m) * nw + mp];
+    sU[t] = make_float2((float)u.x, (float)u.y);
+  }
+  const int64_t grow = (int64_t)(i - i0) * ldg;
+  const int64_t plane = Np2 * Kp2;
+  for (int kp0 = 0; kp0 < Kp2; kp0 += ROT_KT) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ROT_KT * per; t += blockDim.x) {
+      int kk = t / per, e = t % per;
+      int rp = kinv[kp0 + kk];
+      sg[t] = rp >= 0 ? make_float2(gr[grow + (int64_t)rp * per + e], gi[grow + (int64_t)rp * per + e])
+                      : make_float2(0.f, 0.f);
+    }
+    if (threadIdx.x < ROT_KT) {
+      int rp = kinv[kp0 + threadIdx.x];
+      float2 ph = make_float2(0.f, 0.f);
+      if (rp >= 0) {
+        double2 r = roots[phase_idx(p, m1, m2, m3, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
+        ph = make_float2((float)(r.x / degq[rp]), (float)(-r.y / degq[rp]));
+      }
+      sph[threadIdx.x] = ph;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < nsk * ncol * ROT_KT; o += blockDim.x) {
+      const int kk = o % ROT_KT, c = (o / ROT_KT) % ncol, js = o / (ROT_KT * ncol);
+      const int np = c % nw, s = c / nw;
+      float2 acc = make_float2(0.f, 0.f);
+      const float2 *g = sg + kk * per + np + nw * nw * s;
+      const float2 *u = sU + js * nw;
+      for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
+      const float2 ph = sph[kk];
+      const int64_t col = (int64_t)(j0 + js) * ncol + c;
+      put4(Bp, plane, col * Kp2 + kp0 + kk,
+           make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
+    }
+  }
+}
+
+__global__ void k_kinv(int n, const int *kpos, int *kinv) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) kinv[kpos[r]] = r;
+}
+
 // -------------------------------------------- split-form rate epilogue
 struct QTab {
   const float *cx;     // [q][s]: const_tp * g2unitfactor / (2 omega) if omega >= 0.5 meV else 0
@@ -587,6 +656,318 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
   }
 }
 
+// Split-form epilogue, one block per 128 consecutive k' rows and a set of
+// states: for each state the block stages the rows' 48 complex Rp sums in
+// shared memory with coalesced loads, then each thread forms its (k', state)
+// pair exactly as k_epilogue_split does.  Block partials are reduced in a fixed
+// order (deterministic).
+constexpr int EPI_ROWS = 128;
+
+// NW, NB: band and mode counts fixed at compile time (the per-thread arrays then
+// live in registers), or 0 to read them from rp.
+template <int NW, int NB>
+__global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, int jend, int spb, const float *Cr,
+                                                              const float *Ci, int64_t ldc, RateParams rp,
+                                                              EpiData d, QTab qt, double *partial, int nblk) {
+  extern __shared__ float esm[];
+  const int nw = NW ? NW : rp.nw, nb = NB ? NB : rp.nb, ncol = nw * nb, ld = ncol + 1;
+  constexpr int AW = NW ? NW : 32, AB = NB ? NB : 32;
+  float *sr = esm, *si = esm + EPI_ROWS * ld;
+  __shared__ double wsum[EPI_ROWS / 32];
+  const int row = threadIdx.x;
+  const int ip0 = blockIdx.x * EPI_ROWS, ip = ip0 + row;
+  const bool live = ip < nwv;
+  // row-level data, loaded once for all states of the block
+  int pp = 0, b1 = 0, b2 = 0, b3 = 0;
+  if (live) {
+    pp = d.widx[ip];
+    b1 = pp % rp.mesh[0];
+    b2 = (pp / rp.mesh[0]) % rp.mesh[1];
+    b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+  }
+  const double inv_sig = 1.0 / rp.sigma;
+  const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
+  const int jb0 = j0 + blockIdx.y * spb;
+  const int jb1 = min(jend, jb0 + spb);
+  for (int j = jb0; j < jb1; ++j) {
+    __syncthreads();
+    const int64_t cbase = (int64_t)(j - j0) * ncol;
+    for (int t = threadIdx.x; t < EPI_ROWS * ncol; t += EPI_ROWS) {
+      const int r = t / ncol, c = t % ncol;
+      const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + c;    // rows < Mp exist in the chunk
+      sr[r * ld + c] = Cr[o];
+      si[r * ld + c] = Ci[o];
+    }
+    __syncthreads();
+    double v = 0.0;
+    if (live) {
+      const int code = d.st_code[j];
+      const int i = code / nw, m = code % nw;
+      const int p = d.widx[i];
+      const double E = d.ens[(size_t)p * nw + m];
+      const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+      const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
+      const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                          rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+      const float *gr = sr + row * ld, *gi = si + row * ld;
+      float acc = 0.0f;
+      int rank_n = 0;
+      for (int n = 0; n < nw; ++n) {
+        const double eps = d.ens[(size_t)pp * nw + n];
+        if (fabs(eps - rp.enref) > rp.fsthick) continue;
+        const float2 *Ukp = d.Uf + ((size_t)pp * nw + n) * nw;
+        float2 uk[AW];
+#pragma unroll
+        for (int np = 0; np < AW; ++np)
+          if (np < nw) uk[np] = Ukp[np];
+        float2 h[AB];
+#pragma unroll
+        for (int s = 0; s < AB; ++s) {
+          if (s >= nb) break;
+          float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int np = 0; np < AW; ++np)
+            if (np < nw) cfmaf_cj(a, uk[np], make_float2(gr[np + nw * s], gi[np + nw * s]));
+          h[s] = a;
+        }
+        const float dn = (float)((E - eps) * inv_sig);
+#pragma unroll
+        for (int s = 0; s < AB; ++s) {
+          if (s >= nb) break;
+          const int qs = q * nb + s;
+          const float2 *u = d.uf + (size_t)qs * nb;
+          float2 g = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int sp = 0; sp < AB; ++sp)
+            if (sp < nb) cfmaf(g, u[sp], h[sp]);
+          const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
+          const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
+          const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
+          const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
+          const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+          const float xp = g2c * (qt.bose[qs] + fp) * dp;
+          const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+          acc += xp + xm;
+          if (d.g2) {
+            int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
+            if (off < d.cap) {
+              const double om = d.om[qs];
+              d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+              d.xp[off] = xp;
+              d.xm[off] = xm;
+            }
+          }
+        }
+        rank_n++;
+      }
+      v = (double)acc;
+    }
+    // fixed-order block reduction: warp shuffle tree, then the 4 warp sums in order
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sacc = 0.0;
+      for (int w = 0; w < EPI_ROWS / 32; ++w) sacc += wsum[w];
+      partial[(size_t)j * nblk + blockIdx.x] = sacc;
+    }
+  }
+}
+
+// Packed per-(q, s) record of the nb = 6 fast path: the mass-scaled phonon
+// eigenvector row and the four scalars of the epilogue in one 64-byte line.
+struct __align__(16) QRec6 {
+  float2 u[6];
+  float cx, bose, w, v;
+};
+
+__global__ void k_qpack6(int n, const float2 *uf, const float *cx, const float *bs, const float *w, const float *v,
+                         QRec6 *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  QRec6 r;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) r.u[c] = uf[(size_t)i * 6 + c];
+  r.cx = cx[i];
+  r.bose = bs[i];
+  r.w = w[i];
+  r.v = v[i];
+  out[i] = r;
+}
+
+// Epilogue for nw = 8, nb = 6 (the bench crystal): as k_epilogue_split2, with
+// the k'-row data (window bands, their energies) loaded once per block and the
+// per-(q, s) data read as one 64-byte record.
+__global__ void __launch_bounds__(EPI_ROWS) k_epilogue_86(int nwv, int j0, int jend, int spb, const float *Cr,
+                                                          const float *Ci, int64_t ldc, RateParams rp, EpiData d,
+                                                          const QRec6 *qrec, double *partial, int nblk) {
+  // LD = 52: 16-byte aligned rows whose 128-bit shared loads are conflict-free
+  constexpr int NW = 8, NB = 6, NC = NW * NB, LD = 52, NC4 = NC / 4, SPB_MAX = 16;
+  extern __shared__ float esm86[];
+  float *sr = esm86, *si = esm86 + EPI_ROWS * LD;
+  __shared__ double wsum[EPI_ROWS / 32];
+  __shared__ double sE[SPB_MAX];
+  __shared__ float sA[SPB_MAX];
+  __shared__ int sP[SPB_MAX];
+  const int row = threadIdx.x;
+  const int ip0 = blockIdx.x * EPI_ROWS, ip = ip0 + row;
+  const bool live = ip < nwv;
+  const int jb0 = j0 + blockIdx.y * spb;
+  const int jb1 = min(jend, jb0 + spb);
+  // per-state data of the block's states, one round trip for all of them
+  if (threadIdx.x < jb1 - jb0) {
+    const int code = d.st_code[jb0 + threadIdx.x];
+    const int p = d.widx[code / NW];
+    const double E = d.ens[(size_t)p * NW + code % NW];
+    sE[threadIdx.x] = E;
+    sA[threadIdx.x] = (float)((E - rp.chempot) / (kB * rp.T));
+    sP[threadIdx.x] = p;
+  }
+  // k'-row data: window bands, their energies, the first two bands' U_k' rows
+  int b1 = 0, b2 = 0, b3 = 0, pp = 0;
+  unsigned wmask = 0;
+  double epsn[NW];
+  float2 ukr[2][NW];
+  int nfirst[2] = {-1, -1};
+  if (live) {
+    pp = d.widx[ip];
+    b1 = pp % rp.mesh[0];
+    b2 = (pp / rp.mesh[0]) % rp.mesh[1];
+    b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+    int nk = 0;
+#pragma unroll
+    for (int n = 0; n < NW; ++n) {
+      epsn[n] = d.ens[(size_t)pp * NW + n];
+      if (fabs(epsn[n] - rp.enref) <= rp.fsthick) {
+        wmask |= 1u << n;
+        if (nk < 2) nfirst[nk++] = n;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+      if (nfirst[t] >= 0) {
+        const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + nfirst[t]) * NW);
+#pragma unroll
+        for (int h4 = 0; h4 < NW / 2; ++h4) {
+          float4 t4 = Uk4[h4];
+          ukr[t][2 * h4] = make_float2(t4.x, t4.y);
+          ukr[t][2 * h4 + 1] = make_float2(t4.z, t4.w);
+        }
+      }
+  }
+  const int cum0 = live ? d.cum[ip] : 0;
+  const double inv_sig = 1.0 / rp.sigma;
+  const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
+  for (int j = jb0; j < jb1; ++j) {
+    __syncthreads();
+    const int64_t cbase = (int64_t)(j - j0) * NC;
+    {
+      float4 vr[NC4], vi[NC4];
+#pragma unroll
+      for (int k = 0; k < NC4; ++k) {    // all 24 vector loads in flight together
+        const int f = threadIdx.x + EPI_ROWS * k;
+        const int r = f / NC4, c4 = f - r * NC4;
+        const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + 4 * c4;
+        vr[k] = *(const float4 *)(Cr + o);
+        vi[k] = *(const float4 *)(Ci + o);
+      }
+#pragma unroll
+      for (int k = 0; k < NC4; ++k) {
+        const int f = threadIdx.x + EPI_ROWS * k;
+        const int r = f / NC4, c4 = f - r * NC4;
+        *(float4 *)(sr + r * LD + 4 * c4) = vr[k];
+        *(float4 *)(si + r * LD + 4 * c4) = vi[k];
+      }
+    }
+    __syncthreads();
+    double vsum = 0.0;
+    if (live && wmask) {
+      const int js = j - jb0;
+      const double E = sE[js];
+      const float a_occ = sA[js];
+      const int p = sP[js];
+      const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
+      const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                          rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+      const float *gr = sr + row * LD, *gi = si + row * LD;
+      const QRec6 *qr = qrec + (size_t)q * NB;
+      float acc = 0.0f;
+      int rank_n = 0;
+#pragma unroll
+      for (int n = 0; n < NW; ++n) {
+        if (!((wmask >> n) & 1u)) continue;
+        float2 uk[NW];
+        if (n == nfirst[0] || n == nfirst[1]) {
+          const int t = (n == nfirst[0]) ? 0 : 1;
+#pragma unroll
+          for (int c = 0; c < NW; ++c) uk[c] = t == 0 ? ukr[0][c] : ukr[1][c];
+        } else {
+          const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + n) * NW);
+#pragma unroll
+          for (int h4 = 0; h4 < NW / 2; ++h4) {
+            float4 t4 = Uk4[h4];
+            uk[2 * h4] = make_float2(t4.x, t4.y);
+            uk[2 * h4 + 1] = make_float2(t4.z, t4.w);
+          }
+        }
+        float2 h[NB];
+#pragma unroll
+        for (int s = 0; s < NB; ++s) {
+          const float4 r0 = *(const float4 *)(gr + NW * s), r1 = *(const float4 *)(gr + NW * s + 4);
+          const float4 i0 = *(const float4 *)(gi + NW * s), i1 = *(const float4 *)(gi + NW * s + 4);
+          const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+          const float xi[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+          float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int np = 0; np < NW; ++np) cfmaf_cj(a, uk[np], make_float2(xr[np], xi[np]));
+          h[s] = a;
+        }
+        const float dn = (float)((E - epsn[n]) * inv_sig);
+#pragma unroll
+        for (int s = 0; s < NB; ++s) {
+          const float4 *r4 = (const float4 *)(qr + s);
+          const float4 u01 = r4[0], u23 = r4[1], u45 = r4[2], sc = r4[3];
+          float2 g = make_float2(0.f, 0.f);
+          cfmaf(g, make_float2(u01.x, u01.y), h[0]);
+          cfmaf(g, make_float2(u01.z, u01.w), h[1]);
+          cfmaf(g, make_float2(u23.x, u23.y), h[2]);
+          cfmaf(g, make_float2(u23.z, u23.w), h[3]);
+          cfmaf(g, make_float2(u45.x, u45.y), h[4]);
+          cfmaf(g, make_float2(u45.z, u45.w), h[5]);
+          // sc = (cx, bose, w, v)
+          const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
+          const float tp = dn + sc.z, tm = dn - sc.z;
+          const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
+          const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
+          const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+          const float xp = g2c * (sc.y + fp) * dp;
+          const float xm = g2c * (1.0f + sc.y - fm) * dm;
+          acc += xp + xm;
+          if (d.g2) {
+            int64_t off = (int64_t)j * d.per_state + ((int64_t)cum0 + rank_n) * NB + s;
+            if (off < d.cap) {
+              const double om = d.om[(size_t)q * NB + s];
+              d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+              d.xp[off] = xp;
+              d.xm[off] = xm;
+            }
+          }
+        }
+        rank_n++;
+      }
+      vsum = (double)acc;
+    }
+    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_down_sync(0xffffffffu, vsum, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = vsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sacc = 0.0;
+      for (int w = 0; w < EPI_ROWS / 32; ++w) sacc += wsum[w];
+      partial[(size_t)j * nblk + blockIdx.x] = sacc;
+    }
+  }
+}
+
 // ------------------------------------------------------------ orchestration
 void free_split(SplitOperands &s) {
   if (s.G) cudaFree(s.G);
@@ -627,7 +1008,22 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
       (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)4 * Np2 * KpB, &B2)))
     return tfail(6, ws.msg.c_str());
-  TCK(cudaMemsetAsync(B2, 0, (size_t)4 * Np2 * KpB * sizeof(float), st));
+  // the rotation writes every K position of every state row; zero the padding rows only
+  {
+    const int64_t used = (int64_t)nst * ncol;
+    for (int pl = 0; pl < 4; ++pl)
+      if (Np2 > used)
+        TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
+  }
+  // first state of each window k, and the Rp cell at each contraction position
+  int *fs_d, *kinvB;
+  if ((rc = wsget(ws, "tc_fs", (size_t)nwv + 1, &fs_d)) || (rc = wsget(ws, "tc_kinv", (size_t)KpB, &kinvB)))
+    return tfail(6, ws.msg.c_str());
+  TCK(cudaMemcpyAsync(fs_d, first_state.data(), (size_t)(nwv + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  TCK(cudaMemsetAsync(kinvB, 0xFF, (size_t)KpB * sizeof(int), st));
+  k_kinv<<<(nwsq + 255) / 256, 256, 0, st>>>(nwsq, kposB, kinvB);
+  TCK(cudaGetLastError());
+  *launches += 1;
   for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
     const int n = (int)std::min<int64_t>(kc, nwv - i0);
     const int Mp = (int)rup(n, BM);
@@ -639,13 +1035,29 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     tA->begin(st);
     if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st))) return rc;
     tA->end(st);
-    for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
-      int je = std::min(j1, j0 + 32768);
-      dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
-      k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, U, CAr, CAi, NpA, mesh[0],
-                                           mesh[1], mesh[2], L, roots, Rq, degq, kposB, B2, Np2, KpB, 0);
-      TCK(cudaGetLastError());
-      (*launches)++;
+    {
+      const int per = nw * nw * nb;
+      const size_t sm = ((sizeof(float2) * ROT_KT * per + 15) & ~(size_t)15) + sizeof(float2) * (nw * nw + ROT_KT);
+      if (sm <= 160 * 1024) {
+        static bool rattr = false;
+        if (!rattr) {
+          TCK(cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+          rattr = true;
+        }
+        k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, widx, U, CAr, CAi, NpA, mesh[0], mesh[1],
+                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
+        TCK(cudaGetLastError());
+        (*launches)++;
+      } else {   // large nw*nw*nb: one thread per output element
+        for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
+          int je = std::min(j1, j0 + 32768);
+          dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
+          k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, U, CAr, CAi, NpA,
+                                               mesh[0], mesh[1], mesh[2], L, roots, Rq, degq, kposB, B2, Np2, KpB, 0);
+          TCK(cudaGetLastError());
+          (*launches)++;
+        }
+      }
     }
     *launches += 3;
   }
@@ -685,15 +1097,41 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   EpiData ed = ed_in;
   ed.Uf = Uf;
   QTab qt{cx, bs, w, v};
+  QRec6 *qrec = nullptr;
+  if (nw == 8 && nb == 6) {
+    if ((rc = wsget(ws, "tc_qrec", (size_t)N * nb, &qrec))) return tfail(6, ws.msg.c_str());
+    k_qpack6<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.uf, cx, bs, w, v, qrec);
+    TCK(cudaGetLastError());
+    (*launches)++;
+  }
   for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
     if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st))) return rc;
     tB->end(st);
-    dim3 grid(nblk, ns);
-    if (rp.delta_kind == 0) {
+    const size_t esm = (size_t)2 * EPI_ROWS * ((nw == 8 && nb == 6) ? 52 : (ncol + 1)) * sizeof(float);
+    if (rp.delta_kind == 0 && esm > 200 * 1024) {
+      dim3 grid(nblk, ns);
       k_epilogue_split<<<grid, 128, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      TCK(cudaGetLastError());
+    } else if (rp.delta_kind == 0) {
+      const int spb = 16;
+      dim3 grid(nblk, (ns + spb - 1) / spb);
+      const size_t sm = esm;
+      static bool eattr = false;
+      if (!eattr) {
+        TCK(cudaFuncSetAttribute(k_epilogue_split2<8, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        TCK(cudaFuncSetAttribute(k_epilogue_split2<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        TCK(cudaFuncSetAttribute(k_epilogue_86, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        eattr = true;
+      }
+      if (nw == 8 && nb == 6)
+        k_epilogue_86<<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed, qrec,
+                                                 partial, nblk);
+      else
+        k_epilogue_split2<0, 0><<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed,
+                                                           qt, partial, nblk);
       TCK(cudaGetLastError());
     } else {
       launch_epilogue_fp32(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed_in, partial, nblk, st);
