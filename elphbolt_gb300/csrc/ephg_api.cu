@@ -753,9 +753,10 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     ed.xm = xmd;
     ed.cap = vcap;
   }
-  const int nblk = (nwv + 127) / 128;
+  int nblk = (nwv + 127) / 128;                 // k'-row blocks of the rate partials
+  const int nblk_max = (nwv + 15) / 16;
   double *partial;
-  if ((rc = wsget(h->ws, "r_partial", (size_t)nst * nblk, &partial))) return WSFAIL(rc);
+  if ((rc = wsget(h->ws, "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAIL(rc);
   if (!split) {
     double2 *Pk, *gk, *B, *Pq, *Cb;
     const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nwv, ((int64_t)1 << 31) / (Nn * 16)));
@@ -795,8 +796,8 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   } else {
     rc = tc::split_rates_stage(h->split, h->ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
                                mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->kposk,
-                               h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk, ev.e[2],
-                               &h->launches, &h->timer_a, &h->timer_b);
+                               h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk_max, &nblk,
+                               ev.e[2], &h->launches, &h->timer_a, &h->timer_b);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
   }
   CKL();

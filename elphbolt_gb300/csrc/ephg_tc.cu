@@ -795,177 +795,109 @@ __global__ void k_qpack6(int n, const float2 *uf, const float *cx, const float *
   out[i] = r;
 }
 
-// Epilogue for nw = 8, nb = 6 (the bench crystal): as k_epilogue_split2, with
-// the k'-row data (window bands, their energies) loaded once per block and the
-// per-(q, s) data read as one 64-byte record.
-__global__ void __launch_bounds__(EPI_ROWS) k_epilogue_86(int nwv, int j0, int jend, int spb, const float *Cr,
-                                                          const float *Ci, int64_t ldc, RateParams rp, EpiData d,
-                                                          const QRec6 *qrec, double *partial, int nblk) {
-  // LD = 52: 16-byte aligned rows whose 128-bit shared loads are conflict-free
-  constexpr int NW = 8, NB = 6, NC = NW * NB, LD = 52, NC4 = NC / 4, SPB_MAX = 16;
-  extern __shared__ float esm86[];
-  float *sr = esm86, *si = esm86 + EPI_ROWS * LD;
-  __shared__ double wsum[EPI_ROWS / 32];
-  __shared__ double sE[SPB_MAX];
-  __shared__ float sA[SPB_MAX];
-  __shared__ int sP[SPB_MAX];
-  const int row = threadIdx.x;
-  const int ip0 = blockIdx.x * EPI_ROWS, ip = ip0 + row;
-  const bool live = ip < nwv;
-  const int jb0 = j0 + blockIdx.y * spb;
-  const int jb1 = min(jend, jb0 + spb);
-  // per-state data of the block's states, one round trip for all of them
-  if (threadIdx.x < jb1 - jb0) {
-    const int code = d.st_code[jb0 + threadIdx.x];
-    const int p = d.widx[code / NW];
-    const double E = d.ens[(size_t)p * NW + code % NW];
-    sE[threadIdx.x] = E;
-    sA[threadIdx.x] = (float)((E - rp.chempot) / (kB * rp.T));
-    sP[threadIdx.x] = p;
-  }
-  // k'-row data: window bands, their energies, the first two bands' U_k' rows
-  int b1 = 0, b2 = 0, b3 = 0, pp = 0;
-  unsigned wmask = 0;
-  double epsn[NW];
-  float2 ukr[2][NW];
-  int nfirst[2] = {-1, -1};
+// Epilogue for nw = 8, nb = 6, state-parallel: thread t of a block owns initial
+// state j = jb + t and walks the block's 128 k' rows.  Consecutive lanes read
+// consecutive 192-byte state segments of the same GEMM row, so every warp read
+// of C is one contiguous span, and the k'-row data (window bands, energies,
+// U_k') is uniform across the warp.  The sum over the block's rows stays in a
+// register, in row order (deterministic); no shared memory, no barriers.
+// Blocks are 128 states x E86_ROWS k' rows, so that a launch has enough blocks
+// to keep the SMs occupied and each thread's row loop is short.
+constexpr int E86_ROWS = 16;
+
+__global__ void __launch_bounds__(128) k_epilogue_86b(int nwv, int j0, int jend, const float *Cr, const float *Ci,
+                                                      int64_t ldc, RateParams rp, EpiData d, const QRec6 *qrec,
+                                                      double *partial, int nblk) {
+  constexpr int NW = 8, NB = 6, NC = NW * NB;
+  const int j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = j < jend;
+  const int ip0 = blockIdx.y * E86_ROWS, ip1 = min(nwv, ip0 + E86_ROWS);
+  double E = 0.0;
+  float a_occ = 0.f;
+  int a1 = 0, a2 = 0, a3 = 0;
   if (live) {
-    pp = d.widx[ip];
-    b1 = pp % rp.mesh[0];
-    b2 = (pp / rp.mesh[0]) % rp.mesh[1];
-    b3 = pp / (rp.mesh[0] * rp.mesh[1]);
-    int nk = 0;
-#pragma unroll
-    for (int n = 0; n < NW; ++n) {
-      epsn[n] = d.ens[(size_t)pp * NW + n];
-      if (fabs(epsn[n] - rp.enref) <= rp.fsthick) {
-        wmask |= 1u << n;
-        if (nk < 2) nfirst[nk++] = n;
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < 2; ++t)
-      if (nfirst[t] >= 0) {
-        const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + nfirst[t]) * NW);
-#pragma unroll
-        for (int h4 = 0; h4 < NW / 2; ++h4) {
-          float4 t4 = Uk4[h4];
-          ukr[t][2 * h4] = make_float2(t4.x, t4.y);
-          ukr[t][2 * h4 + 1] = make_float2(t4.z, t4.w);
-        }
-      }
+    const int code = d.st_code[j];
+    const int p = d.widx[code / NW];
+    E = d.ens[(size_t)p * NW + code % NW];
+    a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+    a1 = p % rp.mesh[0];
+    a2 = (p / rp.mesh[0]) % rp.mesh[1];
+    a3 = p / (rp.mesh[0] * rp.mesh[1]);
   }
-  const int cum0 = live ? d.cum[ip] : 0;
   const double inv_sig = 1.0 / rp.sigma;
   const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
-  for (int j = jb0; j < jb1; ++j) {
-    __syncthreads();
-    const int64_t cbase = (int64_t)(j - j0) * NC;
-    {
-      float4 vr[NC4], vi[NC4];
+  const int64_t cbase = (int64_t)(j - j0) * NC;
+  double sum = 0.0;
+  for (int ip = ip0; ip < ip1; ++ip) {
+    // warp-uniform k'-row data
+    const int pp = d.widx[ip];
+    const int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+    if (!live) continue;
+    const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                        rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+    const QRec6 *qr = qrec + (size_t)q * NB;
+    const float *gr = Cr + (int64_t)ip * ldc + cbase, *gi = Ci + (int64_t)ip * ldc + cbase;
+    float acc = 0.f;
+    int rank_n = 0;
+    for (int n = 0; n < NW; ++n) {
+      const double eps = d.ens[(size_t)pp * NW + n];
+      if (fabs(eps - rp.enref) > rp.fsthick) continue;
+      const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + n) * NW);
+      float2 uk[NW];
 #pragma unroll
-      for (int k = 0; k < NC4; ++k) {    // all 24 vector loads in flight together
-        const int f = threadIdx.x + EPI_ROWS * k;
-        const int r = f / NC4, c4 = f - r * NC4;
-        const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + 4 * c4;
-        vr[k] = *(const float4 *)(Cr + o);
-        vi[k] = *(const float4 *)(Ci + o);
+      for (int h4 = 0; h4 < NW / 2; ++h4) {
+        const float4 t4 = Uk4[h4];
+        uk[2 * h4] = make_float2(t4.x, t4.y);
+        uk[2 * h4 + 1] = make_float2(t4.z, t4.w);
       }
+      float2 h[NB];
 #pragma unroll
-      for (int k = 0; k < NC4; ++k) {
-        const int f = threadIdx.x + EPI_ROWS * k;
-        const int r = f / NC4, c4 = f - r * NC4;
-        *(float4 *)(sr + r * LD + 4 * c4) = vr[k];
-        *(float4 *)(si + r * LD + 4 * c4) = vi[k];
+      for (int s = 0; s < NB; ++s) {
+        const float4 r0 = *(const float4 *)(gr + NW * s), r1 = *(const float4 *)(gr + NW * s + 4);
+        const float4 i0 = *(const float4 *)(gi + NW * s), i1 = *(const float4 *)(gi + NW * s + 4);
+        const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+        const float xi[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+        float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int np = 0; np < NW; ++np) cfmaf_cj(a, uk[np], make_float2(xr[np], xi[np]));
+        h[s] = a;
       }
-    }
-    __syncthreads();
-    double vsum = 0.0;
-    if (live && wmask) {
-      const int js = j - jb0;
-      const double E = sE[js];
-      const float a_occ = sA[js];
-      const int p = sP[js];
-      const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
-      const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
-                          rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
-      const float *gr = sr + row * LD, *gi = si + row * LD;
-      const QRec6 *qr = qrec + (size_t)q * NB;
-      float acc = 0.0f;
-      int rank_n = 0;
+      const float dn = (float)((E - eps) * inv_sig);
 #pragma unroll
-      for (int n = 0; n < NW; ++n) {
-        if (!((wmask >> n) & 1u)) continue;
-        float2 uk[NW];
-        if (n == nfirst[0] || n == nfirst[1]) {
-          const int t = (n == nfirst[0]) ? 0 : 1;
-#pragma unroll
-          for (int c = 0; c < NW; ++c) uk[c] = t == 0 ? ukr[0][c] : ukr[1][c];
-        } else {
-          const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + n) * NW);
-#pragma unroll
-          for (int h4 = 0; h4 < NW / 2; ++h4) {
-            float4 t4 = Uk4[h4];
-            uk[2 * h4] = make_float2(t4.x, t4.y);
-            uk[2 * h4 + 1] = make_float2(t4.z, t4.w);
+      for (int s = 0; s < NB; ++s) {
+        const float4 *r4 = (const float4 *)(qr + s);
+        const float4 u01 = r4[0], u23 = r4[1], u45 = r4[2], sc = r4[3];
+        float2 g = make_float2(0.f, 0.f);
+        cfmaf(g, make_float2(u01.x, u01.y), h[0]);
+        cfmaf(g, make_float2(u01.z, u01.w), h[1]);
+        cfmaf(g, make_float2(u23.x, u23.y), h[2]);
+        cfmaf(g, make_float2(u23.z, u23.w), h[3]);
+        cfmaf(g, make_float2(u45.x, u45.y), h[4]);
+        cfmaf(g, make_float2(u45.z, u45.w), h[5]);
+        // sc = (cx, bose, w, v)
+        const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
+        const float tp = dn + sc.z, tm = dn - sc.z;
+        const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
+        const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
+        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+        const float xp = g2c * (sc.y + fp) * dp;
+        const float xm = g2c * (1.0f + sc.y - fm) * dm;
+        acc += xp + xm;
+        if (d.g2) {
+          const int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * NB + s;
+          if (off < d.cap) {
+            const double om = d.om[(size_t)q * NB + s];
+            d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+            d.xp[off] = xp;
+            d.xm[off] = xm;
           }
         }
-        float2 h[NB];
-#pragma unroll
-        for (int s = 0; s < NB; ++s) {
-          const float4 r0 = *(const float4 *)(gr + NW * s), r1 = *(const float4 *)(gr + NW * s + 4);
-          const float4 i0 = *(const float4 *)(gi + NW * s), i1 = *(const float4 *)(gi + NW * s + 4);
-          const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-          const float xi[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-          float2 a = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int np = 0; np < NW; ++np) cfmaf_cj(a, uk[np], make_float2(xr[np], xi[np]));
-          h[s] = a;
-        }
-        const float dn = (float)((E - epsn[n]) * inv_sig);
-#pragma unroll
-        for (int s = 0; s < NB; ++s) {
-          const float4 *r4 = (const float4 *)(qr + s);
-          const float4 u01 = r4[0], u23 = r4[1], u45 = r4[2], sc = r4[3];
-          float2 g = make_float2(0.f, 0.f);
-          cfmaf(g, make_float2(u01.x, u01.y), h[0]);
-          cfmaf(g, make_float2(u01.z, u01.w), h[1]);
-          cfmaf(g, make_float2(u23.x, u23.y), h[2]);
-          cfmaf(g, make_float2(u23.z, u23.w), h[3]);
-          cfmaf(g, make_float2(u45.x, u45.y), h[4]);
-          cfmaf(g, make_float2(u45.z, u45.w), h[5]);
-          // sc = (cx, bose, w, v)
-          const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
-          const float tp = dn + sc.z, tm = dn - sc.z;
-          const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
-          const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
-          const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-          const float xp = g2c * (sc.y + fp) * dp;
-          const float xm = g2c * (1.0f + sc.y - fm) * dm;
-          acc += xp + xm;
-          if (d.g2) {
-            int64_t off = (int64_t)j * d.per_state + ((int64_t)cum0 + rank_n) * NB + s;
-            if (off < d.cap) {
-              const double om = d.om[(size_t)q * NB + s];
-              d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
-              d.xp[off] = xp;
-              d.xm[off] = xm;
-            }
-          }
-        }
-        rank_n++;
       }
-      vsum = (double)acc;
+      rank_n++;
     }
-    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_down_sync(0xffffffffu, vsum, o);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = vsum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double sacc = 0.0;
-      for (int w = 0; w < EPI_ROWS / 32; ++w) sacc += wsum[w];
-      partial[(size_t)j * nblk + blockIdx.x] = sacc;
-    }
+    sum += (double)acc;
   }
+  if (live) partial[(size_t)j * nblk + blockIdx.y] = sum;
 }
 
 // ------------------------------------------------------------ orchestration
@@ -980,8 +912,13 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
                       const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
                       const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
-                      const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk,
-                      cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+                      const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
+                      int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+  // k'-row blocks of the rate partials: 16 rows for the nw = 8, nb = 6 epilogue, 128 otherwise
+  const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0);
+  const int nblk = fast86 ? (nwv + E86_ROWS - 1) / E86_ROWS : (nwv + EPI_ROWS - 1) / EPI_ROWS;
+  if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
+  *nblk_used = nblk;
   int rc;
   int *err = nullptr;
   // the device error word lives in the workspace; the caller checks its own word afterwards
@@ -1110,7 +1047,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     tB->begin(st);
     if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st))) return rc;
     tB->end(st);
-    const size_t esm = (size_t)2 * EPI_ROWS * ((nw == 8 && nb == 6) ? 52 : (ncol + 1)) * sizeof(float);
+    const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
     if (rp.delta_kind == 0 && esm > 200 * 1024) {
       dim3 grid(nblk, ns);
       k_epilogue_split<<<grid, 128, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
@@ -1123,15 +1060,16 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
       if (!eattr) {
         TCK(cudaFuncSetAttribute(k_epilogue_split2<8, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         TCK(cudaFuncSetAttribute(k_epilogue_split2<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        TCK(cudaFuncSetAttribute(k_epilogue_86, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+
         eattr = true;
       }
-      if (nw == 8 && nb == 6)
-        k_epilogue_86<<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed, qrec,
-                                                 partial, nblk);
-      else
+      if (nw == 8 && nb == 6) {
+        dim3 g86((ns + 127) / 128, nblk);
+        k_epilogue_86b<<<g86, 128, 0, st>>>(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed, qrec, partial, nblk);
+      } else {
         k_epilogue_split2<0, 0><<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed,
                                                            qt, partial, nblk);
+      }
       TCK(cudaGetLastError());
     } else {
       launch_epilogue_fp32(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed_in, partial, nblk, st);

@@ -18,7 +18,8 @@ struct SplitOperands {
 void free_split(SplitOperands &s);
 const char *last_error();
 
-// Stage A + B + C of the rate pipeline in the split form.  kposA / kposB give
+// Stage A + B + C of the rate pipeline in the split form.  The rate partials
+// [state][k'-block] use up to nblk_max k' blocks; *nblk_used returns the count.  kposA / kposB give
 // the contraction position of each Re / Rp cell (cells ordered far to near).: fills the rate
 // partials [state][k'-block] like the FP64 path.  Records ev_stage_a after
 // stage A.  Returns 0 or an EPHG_ERR_* code (message in last_error()).
@@ -28,8 +29,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const int *st_code, const std::vector<int> &first_state, const int *Rk,
                       const double *degk, const int *kposA, const int *Rq, const double *degq,
                       const int *kposB, const double2 *U, const RateParams &rp, const EpiData &ed,
-                      double *partial, int nblk, cudaEvent_t ev_stage_a, int64_t *launches,
-                      LaunchTimer *tA, LaunchTimer *tB);
+                      double *partial, int nblk_max, int *nblk_used, cudaEvent_t ev_stage_a,
+                      int64_t *launches, LaunchTimer *tA, LaunchTimer *tB);
 
 }  // namespace tc
 }  // namespace ephg
