@@ -115,6 +115,17 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
+// Same with an L2 cache policy (the phase operand, reused by every n-tile, is
+// kept with evict_last so that the streaming output does not push it out).
+__device__ __forceinline__ void tma_load_2d_hint(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%3, "
+      "%4}], [%2], %5;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "l"(policy)
+      : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -206,6 +217,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {   // ---- TMA producer
+      uint64_t keep;
+      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
@@ -217,7 +230,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           mbar_expect_tx(&full[stage], STAGE_BYTES);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
-            tma_load_2d(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + g.Aoff + mt * BM));
+            tma_load_2d_hint(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + g.Aoff + mt * BM),
+                             keep);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
             tma_load_2d(sb + (4 + p) * PLANE_BYTES, &tB, &full[stage], kb * BK, (int)(p * g.Bstride + g.Boff + nt * BN));
@@ -302,8 +316,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          *(float4 *)(cr + c0 + 4 * q) = make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]);
-          *(float4 *)(ci + c0 + 4 * q) = make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]);
+          // streaming stores: the output is read once, later, by another kernel
+          __stcs((float4 *)(cr + c0 + 4 * q), make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]));
+          __stcs((float4 *)(ci + c0 + 4 * q), make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]));
         }
       }
       tc_fence_before();
