@@ -135,8 +135,8 @@ def peaks():
 
 
 def traffic_per_gflop():
-    """DRAM bytes per algorithmic GFLOP of the stage-B contraction, from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "cgemm_stageB_traffic.json")
+    """DRAM bytes per algorithmic GFLOP of the fused stage-B kernel, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "stageB_fused86_traffic.json")
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("dram_bytes_per_alg_gflop")
@@ -258,7 +258,7 @@ def run_ours(args, ws, rank, local):
     W.deallocate_wannier()
     if rank != 0:
         return 0
-    # ---- roofline of the dominant kernel (stage-B 3xTF32 contraction) ----
+    # ---- roofline of the dominant kernel (stage-B 3xTF32 contraction fused with the rate epilogue) ----
     bf16, hbm, src = peaks()
     achieved = st["stage_b_gflop"] / (st["ms_gemm_b"] * 1e-3) / 1e3          # TFLOP/s algorithmic
     peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
@@ -274,7 +274,7 @@ def run_ours(args, ws, rank, local):
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak,
                          "traffic": (tpg * st["stage_b_gflop"] / max(1, st["gemm_b_launches"])) if tpg else None,
-                         "kernel": "k_cgemm_3xtf32 (stage B, Rp Fourier)",
+                         "kernel": "k_stageB_fused86 (stage B Rp Fourier on tcgen05 + rate epilogue)",
                          "peak_source": "%s bf16 %.1f TFLOP/s / 2 (TF32) / 3 (split), of %s" % (src, bf16, src),
                          "launches_per_step": st["gemm_b_launches"],
                          "ms_per_launch": st["ms_gemm_b"] / max(1, st["gemm_b_launches"])},

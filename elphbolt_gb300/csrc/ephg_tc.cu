@@ -6,8 +6,11 @@
 // Each runs here on the 5th-generation tensor cores as a persistent,
 // warp-specialised kernel: one thread issues TMA loads of K-major TF32 operand
 // planes into 64B-swizzled shared memory, one thread issues tcgen05.mma into
-// two double-buffered TMEM accumulators (real, imaginary), and four warps drain
-// TMEM with tcgen05.ld.  Every complex operand X is stored as four planes
+// four TMEM accumulators (main and correction, real and imaginary: all 512
+// columns), and the epilogue warps drain TMEM with tcgen05.ld.  Stage A writes
+// its FP32 result to HBM; for nw = 8, nb = 6 and the Gaussian delta stage B is
+// fused with the rate epilogue (k_stageB_fused86) and its result never leaves
+// the SM.  Every complex operand X is stored as four planes
 // (hi_re, hi_im, lo_re, lo_im) with hi = tf32(X) and lo = tf32(X - hi); each
 // real product uses hi*hi + hi*lo + lo*hi (the "3xTF32" split), FP32
 // accumulation.  -Im*Im terms use the instruction descriptor's negate-A bit.
@@ -143,6 +146,11 @@ __device__ __forceinline__ uint64_t sdesc(const void *p) {
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, K-major, M = 128, N = BN.
 __host__ __device__ constexpr uint32_t idesc_tf32(bool negA) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+__host__ __device__ constexpr uint32_t idesc_tf32_n(bool negA, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
 }
 
@@ -346,14 +354,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2D map over a stack of K-major fp32 planes: (Kp, rows), box (BK, 128), 64B swizzle.
-static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows) {
+// 2D map over a stack of K-major fp32 planes: (Kp, rows), box (BK, box_rows), 64B swizzle.
+static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows, int box_rows = 128) {
   auto fn = encode_fn();
   if (!fn) return tfail(2, "cuTensorMapEncodeTiled unavailable");
   if (((uintptr_t)base & 15) || (Kp % BK)) return tfail(1, "operand planes misaligned");
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
-  cuuint32_t box[2] = {BK, 128};
+  cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -428,6 +436,21 @@ __device__ __forceinline__ void put4(float *P, int64_t plane, int64_t idx, doubl
   P[1 * plane + idx] = hi;
   P[2 * plane + idx] = lr;
   P[3 * plane + idx] = li;
+}
+
+// Six-plane form of a state operand for the stacked (N = 2 x 96) complex MMA:
+// (-hi_im, hi_re, hi_im, -lo_im, lo_re, lo_im), so that [re; im] and [-im; re]
+// are each two adjacent planes.
+__device__ __forceinline__ void put6(float *P, int64_t plane, int64_t idx, double2 v) {
+  float hr, lr, hi, li;
+  split2(v.x, hr, lr);
+  split2(v.y, hi, li);
+  P[0 * plane + idx] = -hi;
+  P[1 * plane + idx] = hr;
+  P[2 * plane + idx] = hi;
+  P[3 * plane + idx] = -li;
+  P[4 * plane + idx] = lr;
+  P[5 * plane + idx] = li;
 }
 
 __device__ inline int phase_idx(int p, int m1, int m2, int m3, int L, int r1, int r2, int r3) {
@@ -510,7 +533,7 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
                                                   const int *widx, const double2 *U, const float *gr, const float *gi,
                                                   int64_t ldg, int m1, int m2, int m3, int L, const double2 *roots,
                                                   const int *Rq, const double *degq, const int *kinv, int Kp2,
-                                                  float *Bp, int64_t Np2) {
+                                                  float *Bp, int64_t Np2, int six) {
   extern __shared__ unsigned char rsm[];
   const int i = i0 + blockIdx.x;
   const int j0 = first_state[i], j1 = first_state[i + 1];
@@ -556,8 +579,9 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
       for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
       const float2 ph = sph[kk];
       const int64_t col = (int64_t)(j0 + js) * ncol + c;
-      put4(Bp, plane, col * Kp2 + kp0 + kk,
-           make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
+      const double2 v = make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x));
+      if (six) put6(Bp, plane, col * Kp2 + kp0 + kk, v);
+      else put4(Bp, plane, col * Kp2 + kp0 + kk, v);
     }
   }
 }
@@ -810,109 +834,352 @@ __global__ void k_qpack6(int n, const float2 *uf, const float *cx, const float *
   out[i] = r;
 }
 
-// Epilogue for nw = 8, nb = 6, state-parallel: thread t of a block owns initial
-// state j = jb + t and walks the block's 128 k' rows.  Consecutive lanes read
-// consecutive 192-byte state segments of the same GEMM row, so every warp read
-// of C is one contiguous span, and the k'-row data (window bands, energies,
-// U_k') is uniform across the warp.  The sum over the block's rows stays in a
-// register, in row order (deterministic); no shared memory, no barriers.
-// Blocks are 128 states x E86_ROWS k' rows, so that a launch has enough blocks
-// to keep the SMs occupied and each thread's row loop is short.
-constexpr int E86_ROWS = 16;
+// ------------------------------------- stage B fused with the rate epilogue
+// For nw = 8, nb = 6 and the Gaussian delta the Rp-Fourier GEMM and the rate
+// epilogue run as one persistent kernel, so that the 48 complex Rp sums of a
+// (k', state) pair never leave the SM.  A tile is 128 window k' rows (TMEM
+// lanes) x 2 whole initial states (96 columns = 2 x 48 of (n', s')).  The
+// state operand is stored as six planes (-hi_im, hi_re, hi_im, -lo_im, lo_re,
+// lo_im), so that each complex product is two MMAs of N = 192 over adjacent
+// planes; the main and correction accumulators (real | imaginary, 192 columns
+// each) start at TMEM columns 0 and 256.  Warp roles: warp 0 lane 0 issues TMA, warp 1 lane 0 issues
+// tcgen05.mma, warps 2..9 are the epilogue: warp w drains TMEM lane quadrant
+// w % 4 for state slot (w - 2) / 4 of the tile.  A drain reads the state's 48
+// columns 8 at a time and forms h(n, s') = sum_n' conj(U_k'[n][n']) G(n', s')
+// for the first two window bands of its k' row in registers (further bands, rare,
+// are finished while the accumulators are still held), releases TMEM, and then
+// forms the vertices while the MMAs of the next tile run.  Each warp reduces its
+// 32 rows' rate contributions in a fixed order and writes one partial per
+// (state, 32-row block): partial[j][mt * 4 + quadrant].
+constexpr int FBN = 96;                                   // state-operand rows per tile (2 states)
+constexpr int F_BPLANE = FBN * BK * 4;                    // 6 KB
+constexpr int F_STAGE = 4 * PLANE_BYTES + 6 * F_BPLANE;   // 68 KB
+constexpr int F_STAGES = 3;
+constexpr int F_THREADS = 320;                            // 10 warps
+constexpr int F_EPI_THREADS = 256;
+constexpr int F_SMEM = F_STAGES * F_STAGE + 1024 + 256;
 
-__global__ void __launch_bounds__(128) k_epilogue_86b(int nwv, int j0, int jend, const float *Cr, const float *Ci,
-                                                      int64_t ldc, RateParams rp, EpiData d, const QRec6 *qrec,
-                                                      double *partial, int nblk) {
-  constexpr int NW = 8, NB = 6, NC = NW * NB;
-  const int j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = j < jend;
-  const int ip0 = blockIdx.y * E86_ROWS, ip1 = min(nwv, ip0 + E86_ROWS);
-  double E = 0.0;
-  float a_occ = 0.f;
-  int a1 = 0, a2 = 0, a3 = 0;
-  if (live) {
-    const int code = d.st_code[j];
-    const int p = d.widx[code / NW];
-    E = d.ens[(size_t)p * NW + code % NW];
-    a_occ = (float)((E - rp.chempot) / (kB * rp.T));
-    a1 = p % rp.mesh[0];
-    a2 = (p / rp.mesh[0]) % rp.mesh[1];
-    a3 = p / (rp.mesh[0] * rp.mesh[1]);
+struct FusedArgs {
+  int mtiles, ntiles, nkb;
+  int64_t Astride, Bstride;   // rows between planes of the phase / state operand stacks
+  int nwv, nst;
+  int *err;
+  const QRec6 *qrec;
+  double *partial;
+  int nblk;
+};
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+// G(n', s') for one s' of the state (8 columns at c0; main + correction combined)
+__device__ __forceinline__ void fused_load_one(uint32_t tr, int c0, float *gre, float *gim) {
+  uint32_t a[8], b[8], c[8], e[8];
+  tmem_ld8_nowait(tr + c0, a);
+  tmem_ld8_nowait(tr + FBN + c0, b);
+  tmem_ld8_nowait(tr + 256 + c0, c);
+  tmem_ld8_nowait(tr + 256 + FBN + c0, e);
+  tmem_wait_ld();
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    gre[i] = __uint_as_float(a[i]) + __uint_as_float(c[i]);
+    gim[i] = __uint_as_float(b[i]) + __uint_as_float(e[i]);
   }
-  const double inv_sig = 1.0 / rp.sigma;
-  const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
-  const int64_t cbase = (int64_t)(j - j0) * NC;
-  double sum = 0.0;
-  for (int ip = ip0; ip < ip1; ++ip) {
-    // warp-uniform k'-row data
-    const int pp = d.widx[ip];
-    const int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
-    if (!live) continue;
-    const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
-                        rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
-    const QRec6 *qr = qrec + (size_t)q * NB;
-    const float *gr = Cr + (int64_t)ip * ldc + cbase, *gi = Ci + (int64_t)ip * ldc + cbase;
-    float acc = 0.f;
-    int rank_n = 0;
-    for (int n = 0; n < NW; ++n) {
-      const double eps = d.ens[(size_t)pp * NW + n];
-      if (fabs(eps - rp.enref) > rp.fsthick) continue;
-      const float4 *Uk4 = (const float4 *)(d.Uf + ((size_t)pp * NW + n) * NW);
-      float2 uk[NW];
+}
+
+__device__ __forceinline__ void load_urow(const float2 *Uf, int pp, int n, float2 *u) {
+  const float4 *U4 = (const float4 *)(Uf + ((size_t)pp * 8 + n) * 8);
 #pragma unroll
-      for (int h4 = 0; h4 < NW / 2; ++h4) {
-        const float4 t4 = Uk4[h4];
-        uk[2 * h4] = make_float2(t4.x, t4.y);
-        uk[2 * h4 + 1] = make_float2(t4.z, t4.w);
+  for (int h4 = 0; h4 < 4; ++h4) {
+    const float4 t = U4[h4];
+    u[2 * h4] = make_float2(t.x, t.y);
+    u[2 * h4 + 1] = make_float2(t.z, t.w);
+  }
+}
+
+// h(s') = sum_n' conj(u[n']) G(n', s') from the 8 loaded columns of s'
+__device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const float *gim) {
+  float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int np = 0; np < 8; ++np) cfmaf_cj(a, u[np], make_float2(gre[np], gim[np]));
+  return a;
+}
+
+// the six vertices (s) of one (k', n) final state for one initial state; returns X+ + X-
+__device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ, float dnorm,
+                                                const EpiData &d, int64_t voff, int q) {
+  float acc = 0.f;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const float4 u01 = __ldg(rec + 4 * s), u23 = __ldg(rec + 4 * s + 1), u45 = __ldg(rec + 4 * s + 2),
+                 sc = __ldg(rec + 4 * s + 3);
+    float2 g = make_float2(0.f, 0.f);
+    cfmaf(g, make_float2(u01.x, u01.y), h[0]);
+    cfmaf(g, make_float2(u01.z, u01.w), h[1]);
+    cfmaf(g, make_float2(u23.x, u23.y), h[2]);
+    cfmaf(g, make_float2(u23.z, u23.w), h[3]);
+    cfmaf(g, make_float2(u45.x, u45.y), h[4]);
+    cfmaf(g, make_float2(u45.z, u45.w), h[5]);
+    // sc = (cx, bose, w, v)
+    const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
+    const float tp = dn + sc.z, tm = dn - sc.z;
+    const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
+    const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
+    const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+    const float xp = g2c * (sc.y + fp) * dp;
+    const float xm = g2c * (1.0f + sc.y - fm) * dm;
+    acc += xp + xm;
+    if (d.g2) {
+      const int64_t off = voff + s;
+      if (off < d.cap) {
+        const double om = d.om[(size_t)q * 6 + s];
+        d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+        d.xp[off] = xp;
+        d.xm[off] = xm;
       }
-      float2 h[NB];
+    }
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(F_THREADS, 1)
+    k_stageB_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedArgs g,
+                     RateParams rp, EpiData d) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + F_STAGES * F_STAGE);
+  uint64_t *empty = full + F_STAGES;
+  uint64_t *tfull = empty + F_STAGES;
+  uint64_t *tempty = tfull + 1;
+  uint32_t *tslot = (uint32_t *)(tempty + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < F_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, F_EPI_THREADS);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int ntile = g.mtiles * g.ntiles;
+
+  if (warp == 0) {
+    if (lane == 0) {   // ---- TMA producer
+      uint64_t keep;
+      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+        const int mt = t % g.mtiles, nt = t / g.mtiles;
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
+          uint8_t *sb = smem + stage * F_STAGE;
+          mbar_expect_tx(&full[stage], F_STAGE);
 #pragma unroll
-      for (int s = 0; s < NB; ++s) {
-        const float4 r0 = *(const float4 *)(gr + NW * s), r1 = *(const float4 *)(gr + NW * s + 4);
-        const float4 i0 = *(const float4 *)(gi + NW * s), i1 = *(const float4 *)(gi + NW * s + 4);
-        const float xr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-        const float xi[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-        float2 a = make_float2(0.f, 0.f);
+          for (int p = 0; p < 4; ++p)
+            tma_load_2d_hint(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + mt * BM), keep);
 #pragma unroll
-        for (int np = 0; np < NW; ++np) cfmaf_cj(a, uk[np], make_float2(xr[np], xi[np]));
-        h[s] = a;
+          for (int p = 0; p < 6; ++p)
+            tma_load_2d(sb + 4 * PLANE_BYTES + p * F_BPLANE, &tB, &full[stage], kb * BK,
+                        (int)(p * g.Bstride + nt * FBN));
+          if (++stage == F_STAGES) { stage = 0; phase ^= 1; }
+        }
       }
-      const float dn = (float)((E - eps) * inv_sig);
+      for (int s = 0; s < F_STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, g.err), stage = (stage + 1) % F_STAGES,
+                                           phase ^= (stage == 0);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {   // ---- MMA issuer
+      // one MMA of N = 192 forms (Ar Br | Ar Bi) from B rows [re; im], the next
+      // (-Ai Bi | Ai Br) from [-im; re]: the real and imaginary halves of a
+      // complex product land side by side in one 192-column accumulator.
+      constexpr uint32_t ID2 = idesc_tf32_n(false, 2 * FBN);
+      int stage = 0;
+      uint32_t phase = 0;
+      int it = 0;
+      bool ok = true;
+      const uint32_t dm = tmem, dc = tmem + 256;   // main, correction (re | im each)
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+        if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&full[stage], phase, g.err)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t *sb = smem + stage * F_STAGE;
 #pragma unroll
-      for (int s = 0; s < NB; ++s) {
-        const float4 *r4 = (const float4 *)(qr + s);
-        const float4 u01 = r4[0], u23 = r4[1], u45 = r4[2], sc = r4[3];
-        float2 g = make_float2(0.f, 0.f);
-        cfmaf(g, make_float2(u01.x, u01.y), h[0]);
-        cfmaf(g, make_float2(u01.z, u01.w), h[1]);
-        cfmaf(g, make_float2(u23.x, u23.y), h[2]);
-        cfmaf(g, make_float2(u23.z, u23.w), h[3]);
-        cfmaf(g, make_float2(u45.x, u45.y), h[4]);
-        cfmaf(g, make_float2(u45.z, u45.w), h[5]);
-        // sc = (cx, bose, w, v)
-        const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
-        const float tp = dn + sc.z, tm = dn - sc.z;
-        const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
-        const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
-        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-        const float xp = g2c * (sc.y + fp) * dp;
-        const float xm = g2c * (1.0f + sc.y - fm) * dm;
-        acc += xp + xm;
-        if (d.g2) {
-          const int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * NB + s;
-          if (off < d.cap) {
-            const double om = d.om[(size_t)q * NB + s];
-            d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
-            d.xp[off] = xp;
-            d.xm[off] = xm;
+          for (int ks = 0; ks < BK / 8; ++ks) {
+            const int off = ks * 32;
+            const uint64_t Ahr = sdesc(sb + 0 * PLANE_BYTES + off), Ahi = sdesc(sb + 1 * PLANE_BYTES + off);
+            const uint64_t Alr = sdesc(sb + 2 * PLANE_BYTES + off), Ali = sdesc(sb + 3 * PLANE_BYTES + off);
+            uint8_t *bb = sb + 4 * PLANE_BYTES;
+            const uint64_t BhN = sdesc(bb + 0 * F_BPLANE + off), BhP = sdesc(bb + 1 * F_BPLANE + off);
+            const uint64_t BlN = sdesc(bb + 3 * F_BPLANE + off), BlP = sdesc(bb + 4 * F_BPLANE + off);
+            const uint32_t acc = (kb == 0 && ks == 0) ? 0u : 1u;
+            umma(dc, Ahr, BlP, ID2, acc);   // hi x lo
+            umma(dc, Ahi, BlN, ID2, 1);
+            umma(dc, Alr, BhP, ID2, 1);     // lo x hi
+            umma(dc, Ali, BhN, ID2, 1);
+            const bool nearblk = (kb == g.nkb - 1) && g.nkb > 1;
+            const uint32_t dd = nearblk ? dc : dm;
+            umma(dd, Ahr, BhP, ID2, nearblk ? 1u : acc);   // hi x hi
+            umma(dd, Ahi, BhN, ID2, 1);
+          }
+          umma_commit(&empty[stage]);
+          if (++stage == F_STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (ok) umma_commit(tfull);
+      }
+    }
+  } else {   // ---- epilogue: warps 2..9
+    const int quad = warp & 3, slot = (warp - 2) >> 2;
+    const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
+    const double inv_sig = 1.0 / rp.sigma;
+    const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
+    const int m0 = rp.mesh[0], m1 = rp.mesh[1], m2 = rp.mesh[2];
+    int it = 0;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
+      const int mt = t % g.mtiles, nt = t / g.mtiles;
+      // ---- row and state data, before the accumulators are ready
+      const int ip = mt * BM + quad * 32 + lane;
+      const int j = nt * 2 + slot;                    // warp-uniform
+      const bool jvalid = j < g.nst;
+      const bool live = jvalid && ip < g.nwv;
+      unsigned wmask = 0;
+      int pp = 0, q = 0;
+      double E = 0.0;
+      float a_occ = 0.f;
+      if (jvalid) {
+        const int code = d.st_code[j];
+        const int p = d.widx[code >> 3];
+        E = d.ens[(size_t)p * 8 + (code & 7)];
+        a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+        if (live) {
+          pp = d.widx[ip];
+          for (int n = 0; n < 8; ++n) wmask |= (fabs(d.ens[(size_t)pp * 8 + n] - rp.enref) <= rp.fsthick) << n;
+          const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
+          const int b1 = pp % m0, b2 = (pp / m0) % m1, b3 = pp / (m0 * m1);
+          q = (int)(floormod(b1 - a1, m0) + m0 * (floormod(b2 - a2, m1) + m1 * floormod(b3 - a3, m2)));
+        }
+      }
+      const int nbw = __popc(wmask);
+      const int n0 = nbw > 0 ? __ffs(wmask) - 1 : 0;
+      const unsigned rest = wmask & (wmask - 1);
+      const int n1 = nbw > 1 ? __ffs(rest) - 1 : 0;
+      float2 u0[8], u1[8];
+      if (nbw > 0) load_urow(d.Uf, pp, n0, u0);
+      if (nbw > 1) load_urow(d.Uf, pp, n1, u1);
+      const float4 *rec = (const float4 *)(g.qrec + (size_t)q * 6);
+      const int64_t vbase = live && d.g2 ? (int64_t)j * d.per_state + (int64_t)d.cum[ip] * 6 : 0;
+      float acc = 0.f;
+      if (!mbar_wait(tfull, it & 1, g.err)) break;
+      tc_fence_after();
+      // ---- drain: h for the first two window bands
+      float2 h0[6], h1[6];
+#pragma unroll
+      for (int sp = 0; sp < 6; ++sp) {
+        float gre[8], gim[8];
+        __syncwarp();
+        fused_load_one(tr, slot * 48 + 8 * sp, gre, gim);
+        if (nbw > 0) h0[sp] = hrot(u0, gre, gim);
+        if (nbw > 1) h1[sp] = hrot(u1, gre, gim);
+      }
+      // further window bands (rare): finished while the accumulators are held
+      const int nbmax = __reduce_max_sync(0xffffffffu, nbw);
+      if (nbmax > 2) {
+        unsigned left = rest & (rest - 1);   // bands after n0, n1
+        for (int b = 2; b < nbmax; ++b) {
+          const bool mine = b < nbw;
+          const int nb_ = mine ? __ffs(left) - 1 : 0;
+          if (mine) left &= left - 1;
+          float2 ux[8], hx[6];
+          if (mine) load_urow(d.Uf, pp, nb_, ux);
+#pragma unroll
+          for (int sp = 0; sp < 6; ++sp) {
+            float gre[8], gim[8];
+            __syncwarp();
+            fused_load_one(tr, slot * 48 + 8 * sp, gre, gim);
+            if (mine) hx[sp] = hrot(ux, gre, gim);
+          }
+          if (mine) {
+            const float dn = (float)((E - d.ens[(size_t)pp * 8 + nb_]) * inv_sig);
+            acc += fused_vertices(hx, rec, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q);
           }
         }
       }
-      rank_n++;
+      tc_fence_before();
+      mbar_arrive(tempty);
+      // ---- vertices of the first two bands, overlapping the next tile's MMAs
+      float acc01 = 0.f;
+      if (nbw > 0) {
+        const float dn = (float)((E - d.ens[(size_t)pp * 8 + n0]) * inv_sig);
+        acc01 += fused_vertices(h0, rec, dn, a_occ, dnorm, d, vbase, q);
+      }
+      if (nbw > 1) {
+        const float dn = (float)((E - d.ens[(size_t)pp * 8 + n1]) * inv_sig);
+        acc01 += fused_vertices(h1, rec, dn, a_occ, dnorm, d, vbase + 6, q);
+      }
+      double v = (double)acc01 + (double)acc;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0 && jvalid) g.partial[(size_t)j * g.nblk + mt * 4 + quad] = v;
     }
-    sum += (double)acc;
   }
-  if (live) partial[(size_t)j * nblk + blockIdx.y] = sum;
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2, int KpB, int nwv, int nst,
+                          const RateParams &rp, const EpiData &ed, const QRec6 *qrec, double *partial, int nblk,
+                          int *err, cudaStream_t st) {
+  if (MpB % BM || Np2 % FBN || KpB % BK) return tfail(1, "stage B: shapes not tile multiples");
+  if (4 * (int64_t)MpB > INT32_MAX || 6 * Np2 > INT32_MAX) return tfail(1, "stage B: operand too tall for TMA coords");
+  CUtensorMap ta, tb;
+  int rc;
+  if ((rc = make_map(&ta, PB, KpB, 4 * (int64_t)MpB)) || (rc = make_map(&tb, B2, KpB, 6 * Np2, FBN))) return rc;
+  static bool attr = false;
+  if (!attr) {
+    TCK(cudaFuncSetAttribute(k_stageB_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
+    attr = true;
+  }
+  FusedArgs g;
+  g.mtiles = MpB / BM;
+  g.ntiles = (nst + 1) / 2;
+  g.nkb = KpB / BK;
+  g.Astride = MpB;
+  g.Bstride = Np2;
+  g.nwv = nwv;
+  g.nst = nst;
+  g.err = err;
+  g.qrec = qrec;
+  g.partial = partial;
+  g.nblk = nblk;
+  if ((int64_t)g.ntiles * FBN > Np2) return tfail(1, "stage B: state operand too short");
+  const int64_t tiles = (int64_t)g.mtiles * g.ntiles;
+  if (tiles > INT32_MAX) return tfail(1, "stage B: too many tiles");
+  const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  k_stageB_fused86<<<grid, F_THREADS, F_SMEM, st>>>(ta, tb, g, rp, ed);
+  TCK(cudaGetLastError());
+  return 0;
 }
 
 // ------------------------------------------------------------ orchestration
@@ -931,7 +1198,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
   // k'-row blocks of the rate partials: 16 rows for the nw = 8, nb = 6 epilogue, 128 otherwise
   const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0);
-  const int nblk = fast86 ? (nwv + E86_ROWS - 1) / E86_ROWS : (nwv + EPI_ROWS - 1) / EPI_ROWS;
+  // rate partials per state: one per 32-row block of the fused kernel, one per 128 rows otherwise
+  const int nblk = fast86 ? (int)(rup(nwv, BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
   if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
   *nblk_used = nblk;
   int rc;
@@ -955,15 +1223,17 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   const int ncol = nw * nb;
   // stage A in k chunks of kc rows (multiple of BM)
   const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nwv, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
-  const int64_t Np2 = rup((int64_t)nst * ncol, BN);
+  // state-operand rows: whole 8-state groups (8 * 48 = 384 rows, a multiple of both tile widths)
+  const int64_t Np2 = fast86 ? rup(nst, 8) * ncol : rup((int64_t)nst * ncol, BN);
+  const int nplB = fast86 ? 6 : 4;   // planes of the state operand
   float *PA, *CAr, *CAi, *B2;
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
-      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)4 * Np2 * KpB, &B2)))
+      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)nplB * Np2 * KpB, &B2)))
     return tfail(6, ws.msg.c_str());
   // the rotation writes every K position of every state row; zero the padding rows only
   {
     const int64_t used = (int64_t)nst * ncol;
-    for (int pl = 0; pl < 4; ++pl)
+    for (int pl = 0; pl < nplB; ++pl)
       if (Np2 > used)
         TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
   }
@@ -997,10 +1267,10 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
           rattr = true;
         }
         k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, widx, U, CAr, CAi, NpA, mesh[0], mesh[1],
-                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
+                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2, fast86 ? 1 : 0);
         TCK(cudaGetLastError());
         (*launches)++;
-      } else {   // large nw*nw*nb: one thread per output element
+      } else {   // large nw*nw*nb: one thread per output element (never the six-plane nw = 8 form)
         for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
           int je = std::min(j1, j0 + 32768);
           dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
@@ -1016,15 +1286,16 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   TCK(cudaEventRecord(ev_stage_a, st));
   // stage B: A planes = e^{2 pi i k'.Rp} for the window k'
   const int MpB = (int)rup(nwv, BM);
-  float *PB, *CBr, *CBi;
+  float *PB, *CBr = nullptr, *CBi = nullptr;
   // states per chunk: a multiple of 8 (8 * 48 = 3 * 128 columns) bounded by ~2 GB of output
   int64_t sc = ((int64_t)1 << 31) / ((int64_t)MpB * ncol * 8);
   sc = std::max<int64_t>(8, sc / 8 * 8);
   sc = std::min<int64_t>(sc, rup(nst, 8));
   sc = std::min<int64_t>(sc, 32768);
   const int64_t NpC = rup(sc * ncol, BN);
-  if ((rc = wsget(ws, "tc_PB", (size_t)4 * MpB * KpB, &PB)) || (rc = wsget(ws, "tc_CBr", (size_t)MpB * NpC, &CBr)) ||
-      (rc = wsget(ws, "tc_CBi", (size_t)MpB * NpC, &CBi)))
+  if ((rc = wsget(ws, "tc_PB", (size_t)4 * MpB * KpB, &PB)) ||
+      (!fast86 && ((rc = wsget(ws, "tc_CBr", (size_t)MpB * NpC, &CBr)) ||
+                   (rc = wsget(ws, "tc_CBi", (size_t)MpB * NpC, &CBi)))))
     return tfail(6, ws.msg.c_str());
   TCK(cudaMemsetAsync(PB, 0, (size_t)4 * MpB * KpB * sizeof(float), st));
   {
@@ -1056,7 +1327,13 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     TCK(cudaGetLastError());
     (*launches)++;
   }
-  for (int64_t j0 = 0; j0 < nst; j0 += sc) {
+  if (fast86) {   // one fused GEMM + epilogue launch over all states
+    tB->begin(st);
+    if ((rc = stageB_fused86(PB, MpB, B2, Np2, KpB, nwv, nst, rp, ed, qrec, partial, nblk, err, st))) return rc;
+    tB->end(st);
+    *launches += 1;
+  }
+  for (int64_t j0 = 0; j0 < nst && !fast86; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
@@ -1073,18 +1350,11 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
       const size_t sm = esm;
       static bool eattr = false;
       if (!eattr) {
-        TCK(cudaFuncSetAttribute(k_epilogue_split2<8, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         TCK(cudaFuncSetAttribute(k_epilogue_split2<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-
         eattr = true;
       }
-      if (nw == 8 && nb == 6) {
-        dim3 g86((ns + 127) / 128, nblk);
-        k_epilogue_86b<<<g86, 128, 0, st>>>(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed, qrec, partial, nblk);
-      } else {
-        k_epilogue_split2<0, 0><<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed,
-                                                           qt, partial, nblk);
-      }
+      k_epilogue_split2<0, 0><<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed, qt,
+                                                         partial, nblk);
       TCK(cudaGetLastError());
     } else {
       launch_epilogue_fp32(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed_in, partial, nblk, st);

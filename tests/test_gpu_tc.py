@@ -93,3 +93,39 @@ def test_el_rates_split_simplex_deltas(oracle_lib, delta):
     mask = o["rates"] > 1e-8 * o["rates"].max()
     rel = np.abs(g["rates"] - o["rates"])[mask] / o["rates"][mask]
     assert rel.max() <= 1e-6, rel.max()
+
+
+def test_el_rates_split_many_window_bands(oracle_lib):
+    """A window of +-3 eV holds 4 to 8 of the 8 bands at every k': the fused
+    stage-B epilogue's path for more than two window bands per k' row."""
+    from elphbolt_gb300.wannier import Wannier
+    wd = S.make_wannier(S.make_crystal_si_like(), 8, supercell=(3, 3, 3), seed=12)
+    req = S.si_like_request(wd, (4, 4, 4), window=3.0, shift=0.0)
+    o = oracle_lib.Wannier(wd).el_rates(req, literal=True, vertices=True)
+    W = Wannier(wd)
+    g = W.el_rates(req, precision=_lib.PREC_SPLIT_TF32, vertices=True)
+    W.deallocate_wannier()
+    assert np.array_equal(g["indexlist"], o["indexlist"]) and g["vertices"] == o["vertices"]
+    scale = np.abs(o["g2"]).max()
+    assert np.all(np.abs(g["g2"] - o["g2"]) <= 1e-5 * np.abs(o["g2"]) + 1e-6 * scale)
+    mask = o["rates"] > 0
+    rel = np.abs(g["rates"] - o["rates"])[mask] / o["rates"][mask]
+    assert rel.max() <= 1e-6, rel.max()
+
+
+def test_el_rates_split_vs_fp64_multi_tile():
+    """12^3 Si-like request (1,441 window k' rows: 12 row tiles, ~800 state-pair
+    tiles): the split form against the library's FP64 form, which the oracle
+    pins on the small cases; rates within 1e-6 relative."""
+    from elphbolt_gb300.wannier import Wannier
+    wd = S.si_like(nw=8)
+    req = S.si_like_request(wd, (12, 12, 12))
+    W = Wannier(wd)
+    d = W.el_rates(req, precision=_lib.PREC_FP64)
+    g = W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+    W.deallocate_wannier()
+    assert g["nwv"] > 1024 and np.array_equal(g["indexlist"], d["indexlist"])
+    mask = d["rates"] > 0
+    rel = np.abs(g["rates"] - d["rates"])[mask] / d["rates"][mask]
+    assert rel.max() <= 1e-6, rel.max()
+    assert np.all(g["rates"][~mask] == 0)
