@@ -813,27 +813,6 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
   }
 }
 
-// Packed per-(q, s) record of the nb = 6 fast path: the mass-scaled phonon
-// eigenvector row and the four scalars of the epilogue in one 64-byte line.
-struct __align__(16) QRec6 {
-  float2 u[6];
-  float cx, bose, w, v;
-};
-
-__global__ void k_qpack6(int n, const float2 *uf, const float *cx, const float *bs, const float *w, const float *v,
-                         QRec6 *out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  QRec6 r;
-#pragma unroll
-  for (int c = 0; c < 6; ++c) r.u[c] = uf[(size_t)i * 6 + c];
-  r.cx = cx[i];
-  r.bose = bs[i];
-  r.w = w[i];
-  r.v = v[i];
-  out[i] = r;
-}
-
 // ------------------------------------- stage B fused with the rate epilogue
 // For nw = 8, nb = 6 and the Gaussian delta the Rp-Fourier GEMM and the rate
 // epilogue run as one persistent kernel, so that the 48 complex Rp sums of a
@@ -859,15 +838,92 @@ constexpr int F_THREADS = 320;                            // 10 warps
 constexpr int F_EPI_THREADS = 256;
 constexpr int F_SMEM = F_STAGES * F_STAGE + 1024 + 256;
 
+// Field-major tables of the fused epilogue.  Window k' rows are nearly
+// consecutive mesh points, so the 32 rows of a warp read nearly consecutive
+// entries of each table (a few cache lines per load instead of 32).
+struct StateRec {      // per initial state j
+  double E;            // eV
+  float a_occ;         // (E - mu) / kT
+  int apack;           // mesh coordinates of k: a1 | a2 << 10 | a3 << 20
+};
+
+// The row and q tables are blocked by 32: entry (i, field) sits at
+// ((i >> 5) * nfields + field) * 32 + (i & 31), so a warp's 32 rows read
+// consecutive words of each field and the field offsets are constants.
+struct FusedTabs {
+  const int4 *row;         // [MpB] (mesh index, window-band mask, first final-state rank, packed coordinates)
+  const StateRec *state;   // [nst]
+  const float4 *U4;        // row-blocked, fields n * 4 + h: U_k'[n][2h], U_k'[n][2h + 1] (fp32 complex)
+  const double *ensw;      // row-blocked, fields n: window-k' band energies
+  const float4 *rec;       // q-blocked, fields s * 4 + f: u[s][0..1], u[s][2..3], u[s][4..5], (cx, bose, w, v)
+  int MpB, N;
+};
+
+__host__ __device__ __forceinline__ int64_t blk32(int64_t i, int nf, int f) {
+  return ((i >> 5) * nf + f) * 32 + (i & 31);
+}
+
 struct FusedArgs {
   int mtiles, ntiles, nkb;
   int64_t Astride, Bstride;   // rows between planes of the phase / state operand stacks
   int nwv, nst;
   int *err;
-  const QRec6 *qrec;
   double *partial;
   int nblk;
 };
+
+__global__ void k_fused_rows(int nwv, int MpB, const int *widx, const double *ens, const float2 *Uf, const int *cum,
+                             double enref, double fsthick, int m0, int m1, int4 *row, float4 *U4, double *ensw) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= MpB) return;
+  if (ip >= nwv) {
+    row[ip] = make_int4(0, 0, 0, 0);
+    for (int n = 0; n < 8; ++n) {
+      ensw[blk32(ip, 8, n)] = 0.0;
+      for (int h = 0; h < 4; ++h) U4[blk32(ip, 32, n * 4 + h)] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
+  const int pp = widx[ip];
+  int wmask = 0;
+  for (int n = 0; n < 8; ++n) {
+    const double e = ens[(size_t)pp * 8 + n];
+    ensw[blk32(ip, 8, n)] = e;
+    wmask |= (fabs(e - enref) <= fsthick) << n;
+    for (int h = 0; h < 4; ++h) {
+      const float2 a = Uf[((size_t)pp * 8 + n) * 8 + 2 * h], b = Uf[((size_t)pp * 8 + n) * 8 + 2 * h + 1];
+      U4[blk32(ip, 32, n * 4 + h)] = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+  const int b1 = pp % m0, b2 = (pp / m0) % m1, b3 = pp / (m0 * m1);
+  row[ip] = make_int4(pp, wmask, cum ? cum[ip] : 0, b1 | (b2 << 10) | (b3 << 20));
+}
+
+__global__ void k_fused_states(int nst, const int *st_code, const int *widx, const double *ens, double chempot,
+                               double kT, int m0, int m1, StateRec *out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nst) return;
+  const int code = st_code[j];
+  const int p = widx[code >> 3];
+  StateRec r;
+  r.E = ens[(size_t)p * 8 + (code & 7)];
+  r.a_occ = (float)((r.E - chempot) / kT);
+  const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
+  r.apack = a1 | (a2 << 10) | (a3 << 20);
+  out[j] = r;
+}
+
+__global__ void k_fused_recs(int N, const float2 *uf, const float *cx, const float *bs, const float *w, const float *v,
+                             float4 *rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;   // (q, s) = (i / 6, i % 6)
+  if (i >= N * 6) return;
+  const int q = i / 6, s = i % 6;
+  const float2 *u = uf + (size_t)i * 6;
+  rec[blk32(q, 24, s * 4 + 0)] = make_float4(u[0].x, u[0].y, u[1].x, u[1].y);
+  rec[blk32(q, 24, s * 4 + 1)] = make_float4(u[2].x, u[2].y, u[3].x, u[3].y);
+  rec[blk32(q, 24, s * 4 + 2)] = make_float4(u[4].x, u[4].y, u[5].x, u[5].y);
+  rec[blk32(q, 24, s * 4 + 3)] = make_float4(cx[i], bs[i], w[i], v[i]);
+}
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -892,13 +948,14 @@ __device__ __forceinline__ void fused_load_one(uint32_t tr, int c0, float *gre, 
   }
 }
 
-__device__ __forceinline__ void load_urow(const float2 *Uf, int pp, int n, float2 *u) {
-  const float4 *U4 = (const float4 *)(Uf + ((size_t)pp * 8 + n) * 8);
+// U_k' row n of this lane's k' row (ub = the lane's entry of field 0)
+__device__ __forceinline__ void load_urow(const float4 *ub, int n, float2 *u) {
+  const float4 *un = ub + n * 128;
 #pragma unroll
-  for (int h4 = 0; h4 < 4; ++h4) {
-    const float4 t = U4[h4];
-    u[2 * h4] = make_float2(t.x, t.y);
-    u[2 * h4 + 1] = make_float2(t.z, t.w);
+  for (int h = 0; h < 4; ++h) {
+    const float4 t = __ldg(un + h * 32);
+    u[2 * h] = make_float2(t.x, t.y);
+    u[2 * h + 1] = make_float2(t.z, t.w);
   }
 }
 
@@ -911,13 +968,14 @@ __device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const 
 }
 
 // the six vertices (s) of one (k', n) final state for one initial state; returns X+ + X-
-__device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ, float dnorm,
-                                                const EpiData &d, int64_t voff, int q) {
+// rec = the lane's entry of field 0 of q's block: fields 32 float4 apart
+__device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ,
+                                                float dnorm, const EpiData &d, int64_t voff, int q) {
   float acc = 0.f;
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
-    const float4 u01 = __ldg(rec + 4 * s), u23 = __ldg(rec + 4 * s + 1), u45 = __ldg(rec + 4 * s + 2),
-                 sc = __ldg(rec + 4 * s + 3);
+    const float4 u01 = __ldg(rec + (4 * s) * 32), u23 = __ldg(rec + (4 * s + 1) * 32),
+                 u45 = __ldg(rec + (4 * s + 2) * 32), sc = __ldg(rec + (4 * s + 3) * 32);
     float2 g = make_float2(0.f, 0.f);
     cfmaf(g, make_float2(u01.x, u01.y), h[0]);
     cfmaf(g, make_float2(u01.z, u01.w), h[1]);
@@ -949,7 +1007,7 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
 
 __global__ void __launch_bounds__(F_THREADS, 1)
     k_stageB_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedArgs g,
-                     RateParams rp, EpiData d) {
+                     FusedTabs tb, RateParams rp, EpiData d) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + F_STAGES * F_STAGE);
@@ -1058,36 +1116,34 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
       const int mt = t % g.mtiles, nt = t / g.mtiles;
       // ---- row and state data, before the accumulators are ready
-      const int ip = mt * BM + quad * 32 + lane;
+      const int ip = mt * BM + quad * 32 + lane;      // < MpB
       const int j = nt * 2 + slot;                    // warp-uniform
       const bool jvalid = j < g.nst;
-      const bool live = jvalid && ip < g.nwv;
+      const int4 ri = __ldg(tb.row + ip);             // zero for padding rows: no window band
       unsigned wmask = 0;
-      int pp = 0, q = 0;
+      int q = 0;
       double E = 0.0;
       float a_occ = 0.f;
       if (jvalid) {
-        const int code = d.st_code[j];
-        const int p = d.widx[code >> 3];
-        E = d.ens[(size_t)p * 8 + (code & 7)];
-        a_occ = (float)((E - rp.chempot) / (kB * rp.T));
-        if (live) {
-          pp = d.widx[ip];
-          for (int n = 0; n < 8; ++n) wmask |= (fabs(d.ens[(size_t)pp * 8 + n] - rp.enref) <= rp.fsthick) << n;
-          const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
-          const int b1 = pp % m0, b2 = (pp / m0) % m1, b3 = pp / (m0 * m1);
-          q = (int)(floormod(b1 - a1, m0) + m0 * (floormod(b2 - a2, m1) + m1 * floormod(b3 - a3, m2)));
-        }
+        const StateRec sr = tb.state[j];
+        E = sr.E;
+        a_occ = sr.a_occ;
+        wmask = (unsigned)ri.y;
+        const int a1 = sr.apack & 1023, a2 = (sr.apack >> 10) & 1023, a3 = sr.apack >> 20;
+        const int b1 = ri.w & 1023, b2 = (ri.w >> 10) & 1023, b3 = ri.w >> 20;
+        q = (int)(floormod(b1 - a1, m0) + m0 * (floormod(b2 - a2, m1) + m1 * floormod(b3 - a3, m2)));
       }
       const int nbw = __popc(wmask);
       const int n0 = nbw > 0 ? __ffs(wmask) - 1 : 0;
       const unsigned rest = wmask & (wmask - 1);
       const int n1 = nbw > 1 ? __ffs(rest) - 1 : 0;
+      const float4 *ub = tb.U4 + blk32(ip, 32, 0);
+      const double *eb = tb.ensw + blk32(ip, 8, 0);
+      const float4 *rq = tb.rec + blk32(q, 24, 0);
       float2 u0[8], u1[8];
-      if (nbw > 0) load_urow(d.Uf, pp, n0, u0);
-      if (nbw > 1) load_urow(d.Uf, pp, n1, u1);
-      const float4 *rec = (const float4 *)(g.qrec + (size_t)q * 6);
-      const int64_t vbase = live && d.g2 ? (int64_t)j * d.per_state + (int64_t)d.cum[ip] * 6 : 0;
+      if (nbw > 0) load_urow(ub, n0, u0);
+      if (nbw > 1) load_urow(ub, n1, u1);
+      const int64_t vbase = (nbw > 0 && d.g2) ? (int64_t)j * d.per_state + (int64_t)ri.z * 6 : 0;
       float acc = 0.f;
       if (!mbar_wait(tfull, it & 1, g.err)) break;
       tc_fence_after();
@@ -1110,7 +1166,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const int nb_ = mine ? __ffs(left) - 1 : 0;
           if (mine) left &= left - 1;
           float2 ux[8], hx[6];
-          if (mine) load_urow(d.Uf, pp, nb_, ux);
+          if (mine) load_urow(ub, nb_, ux);
 #pragma unroll
           for (int sp = 0; sp < 6; ++sp) {
             float gre[8], gim[8];
@@ -1119,8 +1175,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
             if (mine) hx[sp] = hrot(ux, gre, gim);
           }
           if (mine) {
-            const float dn = (float)((E - d.ens[(size_t)pp * 8 + nb_]) * inv_sig);
-            acc += fused_vertices(hx, rec, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q);
+            const float dn = (float)((E - __ldg(eb + nb_ * 32)) * inv_sig);
+            acc += fused_vertices(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q);
           }
         }
       }
@@ -1129,12 +1185,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       // ---- vertices of the first two bands, overlapping the next tile's MMAs
       float acc01 = 0.f;
       if (nbw > 0) {
-        const float dn = (float)((E - d.ens[(size_t)pp * 8 + n0]) * inv_sig);
-        acc01 += fused_vertices(h0, rec, dn, a_occ, dnorm, d, vbase, q);
+        const float dn = (float)((E - __ldg(eb + n0 * 32)) * inv_sig);
+        acc01 += fused_vertices(h0, rq, dn, a_occ, dnorm, d, vbase, q);
       }
       if (nbw > 1) {
-        const float dn = (float)((E - d.ens[(size_t)pp * 8 + n1]) * inv_sig);
-        acc01 += fused_vertices(h1, rec, dn, a_occ, dnorm, d, vbase + 6, q);
+        const float dn = (float)((E - __ldg(eb + n1 * 32)) * inv_sig);
+        acc01 += fused_vertices(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q);
       }
       double v = (double)acc01 + (double)acc;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1149,7 +1205,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
 }
 
 static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2, int KpB, int nwv, int nst,
-                          const RateParams &rp, const EpiData &ed, const QRec6 *qrec, double *partial, int nblk,
+                          const RateParams &rp, const EpiData &ed, const FusedTabs &tabs, double *partial, int nblk,
                           int *err, cudaStream_t st) {
   if (MpB % BM || Np2 % FBN || KpB % BK) return tfail(1, "stage B: shapes not tile multiples");
   if (4 * (int64_t)MpB > INT32_MAX || 6 * Np2 > INT32_MAX) return tfail(1, "stage B: operand too tall for TMA coords");
@@ -1170,14 +1226,13 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   g.nwv = nwv;
   g.nst = nst;
   g.err = err;
-  g.qrec = qrec;
   g.partial = partial;
   g.nblk = nblk;
   if ((int64_t)g.ntiles * FBN > Np2) return tfail(1, "stage B: state operand too short");
   const int64_t tiles = (int64_t)g.mtiles * g.ntiles;
   if (tiles > INT32_MAX) return tfail(1, "stage B: too many tiles");
   const int grid = (int)std::min<int64_t>(tiles, num_sms());
-  k_stageB_fused86<<<grid, F_THREADS, F_SMEM, st>>>(ta, tb, g, rp, ed);
+  k_stageB_fused86<<<grid, F_THREADS, F_SMEM, st>>>(ta, tb, g, tabs, rp, ed);
   TCK(cudaGetLastError());
   return 0;
 }
@@ -1197,7 +1252,9 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
                       int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
   // k'-row blocks of the rate partials: 16 rows for the nw = 8, nb = 6 epilogue, 128 otherwise
-  const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0);
+  // (mesh coordinates are packed in 10 bits each in the fused kernel's tables)
+  const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
+                       mesh[2] <= 1024);
   // rate partials per state: one per 32-row block of the fused kernel, one per 128 rows otherwise
   const int nblk = fast86 ? (int)(rup(nwv, BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
   if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
@@ -1320,16 +1377,28 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   EpiData ed = ed_in;
   ed.Uf = Uf;
   QTab qt{cx, bs, w, v};
-  QRec6 *qrec = nullptr;
-  if (nw == 8 && nb == 6) {
-    if ((rc = wsget(ws, "tc_qrec", (size_t)N * nb, &qrec))) return tfail(6, ws.msg.c_str());
-    k_qpack6<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.uf, cx, bs, w, v, qrec);
+  FusedTabs tabs{};
+  if (fast86) {
+    int4 *trow;
+    StateRec *tst;
+    float4 *tU4, *trec;
+    double *tens;
+    if ((rc = wsget(ws, "tc_frow", (size_t)MpB, &trow)) || (rc = wsget(ws, "tc_fst", (size_t)nst, &tst)) ||
+        (rc = wsget(ws, "tc_fU4", (size_t)32 * MpB, &tU4)) || (rc = wsget(ws, "tc_fens", (size_t)8 * MpB, &tens)) ||
+        (rc = wsget(ws, "tc_frec", (size_t)24 * rup(N, 32), &trec)))
+      return tfail(6, ws.msg.c_str());
+    k_fused_rows<<<(MpB + 127) / 128, 128, 0, st>>>(nwv, MpB, widx, ed_in.ens, Uf, ed_in.cum, rp.enref, rp.fsthick,
+                                                    mesh[0], mesh[1], trow, tU4, tens);
+    k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, widx, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
+                                                      mesh[1], tst);
+    k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, cx, bs, w, v, trec);
     TCK(cudaGetLastError());
-    (*launches)++;
+    *launches += 3;
+    tabs = FusedTabs{trow, tst, tU4, tens, trec, MpB, N};
   }
   if (fast86) {   // one fused GEMM + epilogue launch over all states
     tB->begin(st);
-    if ((rc = stageB_fused86(PB, MpB, B2, Np2, KpB, nwv, nst, rp, ed, qrec, partial, nblk, err, st))) return rc;
+    if ((rc = stageB_fused86(PB, MpB, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st))) return rc;
     tB->end(st);
     *launches += 1;
   }
