@@ -354,18 +354,20 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2D map over a stack of K-major fp32 planes: (Kp, rows), box (BK, box_rows), 64B swizzle.
-static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows, int box_rows = 128) {
+// 2D map over a stack of K-major fp32 planes: (Kp, rows), box (box_k, box_rows);
+// box_k = 16 (64 B rows) uses the 64B swizzle, box_k = 8 (32 B rows) the 32B swizzle.
+static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows, int box_rows = 128, int box_k = BK) {
   auto fn = encode_fn();
   if (!fn) return tfail(2, "cuTensorMapEncodeTiled unavailable");
-  if (((uintptr_t)base & 15) || (Kp % BK)) return tfail(1, "operand planes misaligned");
+  if (((uintptr_t)base & 15) || (Kp % box_k) || (box_k != 8 && box_k != 16))
+    return tfail(1, "operand planes misaligned");
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
-  cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return tfail(2, "cuTensorMapEncodeTiled failed");
   return 0;
 }
@@ -438,7 +440,7 @@ __device__ __forceinline__ void put4(float *P, int64_t plane, int64_t idx, doubl
   P[3 * plane + idx] = li;
 }
 
-// Six-plane form of a state operand for the stacked (N = 2 x 96) complex MMA:
+// Six-plane form of an operand for the stacked complex MMA (two N-halves):
 // (-hi_im, hi_re, hi_im, -lo_im, lo_re, lo_im), so that [re; im] and [-im; re]
 // are each two adjacent planes.
 __device__ __forceinline__ void put6(float *P, int64_t plane, int64_t idx, double2 v) {
@@ -451,6 +453,25 @@ __device__ __forceinline__ void put6(float *P, int64_t plane, int64_t idx, doubl
   P[3 * plane + idx] = -li;
   P[4 * plane + idx] = lr;
   P[5 * plane + idx] = li;
+}
+
+// The stage-A operand of the fused nw = 8, nb = 6 path: column
+// c = m' + 8 (kp + KpB (n' + 8 s')) holds g(Re, Rp = kinvB[kp])[n', m', s'], so
+// that a 128-column tile is 16 contraction positions x 8 initial bands of one
+// (n', s'); K position of Re = kposA[Re].  Six planes [6][NA][KpA].
+__global__ void k_gplanes_a6(int nwsk, int64_t Nn, const double2 *G, const int *kposA, const int *kinvB, int KpB,
+                             float *P, int64_t NA, int KpA) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= NA * nwsk) return;
+  const int64_t c = idx / nwsk;
+  const int re = (int)(idx % nwsk);
+  const int mp = (int)(c & 7);
+  const int64_t rest = c >> 3;
+  const int kp = (int)(rest % KpB), ns = (int)(rest / KpB);
+  const int np = ns & 7, sp = ns >> 3;
+  const int rp = kinvB[kp];
+  const double2 v = rp >= 0 ? G[(int64_t)re * Nn + np + 8 * (mp + 8 * (sp + 6 * (int64_t)rp))] : make_double2(0.0, 0.0);
+  put6(P, NA * KpA, c * KpA + kposA[re], v);
 }
 
 __device__ inline int phase_idx(int p, int m1, int m2, int m3, int L, int r1, int r2, int r3) {
@@ -533,7 +554,7 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
                                                   const int *widx, const double2 *U, const float *gr, const float *gi,
                                                   int64_t ldg, int m1, int m2, int m3, int L, const double2 *roots,
                                                   const int *Rq, const double *degq, const int *kinv, int Kp2,
-                                                  float *Bp, int64_t Np2, int six) {
+                                                  float *Bp, int64_t Np2) {
   extern __shared__ unsigned char rsm[];
   const int i = i0 + blockIdx.x;
   const int j0 = first_state[i], j1 = first_state[i + 1];
@@ -579,9 +600,8 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
       for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
       const float2 ph = sph[kk];
       const int64_t col = (int64_t)(j0 + js) * ncol + c;
-      const double2 v = make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x));
-      if (six) put6(Bp, plane, col * Kp2 + kp0 + kk, v);
-      else put4(Bp, plane, col * Kp2 + kp0 + kk, v);
+      put4(Bp, plane, col * Kp2 + kp0 + kk,
+           make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
     }
   }
 }
@@ -933,13 +953,15 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t *r) {
                : "r"(taddr));
 }
 
-// G(n', s') for one s' of the state (8 columns at c0; main + correction combined)
+// 8 complex columns at c0 (main + correction combined); the main and correction
+// accumulators start at TMEM columns 0 and 256, their imaginary halves IM later
+template <int IM>
 __device__ __forceinline__ void fused_load_one(uint32_t tr, int c0, float *gre, float *gim) {
   uint32_t a[8], b[8], c[8], e[8];
   tmem_ld8_nowait(tr + c0, a);
-  tmem_ld8_nowait(tr + FBN + c0, b);
+  tmem_ld8_nowait(tr + IM + c0, b);
   tmem_ld8_nowait(tr + 256 + c0, c);
-  tmem_ld8_nowait(tr + 256 + FBN + c0, e);
+  tmem_ld8_nowait(tr + 256 + IM + c0, e);
   tmem_wait_ld();
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -1153,7 +1175,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       for (int sp = 0; sp < 6; ++sp) {
         float gre[8], gim[8];
         __syncwarp();
-        fused_load_one(tr, slot * 48 + 8 * sp, gre, gim);
+        fused_load_one<FBN>(tr, slot * 48 + 8 * sp, gre, gim);
         if (nbw > 0) h0[sp] = hrot(u0, gre, gim);
         if (nbw > 1) h1[sp] = hrot(u1, gre, gim);
       }
@@ -1171,7 +1193,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           for (int sp = 0; sp < 6; ++sp) {
             float gre[8], gim[8];
             __syncwarp();
-            fused_load_one(tr, slot * 48 + 8 * sp, gre, gim);
+            fused_load_one<FBN>(tr, slot * 48 + 8 * sp, gre, gim);
             if (mine) hx[sp] = hrot(ux, gre, gim);
           }
           if (mine) {
@@ -1237,33 +1259,330 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   return 0;
 }
 
+// ------------------------------- stage A fused with the initial-band rotation
+// For the same nw = 8, nb = 6 path the stage-A contraction g(k,Rp) = sum_Re
+// e^{2 pi i k.Re}/deg g(Re,Rp) runs fused with the rotation over the initial
+// band and the k-half of the Rp phase, writing the six-plane stage-B state
+// operand directly (the FP32 g(k,Rp) of all window k, 10 GB at 24^3, is never
+// stored).  A tile is 128 window k rows x 128 columns = 16 contraction
+// positions kp x 8 initial bands m' of one (n', s'); a complex product is two
+// MMAs of N = 256 over the six-plane operand, the main and correction
+// accumulators (real | imaginary) filling TMEM columns 0..255 and 256..511.
+// K blocks are 8 wide (32 B rows, 32B swizzle) so that five 40 KB stages fit.
+// Epilogue warp w drains lane quadrant w % 4 for the 8 positions of half
+// (w - 2) / 4: per window state (k, m) of its row it forms
+//   B(state)[n' + 8 s'][kp] = conj(e^{2 pi i k.Rp}) / deg(Rp) sum_m' U_k[m][m'] g(k,Rp)[n', m', s']
+// for the first two states in registers, releases TMEM, and writes 32-byte
+// sectors of the six planes.
+constexpr int A_BK = 8;
+constexpr int A_PLANE = BM * A_BK * 4;          // 4 KB
+constexpr int A_STAGE = 10 * A_PLANE;           // 4 A planes + 6 B planes
+constexpr int A_STAGES = 5;
+constexpr int A_SMEM = A_STAGES * A_STAGE + 1024 + 256;
+
+// SMEM matrix descriptor: K-major, SWIZZLE_32B (atom = 8 rows x 32 B, SBO = 256 B).
+__device__ __forceinline__ uint64_t sdesc32(const void *p) {
+  uint64_t a = smem_u32(p);
+  uint64_t d = (a >> 4) & 0x3FFFull;
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(256 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)6 << 61;
+  return d;
+}
+
+struct FusedAArgs {
+  int mtiles, ntiles, nkb, nkp16;   // nkp16: 16-position blocks of the state operand's K
+  int64_t Astride, Bstride;          // rows between planes: phase operand, stage-A operand
+  int KpB;
+  int64_t Np2;                       // rows per plane of the state operand
+  float *B2;                         // [6][Np2][KpB] output
+  const int *kinvB;                  // Rp cell at each K position (-1: padding)
+  const int *Rq;                     // [nwsq][3]
+  const double *degq;
+  const double2 *roots;              // e^{2 pi i t / L}
+  int L, m0, m1, m2;
+  int *err;
+};
+
+// conj(e^{2 pi i k.Rp}) / deg(Rp) for the lane's k (packed mesh coordinates) at position kp
+__device__ __forceinline__ float2 rp_phase(const FusedAArgs &g, int bpack, int kp) {
+  const int rp = __ldg(g.kinvB + kp);
+  if (rp < 0) return make_float2(0.f, 0.f);
+  const int b1 = bpack & 1023, b2 = (bpack >> 10) & 1023, b3 = bpack >> 20;
+  int64_t t = (int64_t)b1 * __ldg(g.Rq + 3 * rp) * (g.L / g.m0) + (int64_t)b2 * __ldg(g.Rq + 3 * rp + 1) * (g.L / g.m1) +
+              (int64_t)b3 * __ldg(g.Rq + 3 * rp + 2) * (g.L / g.m2);
+  t %= g.L;
+  if (t < 0) t += g.L;
+  const double2 r = __ldg(g.roots + t);
+  const double dg = __ldg(g.degq + rp);
+  return make_float2((float)(r.x / dg), (float)(-r.y / dg));
+}
+
+// write the 8 positions of one state row (32-byte sectors of the six planes)
+__device__ __forceinline__ void write_state8(const FusedAArgs &g, int64_t row, int kp0, const float2 *o,
+                                             const float2 *ph) {
+  float v[6][8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const float xr = ph[r].x * o[r].x - ph[r].y * o[r].y, xi = ph[r].x * o[r].y + ph[r].y * o[r].x;
+    const float hr = tf32_round(xr), hi = tf32_round(xi);
+    const float lr = tf32_round(xr - hr), li = tf32_round(xi - hi);
+    v[0][r] = -hi;
+    v[1][r] = hr;
+    v[2][r] = hi;
+    v[3][r] = -li;
+    v[4][r] = lr;
+    v[5][r] = li;
+  }
+  const int64_t plane = g.Np2 * g.KpB;
+  float *base = g.B2 + row * g.KpB + kp0;
+#pragma unroll
+  for (int pl = 0; pl < 6; ++pl) {
+    float4 *d4 = (float4 *)(base + pl * plane);
+    d4[0] = make_float4(v[pl][0], v[pl][1], v[pl][2], v[pl][3]);
+    d4[1] = make_float4(v[pl][4], v[pl][5], v[pl][6], v[pl][7]);
+  }
+}
+
+// rotation over m' of the 8 loaded columns (one position): sum_m' u[m'] G(m')
+__device__ __forceinline__ float2 mrot(const float2 *u, const float *gre, const float *gim) {
+  float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int mp = 0; mp < 8; ++mp) cfmaf(a, u[mp], make_float2(gre[mp], gim[mp]));
+  return a;
+}
+
+__global__ void __launch_bounds__(F_THREADS, 1)
+    k_stageA_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedAArgs g,
+                     FusedTabs tb) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + A_STAGES * A_STAGE);
+  uint64_t *empty = full + A_STAGES;
+  uint64_t *tfull = empty + A_STAGES;
+  uint64_t *tempty = tfull + 1;
+  uint32_t *tslot = (uint32_t *)(tempty + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < A_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, F_EPI_THREADS);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int ntile = g.mtiles * g.ntiles;
+
+  if (warp == 0) {
+    if (lane == 0) {   // ---- TMA producer
+      uint64_t keep;
+      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+        const int mt = t % g.mtiles, nt = t / g.mtiles;
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
+          uint8_t *sb = smem + stage * A_STAGE;
+          mbar_expect_tx(&full[stage], A_STAGE);
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+            tma_load_2d_hint(sb + p * A_PLANE, &tA, &full[stage], kb * A_BK, (int)(p * g.Astride + mt * BM), keep);
+#pragma unroll
+          for (int p = 0; p < 6; ++p)
+            tma_load_2d(sb + (4 + p) * A_PLANE, &tB, &full[stage], kb * A_BK, (int)(p * g.Bstride + nt * BM));
+          if (++stage == A_STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      for (int s = 0; s < A_STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, g.err), stage = (stage + 1) % A_STAGES,
+                                           phase ^= (stage == 0);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {   // ---- MMA issuer
+      constexpr uint32_t ID2 = idesc_tf32_n(false, 2 * BM);
+      int stage = 0;
+      uint32_t phase = 0;
+      int it = 0;
+      bool ok = true;
+      const uint32_t dm = tmem, dc = tmem + 256;
+      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+        if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < g.nkb; ++kb) {
+          if (!mbar_wait(&full[stage], phase, g.err)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t *sb = smem + stage * A_STAGE;
+          const uint64_t Ahr = sdesc32(sb + 0 * A_PLANE), Ahi = sdesc32(sb + 1 * A_PLANE);
+          const uint64_t Alr = sdesc32(sb + 2 * A_PLANE), Ali = sdesc32(sb + 3 * A_PLANE);
+          const uint64_t BhN = sdesc32(sb + 4 * A_PLANE), BhP = sdesc32(sb + 5 * A_PLANE);
+          const uint64_t BlN = sdesc32(sb + 7 * A_PLANE), BlP = sdesc32(sb + 8 * A_PLANE);
+          const uint32_t acc = kb == 0 ? 0u : 1u;
+          umma(dc, Ahr, BlP, ID2, acc);   // hi x lo
+          umma(dc, Ahi, BlN, ID2, 1);
+          umma(dc, Alr, BhP, ID2, 1);     // lo x hi
+          umma(dc, Ali, BhN, ID2, 1);
+          // the last 16 positions (nearest cells, largest terms) go to the short correction chain
+          const bool nearblk = g.nkb > 2 && kb >= g.nkb - 2;
+          const uint32_t dd = nearblk ? dc : dm;
+          umma(dd, Ahr, BhP, ID2, nearblk ? 1u : acc);   // hi x hi
+          umma(dd, Ahi, BhN, ID2, 1);
+          umma_commit(&empty[stage]);
+          if (++stage == A_STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (ok) umma_commit(tfull);
+      }
+    }
+  } else {   // ---- epilogue: warps 2..9
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
+    int it = 0;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
+      const int mt = t % g.mtiles, nt = t / g.mtiles;
+      const int kpb = nt % g.nkp16, ns = nt / g.nkp16;
+      const int col0 = (ns & 7) + 8 * (ns >> 3);      // n' + 8 s'
+      const int kp0 = kpb * 16 + half * 8;
+      const int ip = mt * BM + quad * 32 + lane;
+      const int4 ri = __ldg(tb.row + ip);             // padding rows: no window band, no state
+      const unsigned wmask = (unsigned)ri.y;
+      const int nbw = __popc(wmask);
+      const int m0b = nbw > 0 ? __ffs(wmask) - 1 : 0;
+      const unsigned rest = wmask & (wmask - 1);
+      const int m1b = nbw > 1 ? __ffs(rest) - 1 : 0;
+      const float4 *ub = tb.U4 + blk32(ip, 32, 0);
+      float2 u0[8], u1[8], ph[8];
+      if (nbw > 0) load_urow(ub, m0b, u0);
+      if (nbw > 1) load_urow(ub, m1b, u1);
+      if (nbw > 0) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) ph[r] = rp_phase(g, ri.w, kp0 + r);
+      }
+      if (!mbar_wait(tfull, it & 1, g.err)) break;
+      tc_fence_after();
+      float2 o0[8], o1[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        float gre[8], gim[8];
+        __syncwarp();
+        fused_load_one<BM>(tr, 8 * (half * 8 + r), gre, gim);
+        if (nbw > 0) o0[r] = mrot(u0, gre, gim);
+        if (nbw > 1) o1[r] = mrot(u1, gre, gim);
+      }
+      // rows with more than two window states (rare): finished while the accumulators are held
+      const int nbmax = __reduce_max_sync(0xffffffffu, nbw);
+      if (nbmax > 2) {
+        unsigned left = rest & (rest - 1);
+        for (int b = 2; b < nbmax; ++b) {
+          const bool mine = b < nbw;
+          const int mb = mine ? __ffs(left) - 1 : 0;
+          if (mine) left &= left - 1;
+          float2 ux[8], ox[8];
+          if (mine) load_urow(ub, mb, ux);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            float gre[8], gim[8];
+            __syncwarp();
+            fused_load_one<BM>(tr, 8 * (half * 8 + r), gre, gim);
+            if (mine) ox[r] = mrot(ux, gre, gim);
+          }
+          if (mine) write_state8(g, (int64_t)(ri.z + b) * 48 + col0, kp0, ox, ph);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(tempty);
+      if (nbw > 0) write_state8(g, (int64_t)ri.z * 48 + col0, kp0, o0, ph);
+      if (nbw > 1) write_state8(g, (int64_t)(ri.z + 1) * 48 + col0, kp0, o1, ph);
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA, int KpA, const FusedTabs &tabs,
+                          FusedAArgs g, cudaStream_t st) {
+  if (MpA % BM || NA % BM || KpA % A_BK || g.KpB % 16) return tfail(1, "stage A: shapes not tile multiples");
+  if (4 * (int64_t)MpA > INT32_MAX || 6 * NA > INT32_MAX) return tfail(1, "stage A: operand too tall for TMA coords");
+  CUtensorMap ta, tb;
+  int rc;
+  if ((rc = make_map(&ta, PA, KpA, 4 * (int64_t)MpA, BM, A_BK)) || (rc = make_map(&tb, GA6, KpA, 6 * NA, BM, A_BK)))
+    return rc;
+  static bool attr = false;
+  if (!attr) {
+    TCK(cudaFuncSetAttribute(k_stageA_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, A_SMEM));
+    attr = true;
+  }
+  g.mtiles = MpA / BM;
+  g.ntiles = (int)(NA / BM);
+  g.nkb = KpA / A_BK;
+  g.nkp16 = g.KpB / 16;
+  g.Astride = MpA;
+  g.Bstride = NA;
+  if ((int64_t)g.nkp16 * 48 != g.ntiles) return tfail(1, "stage A: operand width mismatch");
+  const int64_t tiles = (int64_t)g.mtiles * g.ntiles;
+  if (tiles > INT32_MAX) return tfail(1, "stage A: too many tiles");
+  const int grid = (int)std::min<int64_t>(tiles, num_sms());
+  k_stageA_fused86<<<grid, F_THREADS, A_SMEM, st>>>(ta, tb, g, tabs);
+  TCK(cudaGetLastError());
+  return 0;
+}
+
 // ------------------------------------------------------------ orchestration
 void free_split(SplitOperands &s) {
   if (s.G) cudaFree(s.G);
+  if (s.GA6) cudaFree(s.GA6);
   s.G = nullptr;
+  s.GA6 = nullptr;
 }
 
 static inline int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
-int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk, int nwsq,
-                      int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
-                      const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
-                      const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
-                      const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
-                      int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
-  // k'-row blocks of the rate partials: 16 rows for the nw = 8, nb = 6 epilogue, 128 otherwise
-  // (mesh coordinates are packed in 10 bits each in the fused kernel's tables)
-  const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
-                       mesh[2] <= 1024);
-  // rate partials per state: one per 32-row block of the fused kernel, one per 128 rows otherwise
-  const int nblk = fast86 ? (int)(rup(nwv, BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
-  if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
-  *nblk_used = nblk;
+// fp32 copies of the eigenvectors and the per-(q, s) scalars of the epilogues
+struct EpiTables {
+  float2 *Uf;
+  float *cx, *bs, *w, *v;
+};
+
+static int epi_tables(Workspace &ws, cudaStream_t st, const double2 *U, const RateParams &rp, const EpiData &ed_in,
+                      int64_t *launches, EpiTables *t) {
+  const int N = rp.N, nw = rp.nw, nb = rp.nb;
+  if (wsget(ws, "tc_Uf", (size_t)N * nw * nw, &t->Uf) || wsget(ws, "tc_cx", (size_t)N * nb, &t->cx) ||
+      wsget(ws, "tc_bs", (size_t)N * nb, &t->bs) || wsget(ws, "tc_w", (size_t)N * nb, &t->w) ||
+      wsget(ws, "tc_v", (size_t)N * nb, &t->v))
+    return tfail(6, ws.msg.c_str());
+  k_to_f2<<<(unsigned)(((int64_t)N * nw * nw + 255) / 256), 256, 0, st>>>((int64_t)N * nw * nw, U, t->Uf);
+  k_qtab<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.om, ed_in.bose, rp.sigma, kB * rp.T, rp.const_tp, t->cx,
+                                                t->bs, t->w, t->v);
+  TCK(cudaGetLastError());
+  *launches += 2;
+  return 0;
+}
+
+// Any nw, nb and delta: stage A as chunked GEMMs + rotation into a four-plane
+// state operand, stage B as chunked GEMMs + a separate epilogue.
+static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk,
+                               int nwsq, int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L,
+                               const double2 *roots, const int *widx, const int *st_code,
+                               const std::vector<int> &first_state, const int *Rk, const double *degk,
+                               const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
+                               const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
+                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
   int rc;
-  int *err = nullptr;
-  // the device error word lives in the workspace; the caller checks its own word afterwards
-  if ((rc = wsget(ws, "tc_err", 1, &err))) return tfail(6, ws.msg.c_str());
-  TCK(cudaMemsetAsync(err, 0, sizeof(int), st));
   const int KpA = (int)rup(nwsk, BK), KpB = (int)rup(nwsq, BK);
   const int64_t NpA = rup(Nn, BN);
   // g(Re,Rp) planes, built once per handle
@@ -1280,17 +1599,15 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   const int ncol = nw * nb;
   // stage A in k chunks of kc rows (multiple of BM)
   const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nwv, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
-  // state-operand rows: whole 8-state groups (8 * 48 = 384 rows, a multiple of both tile widths)
-  const int64_t Np2 = fast86 ? rup(nst, 8) * ncol : rup((int64_t)nst * ncol, BN);
-  const int nplB = fast86 ? 6 : 4;   // planes of the state operand
+  const int64_t Np2 = rup((int64_t)nst * ncol, BN);
   float *PA, *CAr, *CAi, *B2;
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
-      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)nplB * Np2 * KpB, &B2)))
+      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)4 * Np2 * KpB, &B2)))
     return tfail(6, ws.msg.c_str());
   // the rotation writes every K position of every state row; zero the padding rows only
   {
     const int64_t used = (int64_t)nst * ncol;
-    for (int pl = 0; pl < nplB; ++pl)
+    for (int pl = 0; pl < 4; ++pl)
       if (Np2 > used)
         TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
   }
@@ -1324,10 +1641,10 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
           rattr = true;
         }
         k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, widx, U, CAr, CAi, NpA, mesh[0], mesh[1],
-                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2, fast86 ? 1 : 0);
+                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
         TCK(cudaGetLastError());
         (*launches)++;
-      } else {   // large nw*nw*nb: one thread per output element (never the six-plane nw = 8 form)
+      } else {   // large nw*nw*nb: one thread per output element
         for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
           int je = std::min(j1, j0 + 32768);
           dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
@@ -1343,16 +1660,15 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   TCK(cudaEventRecord(ev_stage_a, st));
   // stage B: A planes = e^{2 pi i k'.Rp} for the window k'
   const int MpB = (int)rup(nwv, BM);
-  float *PB, *CBr = nullptr, *CBi = nullptr;
+  float *PB, *CBr, *CBi;
   // states per chunk: a multiple of 8 (8 * 48 = 3 * 128 columns) bounded by ~2 GB of output
   int64_t sc = ((int64_t)1 << 31) / ((int64_t)MpB * ncol * 8);
   sc = std::max<int64_t>(8, sc / 8 * 8);
   sc = std::min<int64_t>(sc, rup(nst, 8));
   sc = std::min<int64_t>(sc, 32768);
   const int64_t NpC = rup(sc * ncol, BN);
-  if ((rc = wsget(ws, "tc_PB", (size_t)4 * MpB * KpB, &PB)) ||
-      (!fast86 && ((rc = wsget(ws, "tc_CBr", (size_t)MpB * NpC, &CBr)) ||
-                   (rc = wsget(ws, "tc_CBi", (size_t)MpB * NpC, &CBi)))))
+  if ((rc = wsget(ws, "tc_PB", (size_t)4 * MpB * KpB, &PB)) || (rc = wsget(ws, "tc_CBr", (size_t)MpB * NpC, &CBr)) ||
+      (rc = wsget(ws, "tc_CBi", (size_t)MpB * NpC, &CBi)))
     return tfail(6, ws.msg.c_str());
   TCK(cudaMemsetAsync(PB, 0, (size_t)4 * MpB * KpB * sizeof(float), st));
   {
@@ -1361,48 +1677,12 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                                                                  nullptr, kposB, roots, PB, MpB, KpB);
     TCK(cudaGetLastError());
   }
-  // fp32 copies of the eigenvectors and per-(q,s) tables for the epilogue
-  float2 *Uf;
-  float *cx, *bs, *w, *v;
-  const int N = rp.N;
-  if ((rc = wsget(ws, "tc_Uf", (size_t)N * nw * nw, &Uf)) || (rc = wsget(ws, "tc_cx", (size_t)N * nb, &cx)) ||
-      (rc = wsget(ws, "tc_bs", (size_t)N * nb, &bs)) || (rc = wsget(ws, "tc_w", (size_t)N * nb, &w)) ||
-      (rc = wsget(ws, "tc_v", (size_t)N * nb, &v)))
-    return tfail(6, ws.msg.c_str());
-  k_to_f2<<<(unsigned)(((int64_t)N * nw * nw + 255) / 256), 256, 0, st>>>((int64_t)N * nw * nw, U, Uf);
-  k_qtab<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.om, ed_in.bose, rp.sigma, kB * rp.T, rp.const_tp, cx, bs,
-                                                w, v);
-  TCK(cudaGetLastError());
-  *launches += 3;
+  EpiTables et;
+  if ((rc = epi_tables(ws, st, U, rp, ed_in, launches, &et))) return rc;
   EpiData ed = ed_in;
-  ed.Uf = Uf;
-  QTab qt{cx, bs, w, v};
-  FusedTabs tabs{};
-  if (fast86) {
-    int4 *trow;
-    StateRec *tst;
-    float4 *tU4, *trec;
-    double *tens;
-    if ((rc = wsget(ws, "tc_frow", (size_t)MpB, &trow)) || (rc = wsget(ws, "tc_fst", (size_t)nst, &tst)) ||
-        (rc = wsget(ws, "tc_fU4", (size_t)32 * MpB, &tU4)) || (rc = wsget(ws, "tc_fens", (size_t)8 * MpB, &tens)) ||
-        (rc = wsget(ws, "tc_frec", (size_t)24 * rup(N, 32), &trec)))
-      return tfail(6, ws.msg.c_str());
-    k_fused_rows<<<(MpB + 127) / 128, 128, 0, st>>>(nwv, MpB, widx, ed_in.ens, Uf, ed_in.cum, rp.enref, rp.fsthick,
-                                                    mesh[0], mesh[1], trow, tU4, tens);
-    k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, widx, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
-                                                      mesh[1], tst);
-    k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, cx, bs, w, v, trec);
-    TCK(cudaGetLastError());
-    *launches += 3;
-    tabs = FusedTabs{trow, tst, tU4, tens, trec, MpB, N};
-  }
-  if (fast86) {   // one fused GEMM + epilogue launch over all states
-    tB->begin(st);
-    if ((rc = stageB_fused86(PB, MpB, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st))) return rc;
-    tB->end(st);
-    *launches += 1;
-  }
-  for (int64_t j0 = 0; j0 < nst && !fast86; j0 += sc) {
+  ed.Uf = et.Uf;
+  QTab qt{et.cx, et.bs, et.w, et.v};
+  for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
@@ -1430,13 +1710,154 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
     }
     *launches += 2;
   }
+  return 0;
+}
+
+// The nw = 8, nb = 6 Gaussian-delta path: fused stage A (contraction over Re +
+// initial-band rotation + k-half of the Rp phase, writing the six-plane state
+// operand) and fused stage B (contraction over Rp + rate epilogue).
+static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk,
+                               int nwsq, int64_t Nn, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
+                               const int *widx, const int *st_code, const int *Rk, const double *degk,
+                               const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
+                               const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
+                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+  int rc;
+  const int ncol = 48;
+  const int KpA = (int)rup(nwsk, 16), KpB = (int)rup(nwsq, 16);
+  const int N = rp.N;
+  const int Mp = (int)rup(nwv, BM);                 // window rows (k and k' alike)
+  const int64_t NA = (int64_t)8 * KpB * ncol;       // stage-A columns (m', kp, n', s')
+  // contraction position -> Rp cell
+  int *kinvB;
+  if ((rc = wsget(ws, "tc_kinv", (size_t)KpB, &kinvB))) return tfail(6, ws.msg.c_str());
+  TCK(cudaMemsetAsync(kinvB, 0xFF, (size_t)KpB * sizeof(int), st));
+  k_kinv<<<(nwsq + 255) / 256, 256, 0, st>>>(nwsq, kposB, kinvB);
+  TCK(cudaGetLastError());
+  (*launches)++;
+  // stage-A operand, built once per handle
+  if (!s.GA6 || s.NA != NA || s.KpA6 != KpA) {
+    if (s.GA6) cudaFree(s.GA6);
+    s.GA6 = nullptr;
+    TCK(cudaMalloc(&s.GA6, (size_t)6 * NA * KpA * sizeof(float)));
+    TCK(cudaMemsetAsync(s.GA6, 0, (size_t)6 * NA * KpA * sizeof(float), st));
+    const int64_t ne = NA * nwsk;
+    k_gplanes_a6<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwsk, Nn, G64, kposA, kinvB, KpB, s.GA6, NA, KpA);
+    TCK(cudaGetLastError());
+    s.NA = NA;
+    s.KpA6 = KpA;
+    (*launches)++;
+  }
+  EpiTables et;
+  if ((rc = epi_tables(ws, st, U, rp, ed_in, launches, &et))) return rc;
+  // row, state and q tables of the fused epilogues
+  int4 *trow;
+  StateRec *tst;
+  float4 *tU4, *trec;
+  double *tens;
+  if ((rc = wsget(ws, "tc_frow", (size_t)Mp, &trow)) || (rc = wsget(ws, "tc_fst", (size_t)nst, &tst)) ||
+      (rc = wsget(ws, "tc_fU4", (size_t)32 * Mp, &tU4)) || (rc = wsget(ws, "tc_fens", (size_t)8 * Mp, &tens)) ||
+      (rc = wsget(ws, "tc_frec", (size_t)24 * rup(N, 32), &trec)))
+    return tfail(6, ws.msg.c_str());
+  k_fused_rows<<<(Mp + 127) / 128, 128, 0, st>>>(nwv, Mp, widx, ed_in.ens, et.Uf, ed_in.cum, rp.enref, rp.fsthick,
+                                                 mesh[0], mesh[1], trow, tU4, tens);
+  k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, widx, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
+                                                    mesh[1], tst);
+  k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, et.cx, et.bs, et.w, et.v, trec);
+  TCK(cudaGetLastError());
+  *launches += 3;
+  const FusedTabs tabs{trow, tst, tU4, tens, trec, Mp, N};
+  // state operand: whole 8-state groups (8 x 48 = 384 rows), six planes; padding rows zero
+  const int64_t Np2 = rup(nst, 8) * ncol;
+  float *PA, *PB, *B2;
+  if ((rc = wsget(ws, "tc_PAf", (size_t)4 * Mp * KpA, &PA)) || (rc = wsget(ws, "tc_PB", (size_t)4 * Mp * KpB, &PB)) ||
+      (rc = wsget(ws, "tc_B2", (size_t)6 * Np2 * KpB, &B2)))
+    return tfail(6, ws.msg.c_str());
+  {
+    const int64_t used = (int64_t)nst * ncol;
+    for (int pl = 0; pl < 6; ++pl)
+      if (Np2 > used)
+        TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
+  }
+  // ---- stage A
+  TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
+  {
+    const int64_t ne = (int64_t)nwv * nwsk;
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, widx, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
+                                                                 degk, kposA, roots, PA, Mp, KpA);
+    TCK(cudaGetLastError());
+    (*launches)++;
+  }
+  FusedAArgs ga{};
+  ga.KpB = KpB;
+  ga.Np2 = Np2;
+  ga.B2 = B2;
+  ga.kinvB = kinvB;
+  ga.Rq = Rq;
+  ga.degq = degq;
+  ga.roots = roots;
+  ga.L = L;
+  ga.m0 = mesh[0];
+  ga.m1 = mesh[1];
+  ga.m2 = mesh[2];
+  ga.err = err;
+  tA->begin(st);
+  if ((rc = stageA_fused86(PA, Mp, s.GA6, NA, KpA, tabs, ga, st))) return rc;
+  tA->end(st);
+  (*launches)++;
+  TCK(cudaEventRecord(ev_stage_a, st));
+  // ---- stage B: A planes = e^{2 pi i k'.Rp} for the window k'
+  TCK(cudaMemsetAsync(PB, 0, (size_t)4 * Mp * KpB * sizeof(float), st));
+  {
+    const int64_t ne = (int64_t)nwv * nwsq;
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, widx, mesh[0], mesh[1], mesh[2], L, nwsq, Rq,
+                                                                 nullptr, kposB, roots, PB, Mp, KpB);
+    TCK(cudaGetLastError());
+    (*launches)++;
+  }
+  EpiData ed = ed_in;
+  ed.Uf = et.Uf;
+  tB->begin(st);
+  if ((rc = stageB_fused86(PB, Mp, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st))) return rc;
+  tB->end(st);
+  (*launches)++;
+  return 0;
+}
+
+int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk, int nwsq,
+                      int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
+                      const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
+                      const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
+                      const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
+                      int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+  // The fused path packs mesh coordinates in 10 bits each.
+  const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
+                       mesh[2] <= 1024);
+  // rate partials per state: one per 32-row block of the fused kernel, one per 128 k' rows otherwise
+  const int nblk = fast86 ? (int)(rup(nwv, BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
+  if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
+  *nblk_used = nblk;
+  int rc;
+  int *err = nullptr;
+  // the device error word lives in the workspace; the caller checks its own word afterwards
+  if ((rc = wsget(ws, "tc_err", 1, &err))) return tfail(6, ws.msg.c_str());
+  TCK(cudaMemsetAsync(err, 0, sizeof(int), st));
+  if (fast86) {
+    if ((rc = split_rates_fused86(s, ws, st, G64, nwsk, nwsq, Nn, nwv, nst, mesh, L, roots, widx, st_code, Rk, degk,
+                                  kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err, ev_stage_a, launches, tA,
+                                  tB)))
+      return rc;
+  } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, st_code,
+                                       first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err,
+                                       ev_stage_a, launches, tA, tB))) {
+    return rc;
+  }
   int herr = 0;
   TCK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
   if (herr & DERR_TIMEOUT) return tfail(7, "tcgen05 GEMM: a bounded mbarrier wait gave up");
   return 0;
 }
-
 }  // namespace tc
 }  // namespace ephg
 

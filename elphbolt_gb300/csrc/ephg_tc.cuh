@@ -12,17 +12,21 @@ namespace tc {
 struct SplitOperands {
   float *G = nullptr;      // g(Re,Rp) as K-major TF32 planes [4][Nn][Kpad]: hi_r, hi_i, lo_r, lo_i
   int64_t Nn = 0;
-  int Kp = 0;       // padded K (WS cells)
+  int Kp = 0;              // padded K (WS cells)
+  float *GA6 = nullptr;    // the fused nw = 8, nb = 6 path's stage-A operand: six planes [6][NA][KpA6]
+  int64_t NA = 0;
+  int KpA6 = 0;
 };
 
 void free_split(SplitOperands &s);
 const char *last_error();
 
-// Stage A + B + C of the rate pipeline in the split form.  The rate partials
-// [state][k'-block] use up to nblk_max k' blocks; *nblk_used returns the count.  kposA / kposB give
-// the contraction position of each Re / Rp cell (cells ordered far to near).: fills the rate
-// partials [state][k'-block] like the FP64 path.  Records ev_stage_a after
-// stage A.  Returns 0 or an EPHG_ERR_* code (message in last_error()).
+// Stage A + B + C of the rate pipeline in the split form: fills the rate
+// partials [state][k'-block] like the FP64 path, using up to nblk_max k'
+// blocks (*nblk_used returns the count).  kposA / kposB give the contraction
+// position of each Re / Rp cell (cells ordered far to near).  Records
+// ev_stage_a after stage A.  Returns 0 or an EPHG_ERR_* code (message in
+// last_error()).
 int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64,
                       int nwsk, int nwsq, int64_t Nn, int nw, int nb, int nwv, int nst,
                       const int mesh[3], int L, const double2 *roots, const int *widx,
