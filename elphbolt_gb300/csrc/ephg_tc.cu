@@ -1297,26 +1297,25 @@ struct FusedAArgs {
   int KpB;
   int64_t Np2;                       // rows per plane of the state operand
   float *B2;                         // [6][Np2][KpB] output
-  const int *kinvB;                  // Rp cell at each K position (-1: padding)
-  const int *Rq;                     // [nwsq][3]
-  const double *degq;
-  const double2 *roots;              // e^{2 pi i t / L}
-  int L, m0, m1, m2;
+  const float2 *phk;                 // conj(e^{2 pi i k.Rp}) / deg(Rp): row-blocked, fields kp (0 at padding)
   int *err;
 };
 
-// conj(e^{2 pi i k.Rp}) / deg(Rp) for the lane's k (packed mesh coordinates) at position kp
-__device__ __forceinline__ float2 rp_phase(const FusedAArgs &g, int bpack, int kp) {
-  const int rp = __ldg(g.kinvB + kp);
-  if (rp < 0) return make_float2(0.f, 0.f);
-  const int b1 = bpack & 1023, b2 = (bpack >> 10) & 1023, b3 = bpack >> 20;
-  int64_t t = (int64_t)b1 * __ldg(g.Rq + 3 * rp) * (g.L / g.m0) + (int64_t)b2 * __ldg(g.Rq + 3 * rp + 1) * (g.L / g.m1) +
-              (int64_t)b3 * __ldg(g.Rq + 3 * rp + 2) * (g.L / g.m2);
-  t %= g.L;
-  if (t < 0) t += g.L;
-  const double2 r = __ldg(g.roots + t);
-  const double dg = __ldg(g.degq + rp);
-  return make_float2((float)(r.x / dg), (float)(-r.y / dg));
+// conj(e^{2 pi i k.Rp}) / deg(Rp) for window row ip and contraction position kp,
+// stored row-blocked by 32 (field kp): built once per request (its FP64
+// divisions kept out of the GEMM epilogue), read coalesced.
+__global__ void k_phase_k_table(int nwv, int Mp, int KpB, const int *widx, const int *kinvB, int m0, int m1, int m2,
+                                int L, const int *Rq, const double *degq, const double2 *roots, float2 *phk) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)Mp * KpB) return;
+  const int ip = (int)(idx / KpB), kp = (int)(idx % KpB);
+  const int rp = kinvB[kp];
+  float2 v = make_float2(0.f, 0.f);
+  if (ip < nwv && rp >= 0) {
+    const double2 r = roots[phase_idx(widx[ip], m0, m1, m2, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
+    v = make_float2((float)(r.x / degq[rp]), (float)(-r.y / degq[rp]));
+  }
+  phk[blk32(ip, KpB, kp)] = v;
 }
 
 // write the 8 positions of one state row (32-byte sectors of the six planes)
@@ -1467,8 +1466,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       if (nbw > 0) load_urow(ub, m0b, u0);
       if (nbw > 1) load_urow(ub, m1b, u1);
       if (nbw > 0) {
+        const float2 *pk = g.phk + blk32(ip, g.KpB, kp0);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) ph[r] = rp_phase(g, ri.w, kp0 + r);
+        for (int r = 0; r < 8; ++r) ph[r] = __ldg(pk + 32 * r);
       }
       if (!mbar_wait(tfull, it & 1, g.err)) break;
       tc_fence_after();
@@ -1788,18 +1788,20 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
     TCK(cudaGetLastError());
     (*launches)++;
   }
+  float2 *phk;
+  if ((rc = wsget(ws, "tc_phk", (size_t)Mp * KpB, &phk))) return tfail(6, ws.msg.c_str());
+  {
+    const int64_t ne = (int64_t)Mp * KpB;
+    k_phase_k_table<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, Mp, KpB, widx, kinvB, mesh[0], mesh[1], mesh[2],
+                                                                  L, Rq, degq, roots, phk);
+    TCK(cudaGetLastError());
+    (*launches)++;
+  }
   FusedAArgs ga{};
   ga.KpB = KpB;
   ga.Np2 = Np2;
   ga.B2 = B2;
-  ga.kinvB = kinvB;
-  ga.Rq = Rq;
-  ga.degq = degq;
-  ga.roots = roots;
-  ga.L = L;
-  ga.m0 = mesh[0];
-  ga.m1 = mesh[1];
-  ga.m2 = mesh[2];
+  ga.phk = phk;
   ga.err = err;
   tA->begin(st);
   if ((rc = stageA_fused86(PA, Mp, s.GA6, NA, KpA, tabs, ga, st))) return rc;
