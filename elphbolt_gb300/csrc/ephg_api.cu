@@ -754,7 +754,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     ed.cap = vcap;
   }
   int nblk = (nwv + 127) / 128;                 // k'-row blocks of the rate partials
-  const int nblk_max = std::max((nwv + 15) / 16, (nwv + 127) / 128 * 4);
+  const int nblk_max = std::max((nwv + 15) / 16, (nwv + 255) / 256 * 8);
   double *partial;
   if ((rc = wsget(h->ws, "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAIL(rc);
   if (!split) {

@@ -167,6 +167,37 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
                : "memory");
 }
 
+// ---- 2-CTA cluster helpers (operand tiles multicast to both CTAs of a pair)
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// TMA load written to the same shared-memory offset of every CTA in mask, each
+// CTA's mbarrier at the offset of bar receiving the bytes it got
+__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%3, "
+      "%4}], [%2], %5;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "h"(mask)
+      : "memory");
+}
+
+// commit: arrive on the mbarrier at bar's offset in every CTA of mask when the MMAs retire
+__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   uint32_t r[16];
   asm volatile(
@@ -1364,10 +1395,14 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   uint32_t *tslot = (uint32_t *)(tempty + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  // CTA pairs (clusters of 2) take m-tiles 2x, 2x + 1 of the same n-tile: each
+  // loads its own phase tile and multicasts three of the six operand planes to
+  // both; a stage is refilled once both CTAs' MMAs have read it.
+  const uint32_t crank = cluster_rank();
   if (threadIdx.x == 0) {
     for (int s = 0; s < A_STAGES; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], 2);
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, F_EPI_THREADS);
@@ -1381,9 +1416,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   __syncthreads();
+  cluster_sync();   // the peer's barriers are initialised before any multicast or remote arrive
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int ntile = g.mtiles * g.ntiles;
+  const int mpairs = g.mtiles >> 1;
+  const int ntile = mpairs * g.ntiles;           // tile pairs
+  const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
 
   if (warp == 0) {
     if (lane == 0) {   // ---- TMA producer
@@ -1392,8 +1430,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
-        const int mt = t % g.mtiles, nt = t / g.mtiles;
+      for (int t = cid; t < ntile && ok; t += ncl) {
+        const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
           uint8_t *sb = smem + stage * A_STAGE;
@@ -1402,8 +1440,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           for (int p = 0; p < 4; ++p)
             tma_load_2d_hint(sb + p * A_PLANE, &tA, &full[stage], kb * A_BK, (int)(p * g.Astride + mt * BM), keep);
 #pragma unroll
-          for (int p = 0; p < 6; ++p)
-            tma_load_2d(sb + (4 + p) * A_PLANE, &tB, &full[stage], kb * A_BK, (int)(p * g.Bstride + nt * BM));
+          for (int p = 3 * (int)crank; p < 3 * (int)crank + 3; ++p)
+            tma_load_2d_mc(sb + (4 + p) * A_PLANE, &tB, &full[stage], kb * A_BK, (int)(p * g.Bstride + nt * BM),
+                           (uint16_t)3);
           if (++stage == A_STAGES) { stage = 0; phase ^= 1; }
         }
       }
@@ -1418,7 +1457,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t dm = tmem, dc = tmem + 256;
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+      for (int t = cid; t < ntile && ok; t += ncl, ++it) {
         if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < g.nkb; ++kb) {
@@ -1439,7 +1478,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const uint32_t dd = nearblk ? dc : dm;
           umma(dd, Ahr, BhP, ID2, nearblk ? 1u : acc);   // hi x hi
           umma(dd, Ahi, BhN, ID2, 1);
-          umma_commit(&empty[stage]);
+          umma_commit_mc(&empty[stage], (uint16_t)3);
           if (++stage == A_STAGES) { stage = 0; phase ^= 1; }
         }
         if (ok) umma_commit(tfull);
@@ -1449,8 +1488,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const int quad = warp & 3, half = (warp - 2) >> 2;
     const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
     int it = 0;
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
-      const int mt = t % g.mtiles, nt = t / g.mtiles;
+    for (int t = cid; t < ntile; t += ncl, ++it) {
+      const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
       const int kpb = nt % g.nkp16, ns = nt / g.nkp16;
       const int col0 = (ns & 7) + 8 * (ns >> 3);      // n' + 8 s'
       const int kp0 = kpb * 16 + half * 8;
@@ -1512,6 +1551,32 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+  cluster_sync();   // no CTA leaves while its peer may still arrive on its barriers
+}
+
+// Launch a persistent kernel as clusters of 2 CTAs: as many pairs as can be
+// resident at once (at most one CTA per SM), at most `pairs`.
+template <class F>
+static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_t st, F launch) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(F_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(2 * std::max<int64_t>(1, std::min<int64_t>(pairs, num_sms() / 2))));
+  int ncl = 0;
+  TCK(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
+  if (ncl <= 0) return tfail(2, "no 2-CTA cluster fits on the device");
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(pairs, ncl)));
+  TCK(launch(cfg));
+  TCK(cudaGetLastError());
+  return 0;
 }
 
 static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA, int KpA, const FusedTabs &tabs,
@@ -1534,12 +1599,12 @@ static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA
   g.Astride = MpA;
   g.Bstride = NA;
   if ((int64_t)g.nkp16 * 48 != g.ntiles) return tfail(1, "stage A: operand width mismatch");
-  const int64_t tiles = (int64_t)g.mtiles * g.ntiles;
-  if (tiles > INT32_MAX) return tfail(1, "stage A: too many tiles");
-  const int grid = (int)std::min<int64_t>(tiles, num_sms());
-  k_stageA_fused86<<<grid, F_THREADS, A_SMEM, st>>>(ta, tb, g, tabs);
-  TCK(cudaGetLastError());
-  return 0;
+  if (g.mtiles % 2) return tfail(1, "stage A: row tiles must pair");
+  const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
+  if (pairs > INT32_MAX) return tfail(1, "stage A: too many tiles");
+  return launch_pairs((const void *)k_stageA_fused86, A_SMEM, pairs, st, [&](cudaLaunchConfig_t &cfg) {
+    return cudaLaunchKernelEx(&cfg, k_stageA_fused86, ta, tb, g, tabs);
+  });
 }
 
 // ------------------------------------------------------------ orchestration
@@ -1726,7 +1791,7 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   const int ncol = 48;
   const int KpA = (int)rup(nwsk, 16), KpB = (int)rup(nwsq, 16);
   const int N = rp.N;
-  const int Mp = (int)rup(nwv, BM);                 // window rows (k and k' alike)
+  const int Mp = (int)rup(nwv, 2 * BM);             // window rows (k and k' alike), whole tile pairs
   const int64_t NA = (int64_t)8 * KpB * ncol;       // stage-A columns (m', kp, n', s')
   // contraction position -> Rp cell
   int *kinvB;
@@ -1836,7 +1901,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
                        mesh[2] <= 1024);
   // rate partials per state: one per 32-row block of the fused kernel, one per 128 k' rows otherwise
-  const int nblk = fast86 ? (int)(rup(nwv, BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
+  const int nblk = fast86 ? (int)(rup(nwv, 2 * BM) / 32) : (nwv + EPI_ROWS - 1) / EPI_ROWS;
   if (nblk > nblk_max) return tfail(1, "rate partial buffer too small");
   *nblk_used = nblk;
   int rc;
