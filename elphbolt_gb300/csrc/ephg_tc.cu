@@ -1070,10 +1070,14 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   uint32_t *tslot = (uint32_t *)(tempty + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  // CTA pairs (clusters of 2) take m-tiles 2x, 2x + 1 of the same state pair:
+  // each loads its own phase tile and multicasts three of the six state-operand
+  // planes to both; a stage is refilled once both CTAs' MMAs have read it.
+  const uint32_t crank = cluster_rank();
   if (threadIdx.x == 0) {
     for (int s = 0; s < F_STAGES; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], 2);
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, F_EPI_THREADS);
@@ -1087,9 +1091,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   __syncthreads();
+  cluster_sync();   // the peer's barriers are initialised before any multicast or remote arrive
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int ntile = g.mtiles * g.ntiles;
+  const int mpairs = g.mtiles >> 1;
+  const int ntile = mpairs * g.ntiles;           // tile pairs
+  const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
 
   if (warp == 0) {
     if (lane == 0) {   // ---- TMA producer
@@ -1098,8 +1105,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
-        const int mt = t % g.mtiles, nt = t / g.mtiles;
+      for (int t = cid; t < ntile && ok; t += ncl) {
+        const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
           uint8_t *sb = smem + stage * F_STAGE;
@@ -1108,9 +1115,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           for (int p = 0; p < 4; ++p)
             tma_load_2d_hint(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + mt * BM), keep);
 #pragma unroll
-          for (int p = 0; p < 6; ++p)
-            tma_load_2d(sb + 4 * PLANE_BYTES + p * F_BPLANE, &tB, &full[stage], kb * BK,
-                        (int)(p * g.Bstride + nt * FBN));
+          for (int p = 3 * (int)crank; p < 3 * (int)crank + 3; ++p)
+            tma_load_2d_mc(sb + 4 * PLANE_BYTES + p * F_BPLANE, &tB, &full[stage], kb * BK,
+                           (int)(p * g.Bstride + nt * FBN), (uint16_t)3);
           if (++stage == F_STAGES) { stage = 0; phase ^= 1; }
         }
       }
@@ -1128,7 +1135,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t dm = tmem, dc = tmem + 256;   // main, correction (re | im each)
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+      for (int t = cid; t < ntile && ok; t += ncl, ++it) {
         if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < g.nkb; ++kb) {
@@ -1153,7 +1160,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
             umma(dd, Ahr, BhP, ID2, nearblk ? 1u : acc);   // hi x hi
             umma(dd, Ahi, BhN, ID2, 1);
           }
-          umma_commit(&empty[stage]);
+          umma_commit_mc(&empty[stage], (uint16_t)3);
           if (++stage == F_STAGES) { stage = 0; phase ^= 1; }
         }
         if (ok) umma_commit(tfull);
@@ -1166,8 +1173,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
     const int m0 = rp.mesh[0], m1 = rp.mesh[1], m2 = rp.mesh[2];
     int it = 0;
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
-      const int mt = t % g.mtiles, nt = t / g.mtiles;
+    for (int t = cid; t < ntile; t += ncl, ++it) {
+      const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
       // ---- row and state data, before the accumulators are ready
       const int ip = mt * BM + quad * 32 + lane;      // < MpB
       const int j = nt * 2 + slot;                    // warp-uniform
@@ -1255,6 +1262,32 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+  cluster_sync();   // no CTA leaves while its peer may still arrive on its barriers
+}
+
+// Launch a persistent kernel as clusters of 2 CTAs: as many pairs as can be
+// resident at once (at most one CTA per SM), at most `pairs`.
+template <class F>
+static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_t st, F launch) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(F_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(2 * std::max<int64_t>(1, std::min<int64_t>(pairs, num_sms() / 2))));
+  int ncl = 0;
+  TCK(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
+  if (ncl <= 0) return tfail(2, "no 2-CTA cluster fits on the device");
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(pairs, ncl)));
+  TCK(launch(cfg));
+  TCK(cudaGetLastError());
+  return 0;
 }
 
 static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2, int KpB, int nwv, int nst,
@@ -1282,12 +1315,12 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   g.partial = partial;
   g.nblk = nblk;
   if ((int64_t)g.ntiles * FBN > Np2) return tfail(1, "stage B: state operand too short");
-  const int64_t tiles = (int64_t)g.mtiles * g.ntiles;
-  if (tiles > INT32_MAX) return tfail(1, "stage B: too many tiles");
-  const int grid = (int)std::min<int64_t>(tiles, num_sms());
-  k_stageB_fused86<<<grid, F_THREADS, F_SMEM, st>>>(ta, tb, g, tabs, rp, ed);
-  TCK(cudaGetLastError());
-  return 0;
+  if (g.mtiles % 2) return tfail(1, "stage B: row tiles must pair");
+  const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
+  if (pairs > INT32_MAX) return tfail(1, "stage B: too many tiles");
+  return launch_pairs((const void *)k_stageB_fused86, F_SMEM, pairs, st, [&](cudaLaunchConfig_t &cfg) {
+    return cudaLaunchKernelEx(&cfg, k_stageB_fused86, ta, tb, g, tabs, rp, ed);
+  });
 }
 
 // ------------------------------- stage A fused with the initial-band rotation
@@ -1552,31 +1585,6 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
   cluster_sync();   // no CTA leaves while its peer may still arrive on its barriers
-}
-
-// Launch a persistent kernel as clusters of 2 CTAs: as many pairs as can be
-// resident at once (at most one CTA per SM), at most `pairs`.
-template <class F>
-static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_t st, F launch) {
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = 2;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(F_THREADS);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cfg.gridDim = dim3((unsigned)(2 * std::max<int64_t>(1, std::min<int64_t>(pairs, num_sms() / 2))));
-  int ncl = 0;
-  TCK(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
-  if (ncl <= 0) return tfail(2, "no 2-CTA cluster fits on the device");
-  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(pairs, ncl)));
-  TCK(launch(cfg));
-  TCK(cudaGetLastError());
-  return 0;
 }
 
 static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA, int KpA, const FusedTabs &tabs,
