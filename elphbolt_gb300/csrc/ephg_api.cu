@@ -141,7 +141,7 @@ int ephg_device_count(void) {
 int ephg_destroy(ephg_handle *h) {
   if (!h) return EPHG_OK;
   void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->graw, h->G64,
-                  h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_den,
+                  h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_rden,
                   h->rcartq, h->D, h->err, h->kposk, h->kposq};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -234,7 +234,7 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
   // phonon terms: for each atom pair and WS cell, the shortest wraps
   {
     std::vector<int> pair_off(h->nat * h->nat + 1, 0), ent_iuc, ent_woff(1, 0), wrapR;
-    std::vector<double> ent_den;
+    std::vector<double> ent_rden;
     for (int jat = 0; jat < h->nat; ++jat)
       for (int iat = 0; iat < h->nat; ++iat) {
         int pair = iat + h->nat * jat;
@@ -247,7 +247,7 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
           std::vector<int> w = ws_wrap(h->lattvecs, dist, 1.0e-6);
           int nwrap = (int)w.size() / 3;
           ent_iuc.push_back(iuc);
-          ent_den.push_back((double)(d->phwsdeg[iuc] * nwrap));
+          ent_rden.push_back(1.0 / (double)(d->phwsdeg[iuc] * nwrap));
           for (int iw = 0; iw < nwrap; ++iw)
             for (int c = 0; c < 3; ++c) wrapR.push_back(rq[3 * iuc + c] + w[3 * iw + c] * h->cq[c]);
           ent_woff.push_back((int)wrapR.size() / 3);
@@ -274,7 +274,7 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
         (rc = upload(&h->ent_iuc, ent_iuc.data(), ent_iuc.size(), h->st)) ||
         (rc = upload(&h->ent_woff, ent_woff.data(), ent_woff.size(), h->st)) ||
         (rc = upload(&h->wrapR, wrapR.data(), wrapR.size(), h->st)) ||
-        (rc = upload(&h->ent_den, ent_den.data(), ent_den.size(), h->st)) ||
+        (rc = upload(&h->ent_rden, ent_rden.data(), ent_rden.size(), h->st)) ||
         (rc = upload(&h->rcartq, rcq.data(), rcq.size(), h->st)) ||
         (rc = upload(&h->D, (const double2 *)d->Dphwann, (size_t)nwsq * nb * nb, h->st)))
       return bail(rc);
@@ -283,7 +283,7 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
     h->terms.ent_iuc = h->ent_iuc;
     h->terms.ent_woff = h->ent_woff;
     h->terms.wrapR = h->wrapR;
-    h->terms.ent_den = h->ent_den;
+    h->terms.ent_rden = h->ent_rden;
     h->terms.D = h->D;
     h->terms.rcart = h->rcartq;
     h->terms.masses = h->masses;

@@ -26,7 +26,7 @@ struct ephg_handle {
   double *masses = nullptr;
   // phonon wrap terms
   int *pair_off = nullptr, *ent_iuc = nullptr, *ent_woff = nullptr, *wrapR = nullptr;
-  double *ent_den = nullptr, *rcartq = nullptr;
+  double *ent_rden = nullptr, *rcartq = nullptr;
   double2 *D = nullptr;
   ephg::PhTerms terms;
   int *kposk = nullptr, *kposq = nullptr;   // split-form contraction order (far cells first)

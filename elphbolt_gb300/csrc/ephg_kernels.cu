@@ -211,15 +211,39 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
         int p = min(a, b), q = max(a, b);
         double c = 1.0, s = 0.0, phx = 1.0, phy = 0.0;
         if (q < n) {
-          double2 apq = sA[p + n * q];
-          double rr = hypot(apq.x, apq.y);
-          if (rr > 1e-300) {
-            phx = apq.x / rr; phy = apq.y / rr;
-            double app = sA[p + n * p].x, aqq = sA[q + n * q].x;
-            double tau = (aqq - app) / (2.0 * rr);
-            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
+          // The rotation angle is computed in FP32 on operands scaled by the
+          // power of two of a_pq (GB300's FP64 divide / sqrt are slow); the
+          // rotation is then made unitary to FP64 rounding, so it is an exact
+          // similarity transform that leaves a_pq ~ 1e-7 of its value.  Later
+          // rotations remove that residual; a_pq is not forced to zero.  With
+          // |a_qq - a_pp| > 1e30 |a_pq| the rotation is negligible and skipped.
+          const double2 apq = sA[p + n * q];
+          const double d = sA[q + n * q].x - sA[p + n * p].x;
+          const double mx = fmax(fabs(apq.x), fabs(apq.y));
+          const int ex = ((__double2hiint(mx) >> 20) & 0x7ff) - 1023;
+          if (mx > 0.0 && ex > -1000 && ex < 1000) {
+            const double sc = __hiloint2double((1023 - ex) << 20, 0);   // 2^-ex: max |a_pq| -> [1, 2)
+            const float ax = (float)(apq.x * sc), ay = (float)(apq.y * sc);
+            const double dsc = d * sc;
+            const float rr = sqrtf(ax * ax + ay * ay);
+            if (fabs(dsc) <= 1e30) {
+              const float tau = (float)dsc / (2.f * rr);
+              const float tf = fabsf(tau) > 1e18f ? 0.5f / tau
+                                                  : (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+              double px = (double)(ax / rr), py = (double)(ay / rr);
+              double cc = (double)rsqrtf(1.f + tf * tf);
+              double ss = (double)tf * cc;
+              // two Newton steps of 1/sqrt(r2) from 1: |ph| = 1 and c^2 + s^2 = 1 in FP64
+              double r2 = px * px + py * py, f = 1.5 - 0.5 * r2;
+              f = f * (1.5 - 0.5 * r2 * f * f);
+              phx = px * f;
+              phy = py * f;
+              r2 = cc * cc + ss * ss;
+              f = 1.5 - 0.5 * r2;
+              f = f * (1.5 - 0.5 * r2 * f * f);
+              c = cc * f;
+              s = ss * f;
+            }
           }
         }
         sP[3 * lane] = make_double2(c, s);
@@ -263,9 +287,7 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
         int q = (int)sP[3 * lane + 2].y;
         if (q >= 0) {
           int p = (int)sP[3 * lane + 2].x;
-          sA[p + n * q] = make_double2(0.0, 0.0);
-          sA[q + n * p] = make_double2(0.0, 0.0);
-          sA[p + n * p].y = 0.0;
+          sA[p + n * p].y = 0.0;   // the diagonal of a Hermitian matrix is real
           sA[q + n * q].y = 0.0;
         }
       }
@@ -357,6 +379,9 @@ __global__ void __launch_bounds__(128) k_dbuild(int nq, const int *qp, int m1, i
   const int ne = nb * nb;
   // each thread owns up to DB_U matrix elements (nb <= 32 gives <= 1024 elements)
   constexpr int DB_U = 8;
+  // without velocities and for nb^2 <= blockDim / 2, the cells of each chunk are
+  // split over nsl thread slices per element; the slices are added in order at the end
+  const int nsl = (!with_vel && 2 * ne <= (int)blockDim.x) ? (int)blockDim.x / ne : 1;
   double2 acc[DB_U], dacc[DB_U][3];
   for (int u = 0; u < DB_U; ++u) {
     acc[u] = make_double2(0.0, 0.0);
@@ -383,10 +408,28 @@ __global__ void __launch_bounds__(128) k_dbuild(int nq, const int *qp, int m1, i
         cs.x += ph.x;
         cs.y += ph.y;
       }
-      const double den = t.ent_den[en];
-      dsm[pair * DB_CHUNK + (iuc - c0)] = make_double2(cs.x / den, cs.y / den);
+      const double rden = t.ent_rden[en];
+      dsm[pair * DB_CHUNK + (iuc - c0)] = make_double2(cs.x * rden, cs.y * rden);
     }
     __syncthreads();
+    if (nsl > 1) {   // small nb: thread = (element, slice of the chunk's cells), 4-FMA complex MACs
+      if (threadIdx.x < nsl * ne) {
+        const int e = threadIdx.x % ne, sl = threadIdx.x / ne;
+        const int a = e % nb, b = e / nb;
+        const int pair = (a / 3) + t.nat * (b / 3);
+        const double2 *Dp = t.D + (int64_t)nwsq * (a + (int64_t)nb * b);
+        double ar = acc[0].x, ai = acc[0].y;
+        for (int k = sl; k < nc; k += nsl) {
+          const double2 ph = dsm[pair * DB_CHUNK + k], dv = Dp[c0 + k];
+          ar = fma(ph.x, dv.x, ar);
+          ar = fma(-ph.y, dv.y, ar);
+          ai = fma(ph.x, dv.y, ai);
+          ai = fma(ph.y, dv.x, ai);
+        }
+        acc[0] = make_double2(ar, ai);
+      }
+      continue;
+    }
 #pragma unroll
     for (int u = 0; u < DB_U; ++u) {
       const int e = threadIdx.x + u * blockDim.x;
@@ -405,6 +448,20 @@ __global__ void __launch_bounds__(128) k_dbuild(int nq, const int *qp, int m1, i
       }
     }
   }
+  if (nsl > 1) {
+    __syncthreads();
+    double2 *part = dsm;   // [nsl][ne] slice sums (nsl * ne <= blockDim = 128 entries)
+    if (threadIdx.x < nsl * ne) part[threadIdx.x] = acc[0];
+    __syncthreads();
+    if (threadIdx.x < ne) {
+      const int e = threadIdx.x, a = e % nb, b = e / nb;
+      double2 sum = part[e];
+      for (int sl = 1; sl < nsl; ++sl) sum = cadd(sum, part[sl * ne + e]);
+      const double massnorm = 1.0 / sqrt(t.masses[a / 3] * t.masses[b / 3]) * Ryd2amu;
+      Dq[(size_t)q * ne + e] = cscale(sum, massnorm);
+    }
+    return;
+  }
 #pragma unroll
   for (int u = 0; u < DB_U; ++u) {
     const int e = threadIdx.x + u * blockDim.x;
@@ -421,7 +478,8 @@ void launch_dbuild(int nq, const int *qp, const int mesh[3], int L, const double
                    const double *qv, const PhTerms &t, int with_vel, double2 *Dq, double2 *dDq,
                    cudaStream_t st) {
   if (nq <= 0) return;
-  const size_t smem = (size_t)t.npair * DB_CHUNK * sizeof(double2);
+  // phase sums [npair][DB_CHUNK], reused for the slice sums (<= 128 entries)
+  const size_t smem = (size_t)std::max(t.npair * DB_CHUNK, 128) * sizeof(double2);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_dbuild, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);

@@ -38,7 +38,7 @@ struct PhTerms {
   const int *ent_iuc;   // entry -> WS cell
   const int *ent_woff;  // entry -> first wrap vector (wrap list offsets, nent+1)
   const int *wrapR;     // wrap vectors R + w*N_c, 3 ints each
-  const double *ent_den;// phwsdeg * nwrap
+  const double *ent_rden;// 1 / (phwsdeg * nwrap)
   const double2 *D;     // (nwsq, nb, nb) column-major
   const double *rcart;  // (nwsq, 3) lattvecs @ R, nm
   const double *masses; // per atom
