@@ -88,7 +88,9 @@ void launch_phase_frac(int nrows, const double *kv, int nR, const int *R, const 
 // ============================================================ FP64 GEMM
 // C[M][N] = A[M][K] * B[K][N], complex double, row-major.  64x64 tile per
 // 256-thread block, 4x4 complex outputs per thread; FP64-FMA bound on GB300.
-constexpr int ZBM = 64, ZBN = 64, ZBK = 8;
+// 32-row tiles: the H(k) assembly (N = 64 columns) then spreads over ~3 waves of
+// the 152 SMs instead of 1.4, which an FP64-bound kernel pays for in full.
+constexpr int ZBM = 32, ZBN = 64, ZBK = 8, ZRM = ZBM / 16;
 
 __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, const double2 *__restrict__ A,
                                                int64_t lda, const double2 *__restrict__ B,
@@ -97,19 +99,19 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, const double
   __shared__ double2 sB[ZBK][ZBN];
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
   const int64_t m0 = (int64_t)blockIdx.y * ZBM, n0 = (int64_t)blockIdx.x * ZBN;
-  double2 acc[4][4];
+  double2 acc[ZRM][4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < ZRM; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
   for (int k0 = 0; k0 < K; k0 += ZBK) {
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      int idx = t + 256 * r;
+    for (int idx = t; idx < ZBM * ZBK; idx += 256) {
       int row = idx / ZBK, kk = idx % ZBK;
       int64_t gm = m0 + row;
       int gk = k0 + kk;
       sA[kk][row] = (gm < M && gk < K) ? A[gm * lda + gk] : make_double2(0.0, 0.0);
+    }
+    for (int idx = t; idx < ZBK * ZBN; idx += 256) {
       int kb = idx / ZBN, col = idx % ZBN;
       int64_t gn = n0 + col;
       int gkb = k0 + kb;
@@ -118,20 +120,20 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, const double
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < ZBK; ++kk) {
-      double2 a[4], b[4];
+      double2 a[ZRM], b[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty + 16 * i];
+      for (int i = 0; i < ZRM; ++i) a[i] = sA[kk][ty + 16 * i];
 #pragma unroll
       for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < ZRM; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < ZRM; ++i) {
     int64_t gm = m0 + ty + 16 * i;
     if (gm >= M) continue;
 #pragma unroll
