@@ -32,7 +32,10 @@ c_dp = ct.POINTER(ct.c_double)
 # every symbol include/ephg.h declares
 EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count", "ephg_el_wann",
            "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates",
-           "ephg_el_wann_noalloc"]
+           "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
+           "ephg_server_stats_get", "ephg_el_wann_noalloc"]
+
+TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
 
 
 class EphgError(RuntimeError):
@@ -70,6 +73,16 @@ class RateStats(ct.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerStats(ct.Structure):
+    _fields_ = [("submitted", ct.c_int64), ("completed", ct.c_int64), ("failed", ct.c_int64),
+                ("rejected", ct.c_int64), ("vertices", ct.c_int64), ("p50_ms", ct.c_double),
+                ("p99_ms", ct.c_double), ("max_ms", ct.c_double), ("mean_ms", ct.c_double),
+                ("wall_s", ct.c_double), ("vertices_per_s", ct.c_double), ("peak_device_bytes", ct.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -97,6 +110,12 @@ def load(path: str = LIB_PATH):
     L.ephg_el_rates.argtypes = [vp, ct.POINTER(RateRequest), c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, c_dp, ct.c_int64]
     L.ephg_el_wann_noalloc.argtypes = [vp, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    L.ephg_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_int64, ct.c_int, ct.POINTER(vp)]
+    L.ephg_server_destroy.argtypes = [vp]
+    L.ephg_submit.argtypes = [vp, ct.c_int, ct.POINTER(RateRequest), c_i64p]
+    L.ephg_poll.argtypes = [vp, ct.c_int64, ct.POINTER(ct.c_int)]
+    L.ephg_wait.argtypes = [vp, ct.c_int64, c_dp, c_i64p, ct.POINTER(RateStats), c_dp]
+    L.ephg_server_stats_get.argtypes = [vp, ct.POINTER(ServerStats)]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ct.c_int
     L.ephg_last_error.restype = ct.c_char_p

@@ -175,9 +175,12 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
     ephg_destroy(h);
     return r;
   };
+  size_t free0 = 0, total0 = 0;
+  cudaMemGetInfo(&free0, &total0);
   if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaGetDevice"));
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(EPHG_ERR_CUDA, "cudaStreamCreate"));
+  h->ws.st = h->st;
   h->nw = (int)d->numwannbands;
   h->nb = (int)d->numbranches;
   h->nwsk = (int)d->nwsk;
@@ -316,6 +319,11 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
   if (cudaMemsetAsync(h->err, 0, sizeof(int), h->st) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "memset"));
   if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return bail(fail(EPHG_ERR_CUDA, "create: %s", cudaGetErrorString(cudaGetLastError())));
+  {
+    size_t free1 = 0, total1 = 0;
+    cudaMemGetInfo(&free1, &total1);
+    h->resident_bytes = free0 > free1 ? (int64_t)(free0 - free1) : 0;   // the uploads, at allocation granularity
+  }
   *out = h;
   return EPHG_OK;
 }
@@ -587,9 +595,25 @@ struct EvTimer {
 
 }  // namespace
 
-extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
-                             int64_t *indexlist, ephg_rate_stats *stats, double *g2,
-                             double *xplus, double *xminus, int64_t cap) {
+
+// the device error word of an execution view: read, clear, translate
+static int check_err_view(const ExecView &x) {
+  int w = 0;
+  CK(cudaMemcpyAsync(&w, x.err, sizeof(int), cudaMemcpyDeviceToHost, x.st));
+  CK(cudaStreamSynchronize(x.st));
+  CK(cudaMemsetAsync(x.err, 0, sizeof(int), x.st));
+  if (w & DERR_NEG_PHONON) return fail(EPHG_ERR_NEG_PHONON, "Large negative phonon energy found!");
+  if (w & DERR_EIG) return fail(EPHG_ERR_EIG, "Jacobi eigensolver did not converge");
+  if (w & DERR_INDEX) return fail(EPHG_ERR_INDEX, "device index check failed");
+  if (w & DERR_TIMEOUT) return fail(EPHG_ERR_TIMEOUT, "bounded device wait gave up");
+  return EPHG_OK;
+}
+
+#define WSFAILX(rc) fail((rc), "%s", x.ws->msg.c_str())
+
+int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
+                        int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus,
+                        int64_t cap) {
   if (!h || !req || !rates || !indexlist) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   for (int i = 0; i < 3; ++i)
     if (req->mesh[i] <= 0) return fail(EPHG_ERR_ARG, "el_rates: bad mesh");
@@ -607,61 +631,61 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   const size_t nn = (size_t)nw * nw;
   const int ncol = nw * nb;   // columns per initial state in stage B
   const bool split = req->precision == EPHG_PREC_SPLIT_TF32;
-  cudaStream_t st = h->st;
+  cudaStream_t st = x.st;
   int rc;
-  int64_t launches0 = h->launches;
+  int64_t launches0 = (*x.launches);
   EvTimer ev;
-  h->timer_a.reset();
-  h->timer_b.reset();
+  (*x.ta).reset();
+  (*x.tb).reset();
   CK(cudaEventRecord(ev.e[0], st));
   // ---- set-up: electrons on the full mesh (el_wann, electron.f90:364) ----
   double2 *roots, *P, *Hk, *V, *Dq, *Vq, *u;
   double *w, *ens, *wq, *om, *bose, *rates_d;
   int *flag, *widx, *nwv_d, *sflag, *iota, *st_code, *nst_d, *nin_k, *cum;
-  if ((rc = wsget(h->ws, "r_roots", (size_t)L, &roots)) || (rc = wsget(h->ws, "r_P", (size_t)N * nwsk, &P)) ||
-      (rc = wsget(h->ws, "r_Hk", (size_t)N * nn, &Hk)) || (rc = wsget(h->ws, "r_w", (size_t)N * nw, &w)) ||
-      (rc = wsget(h->ws, "r_V", (size_t)N * nn, &V)) || (rc = wsget(h->ws, "r_ens", (size_t)N * nw, &ens)) ||
-      (rc = wsget(h->ws, "r_flag", (size_t)N, &flag)) || (rc = wsget(h->ws, "r_widx", (size_t)N, &widx)) ||
-      (rc = wsget(h->ws, "r_nwv", 4, &nwv_d)) || (rc = wsget(h->ws, "r_iota", (size_t)N * nw, &iota)) ||
-      (rc = wsget(h->ws, "r_Dq", (size_t)N * nb * nb, &Dq)) || (rc = wsget(h->ws, "r_wq", (size_t)N * nb, &wq)) ||
-      (rc = wsget(h->ws, "r_Vq", (size_t)N * nb * nb, &Vq)) || (rc = wsget(h->ws, "r_om", (size_t)N * nb, &om)) ||
-      (rc = wsget(h->ws, "r_u", (size_t)N * nb * nb, &u)) || (rc = wsget(h->ws, "r_bose", (size_t)N * nb, &bose)) ||
-      (rc = wsget(h->ws, "r_rates", (size_t)N * nw, &rates_d)))
-    return WSFAIL(rc);
+  if ((rc = wsget((*x.ws), "r_roots", (size_t)L, &roots)) || (rc = wsget((*x.ws), "r_P", (size_t)N * nwsk, &P)) ||
+      (rc = wsget((*x.ws), "r_Hk", (size_t)N * nn, &Hk)) || (rc = wsget((*x.ws), "r_w", (size_t)N * nw, &w)) ||
+      (rc = wsget((*x.ws), "r_V", (size_t)N * nn, &V)) || (rc = wsget((*x.ws), "r_ens", (size_t)N * nw, &ens)) ||
+      (rc = wsget((*x.ws), "r_flag", (size_t)N, &flag)) || (rc = wsget((*x.ws), "r_widx", (size_t)N, &widx)) ||
+      (rc = wsget((*x.ws), "r_nwv", 4, &nwv_d)) || (rc = wsget((*x.ws), "r_iota", (size_t)N * nw, &iota)) ||
+      (rc = wsget((*x.ws), "r_Dq", (size_t)N * nb * nb, &Dq)) || (rc = wsget((*x.ws), "r_wq", (size_t)N * nb, &wq)) ||
+      (rc = wsget((*x.ws), "r_Vq", (size_t)N * nb * nb, &Vq)) || (rc = wsget((*x.ws), "r_om", (size_t)N * nb, &om)) ||
+      (rc = wsget((*x.ws), "r_u", (size_t)N * nb * nb, &u)) || (rc = wsget((*x.ws), "r_bose", (size_t)N * nb, &bose)) ||
+      (rc = wsget((*x.ws), "r_rates", (size_t)N * nw, &rates_d)))
+    return WSFAILX(rc);
   launch_roots(L, roots, st);
   launch_phase_mesh(N, nullptr, mesh, L, nwsk, h->Rk, h->degk, 0, roots, P, nwsk, st);
   launch_zgemm(N, (int)nn, nwsk, P, nwsk, h->Hext, 4 * (int64_t)nn, Hk, nn, st);
-  launch_heig(N, nw, Hk, nn, w, V, h->err, st);
+  launch_heig(N, nw, Hk, nn, w, V, x.err, st);
   launch_el_post(N, nw, w, V, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, ens, st);
   // ---- window (apply_energy_window, electron.f90:597-636) ----
   launch_window_flags(N, nw, ens, req->enref, req->fsthick, flag, st);
   launch_iota(N * nw, iota, st);
   size_t tmp_bytes = 0, tb2 = 0, tb3 = 0;
   cub::DeviceSelect::Flagged(nullptr, tmp_bytes, iota, flag, widx, nwv_d, N, st);
-  if ((rc = wsget(h->ws, "r_sflag", (size_t)N * nw, &sflag)) || (rc = wsget(h->ws, "r_stcode", (size_t)N * nw, &st_code)) ||
-      (rc = wsget(h->ws, "r_nst", 4, &nst_d)) || (rc = wsget(h->ws, "r_nink", (size_t)N + 1, &nin_k)) ||
-      (rc = wsget(h->ws, "r_cum", (size_t)N + 1, &cum)))
-    return WSFAIL(rc);
+  if ((rc = wsget((*x.ws), "r_sflag", (size_t)N * nw, &sflag)) || (rc = wsget((*x.ws), "r_stcode", (size_t)N * nw, &st_code)) ||
+      (rc = wsget((*x.ws), "r_nst", 4, &nst_d)) || (rc = wsget((*x.ws), "r_nink", (size_t)N + 1, &nin_k)) ||
+      (rc = wsget((*x.ws), "r_cum", (size_t)N + 1, &cum)))
+    return WSFAILX(rc);
   cub::DeviceSelect::Flagged(nullptr, tb2, iota, sflag, st_code, nst_d, N * nw, st);
   cub::DeviceScan::ExclusiveSum(nullptr, tb3, nin_k, cum, N + 1, st);
   void *cubtmp;
-  if ((rc = h->ws.get("r_cub", std::max(tmp_bytes, std::max(tb2, tb3)), &cubtmp))) return WSFAIL(rc);
+  if ((rc = x.ws->get("r_cub", std::max(tmp_bytes, std::max(tb2, tb3)), &cubtmp))) return WSFAILX(rc);
   size_t tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
   cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, flag, widx, nwv_d, N, st);
-  h->launches += 8;
+  (*x.launches) += 8;
   CKL();
   int nwv = 0;
   CK(cudaMemcpyAsync(&nwv, nwv_d, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if ((rc = ephg::api_check_err(h))) return rc;
+  if ((rc = check_err_view(x))) return rc;
   if (nwv == 0) return fail(EPHG_ERR_EMPTY_WINDOW, "No states found within Fermi window.");
   // ---- phonons on the q mesh (phonon.f90:208-214) ----
   launch_dbuild(N, iota, mesh, L, roots, nullptr, h->terms, 0, Dq, nullptr, st);
-  launch_heig(N, nb, Dq, (int64_t)nb * nb, wq, Vq, h->err, st);
+  launch_heig(N, nb, Dq, (int64_t)nb * nb, wq, Vq, x.err, st);
   float2 *uf = nullptr;
-  if (split && (rc = wsget(h->ws, "r_uf", (size_t)N * nb * nb, &uf))) return WSFAIL(rc);
+  if (split && (rc = wsget((*x.ws), "r_uf", (size_t)N * nb * nb, &uf))) return WSFAILX(rc);
   launch_ph_post(N, nb, iota, nullptr, wq, Vq, nullptr, 0, h->masses, nullptr, nullptr, nullptr, om,
-                 u, uf, h->err, st);
+                 u, uf, x.err, st);
   launch_bose(N, nb, om, req->T, bose, st);
   // ---- initial states (demux_state order, interactions.f90:2169-2191) ----
   launch_state_flags(nwv, nw, widx, ens, req->enref, req->fsthick, sflag, nin_k, st);
@@ -670,7 +694,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, sflag, st_code, nst_d, nwv * nw, st);
   tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
   cub::DeviceScan::ExclusiveSum(cubtmp, tbytes, nin_k, cum, nwv + 1, st);
-  h->launches += 7;
+  (*x.launches) += 7;
   CKL();
   int nst = 0, nin = 0;
   CK(cudaMemcpyAsync(&nst, nst_d, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -678,7 +702,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   std::vector<int> widx_h(nwv), code_h;
   CK(cudaMemcpyAsync(widx_h.data(), widx, nwv * sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if ((rc = ephg::api_check_err(h))) return rc;
+  if ((rc = check_err_view(x))) return rc;
   code_h.resize(nst);
   CK(cudaMemcpyAsync(code_h.data(), st_code, nst * sizeof(int), cudaMemcpyDeviceToHost, st));
   // simplices for triangle / tetrahedron deltas
@@ -696,9 +720,9 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     build_simplices((int)req->delta_kind, mesh, widx_h, ens_w, nw, map, count, sev, ns, maxc, nvx);
     int *dmap, *dcount;
     double *dsev;
-    if ((rc = wsget(h->ws, "r_smap", map.size(), &dmap)) || (rc = wsget(h->ws, "r_scount", count.size(), &dcount)) ||
-        (rc = wsget(h->ws, "r_sev", sev.size(), &dsev)))
-      return WSFAIL(rc);
+    if ((rc = wsget((*x.ws), "r_smap", map.size(), &dmap)) || (rc = wsget((*x.ws), "r_scount", count.size(), &dcount)) ||
+        (rc = wsget((*x.ws), "r_sev", sev.size(), &dsev)))
+      return WSFAILX(rc);
     CK(cudaMemcpyAsync(dmap, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dcount, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dsev, sev.data(), sev.size() * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -715,6 +739,7 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   for (int i = nwv - 1; i >= 0; --i)
     if (first_state[i] > first_state[i + 1]) first_state[i] = first_state[i + 1];
   CK(cudaEventRecord(ev.e[1], st));
+  x.yield();   // serving: hand the GPU to a smaller request before the contractions
   // ---- stage A: g(k,Rp) for window k, rotation over m, k-half of the Rp phase ----
   const int64_t ldb = (int64_t)ncol * nst;
   const int64_t Nn = h->Nn;
@@ -745,9 +770,9 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   int64_t vtot = (int64_t)nst * nin * nb;
   int64_t vcap = std::min<int64_t>(cap, vtot);
   if (g2 && vcap > 0) {
-    if ((rc = wsget(h->ws, "r_vg2", (size_t)vcap, &g2d)) || (rc = wsget(h->ws, "r_vxp", (size_t)vcap, &xpd)) ||
-        (rc = wsget(h->ws, "r_vxm", (size_t)vcap, &xmd)))
-      return WSFAIL(rc);
+    if ((rc = wsget((*x.ws), "r_vg2", (size_t)vcap, &g2d)) || (rc = wsget((*x.ws), "r_vxp", (size_t)vcap, &xpd)) ||
+        (rc = wsget((*x.ws), "r_vxm", (size_t)vcap, &xmd)))
+      return WSFAILX(rc);
     ed.g2 = g2d;
     ed.xp = xpd;
     ed.xm = xmd;
@@ -756,64 +781,65 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   int nblk = (nwv + 127) / 128;                 // k'-row blocks of the rate partials
   const int nblk_max = std::max((nwv + 15) / 16, (nwv + 255) / 256 * 8);
   double *partial;
-  if ((rc = wsget(h->ws, "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAIL(rc);
+  if ((rc = wsget((*x.ws), "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAILX(rc);
   if (!split) {
     double2 *Pk, *gk, *B, *Pq, *Cb;
     const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nwv, ((int64_t)1 << 31) / (Nn * 16)));
     const int64_t sc = std::max<int64_t>(1, std::min<int64_t>({(int64_t)nst, (int64_t)32768,
                                                               ((int64_t)1 << 31) / ((int64_t)nwv * ncol * 16)}));
-    if ((rc = wsget(h->ws, "a_Pk", (size_t)kc * nwsk, &Pk)) || (rc = wsget(h->ws, "a_gk", (size_t)kc * Nn, &gk)) ||
-        (rc = wsget(h->ws, "a_B", (size_t)nwsq * ldb, &B)) || (rc = wsget(h->ws, "b_Pq", (size_t)nwv * nwsq, &Pq)) ||
-        (rc = wsget(h->ws, "b_C", (size_t)nwv * ncol * sc, &Cb)))
-      return WSFAIL(rc);
+    if ((rc = wsget((*x.ws), "a_Pk", (size_t)kc * nwsk, &Pk)) || (rc = wsget((*x.ws), "a_gk", (size_t)kc * Nn, &gk)) ||
+        (rc = wsget((*x.ws), "a_B", (size_t)nwsq * ldb, &B)) || (rc = wsget((*x.ws), "b_Pq", (size_t)nwv * nwsq, &Pq)) ||
+        (rc = wsget((*x.ws), "b_C", (size_t)nwv * ncol * sc, &Cb)))
+      return WSFAILX(rc);
     for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
       int n = (int)std::min<int64_t>(kc, nwv - i0);
       launch_phase_mesh(n, widx + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
-      h->timer_a.begin(st);
+      (*x.ta).begin(st);
       launch_zgemm(n, (int)Nn, nwsk, Pk, nwsk, h->G64, Nn, gk, Nn, st);
-      h->timer_a.end(st);
+      (*x.ta).end(st);
       // the rotation writes B columns of states [j0, j1) (grid.y <= 32768 per launch)
       for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
         int je = std::min(j1, j0 + 32768);
         launch_rotate_states_fp64(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, V, gk, Nn, mesh, L,
                                   roots, h->Rq, h->degq, B + (int64_t)j0 * ncol, ldb, st);
-        h->launches += 1;
+        (*x.launches) += 1;
       }
-      h->launches += 2;
+      (*x.launches) += 2;
     }
     CK(cudaEventRecord(ev.e[2], st));
     // ---- stage B + C: Rp Fourier against e^{2 pi i k'.Rp}, then the epilogue ----
     launch_phase_mesh(nwv, widx, mesh, L, nwsq, h->Rq, nullptr, 0, roots, Pq, nwsq, st);
-    h->launches += 1;
+    (*x.launches) += 1;
     for (int64_t j0 = 0; j0 < nst; j0 += sc) {
       int ns = (int)std::min<int64_t>(sc, nst - j0);
-      h->timer_b.begin(st);
+      (*x.tb).begin(st);
       launch_zgemm(nwv, ns * ncol, nwsq, Pq, nwsq, B + j0 * ncol, ldb, Cb, (int64_t)ns * ncol, st);
-      h->timer_b.end(st);
+      (*x.tb).end(st);
       launch_epilogue_fp64(nwv, (int)j0, (int)j0 + ns, Cb, (int64_t)ns * ncol, rp, ed, partial, nblk, st);
-      h->launches += 2;
+      (*x.launches) += 2;
     }
   } else {
-    rc = tc::split_rates_stage(h->split, h->ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
+    rc = tc::split_rates_stage(h->split, *x.ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
                                mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->kposk,
                                h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk_max, &nblk,
-                               ev.e[2], &h->launches, &h->timer_a, &h->timer_b);
+                               ev.e[2], x.launches, x.ta, x.tb, &h->split_mu, x.chunk_us, x.yield);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
   }
   CKL();
   CK(cudaMemsetAsync(rates_d, 0, (size_t)N * nw * sizeof(double), st));
   launch_rate_final(nst, nblk, partial, st_code, nw, N, rates_d, st);
-  h->launches += 1;
+  (*x.launches) += 1;
   CK(cudaEventRecord(ev.e[3], st));
   CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   for (int i = 0; i < nwv; ++i) indexlist[i] = (int64_t)widx_h[i] + 1;
   if (g2 && vcap > 0) {
-    CK(cudaMemcpy(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost));
-    if (xplus) CK(cudaMemcpy(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
-    if (xminus) CK(cudaMemcpy(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (xplus) CK(cudaMemcpyAsync(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (xminus) CK(cudaMemcpyAsync(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
   }
-  if ((rc = ephg::api_check_err(h))) return rc;
+  if ((rc = check_err_view(x))) return rc;
   if (stats) {
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
     cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
@@ -825,17 +851,25 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
     stats->nstates = nst;
     stats->vertices = vtot;
     stats->pairs = (int64_t)nst * nwv;
-    stats->kernel_launches = h->launches - launches0;
+    stats->kernel_launches = (*x.launches) - launches0;
     stats->ms_setup = t01;
     stats->ms_stage_a = t12;
     stats->ms_stage_bc = t23;
     stats->ms_total = t03;
     stats->stage_a_gflop = 8.0 * (double)nwv * nwsk * (double)Nn * 1e-9;
     stats->stage_b_gflop = 8.0 * (double)nwv * nwsq * (double)ncol * nst * 1e-9;
-    stats->ms_gemm_a = h->timer_a.total_ms();
-    stats->ms_gemm_b = h->timer_b.total_ms();
-    stats->gemm_a_launches = h->timer_a.n;
-    stats->gemm_b_launches = h->timer_b.n;
+    stats->ms_gemm_a = (*x.ta).total_ms();
+    stats->ms_gemm_b = (*x.tb).total_ms();
+    stats->gemm_a_launches = (*x.ta).n;
+    stats->gemm_b_launches = (*x.tb).n;
   }
   return EPHG_OK;
+}
+
+extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
+                             int64_t *indexlist, ephg_rate_stats *stats, double *g2,
+                             double *xplus, double *xminus, int64_t cap) {
+  if (!h) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
+  const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
+  return el_rates_view(h, x, req, rates, indexlist, stats, g2, xplus, xminus, cap);
 }

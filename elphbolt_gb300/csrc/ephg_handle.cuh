@@ -1,5 +1,6 @@
 // ephg_handle.cuh - the library handle (internal; the C ABI sees an opaque pointer).
 #pragma once
+#include <mutex>
 #include <vector>
 
 #include "../../include/ephg.h"
@@ -35,9 +36,27 @@ struct ephg_handle {
   ephg::tc::SplitOperands split;   // split-TF32 operand planes (lazy)
   ephg::LaunchTimer timer_a, timer_b;   // device time of the contraction launches of the last request
   int64_t launches = 0;
+  int64_t resident_bytes = 0;   // device bytes taken by ephg_create (Wannier data, tables)
+  std::mutex split_mu;          // guards the one-time build of `split`
 };
 
 namespace ephg {
+// Where a rate request runs: stream, device error word, workspace, timers and
+// launch counter.  The handle's own fields form the default view
+// (ephg_el_rates); the serving loop gives each of its slots one of its own, so
+// that requests on one crystal overlap on the device.  The crystal's resident
+// data is shared read-only.
+struct ExecView {
+  cudaStream_t st;
+  int *err;
+  Workspace *ws;
+  LaunchTimer *ta, *tb;
+  int64_t *launches;
+  int chunk_us = 0;   // > 0: persistent kernels run as launches of about this length (serving)
+  Yield yield;        // called between chunks and stages (serving); no-op by default
+};
+int el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
+                  int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus, int64_t cap);
 // record a failure message for ephg_last_error() and return code
 int api_fail(int code, const char *fmt, ...);
 // read, clear and translate the handle's device error word

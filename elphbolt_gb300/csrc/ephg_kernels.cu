@@ -4,6 +4,7 @@
 // eigensolver, the FP64 complex GEMM used by the plain drop-in, and the
 // per-(k', state) epilogue that forms |g|^2, X+- and the RTA rate partials.
 // Each kernel names the reference lines it restates.
+#include <mutex>
 #include <cstdio>
 
 #include "ephg_kernels.cuh"
@@ -315,11 +316,11 @@ void launch_heig(int batch, int n, const double2 *A, int64_t stride, double *w, 
   if (batch <= 0) return;
   int wpb = n <= 16 ? 4 : 2;
   size_t smem = (size_t)wpb * (2 * n * n + 3 * 16) * sizeof(double2);
-  static bool attr_set = false;
-  if (!attr_set) {
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
     cudaFuncSetAttribute(k_heig, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-    attr_set = true;
-  }
+  });
   k_heig<<<(batch + wpb - 1) / wpb, 32 * wpb, smem, st>>>(batch, n, A, stride, w, V, err);
 }
 
@@ -482,11 +483,11 @@ void launch_dbuild(int nq, const int *qp, const int mesh[3], int L, const double
   if (nq <= 0) return;
   // phase sums [npair][DB_CHUNK], reused for the slice sums (<= 128 entries)
   const size_t smem = (size_t)std::max(t.npair * DB_CHUNK, 128) * sizeof(double2);
-  static bool attr = false;
-  if (!attr) {
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
     cudaFuncSetAttribute(k_dbuild, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-    attr = true;
-  }
+  });
   k_dbuild<<<nq, 128, smem, st>>>(nq, qp, mesh ? mesh[0] : 1, mesh ? mesh[1] : 1, mesh ? mesh[2] : 1, L, roots, qv,
                                   t, with_vel, Dq, dDq);
 }

@@ -29,6 +29,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -39,7 +40,7 @@
 namespace ephg {
 namespace tc {
 
-static std::string g_msg;
+static thread_local std::string g_msg;
 const char *last_error() { return g_msg.c_str(); }
 
 static int tfail(int code, const char *m) {
@@ -213,6 +214,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 // -------------------------------------------------------- the GEMM kernel
 struct GemmArgs {
   int mtiles, ntiles, nkb;   // tile counts, K blocks of BK
+  int t0, t1;                // tiles [t0, t1) of this launch
   int64_t Astride, Bstride;  // rows between consecutive planes of the A / B stacks
   int64_t Aoff, Boff;        // first row of the operand inside plane 0
   float *Cr, *Ci;            // [Mp][ldc] outputs
@@ -252,7 +254,6 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int ntile = g.mtiles * g.ntiles;
 
   if (warp == 0) {
     if (lane == 0) {   // ---- TMA producer
@@ -261,7 +262,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+      for (int t = g.t0 + blockIdx.x; t < g.t1 && ok; t += gridDim.x) {
         const int mt = t % g.mtiles, nt = t / g.mtiles;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t mr = tmem, mi = tmem + BN, cr = tmem + 2 * BN, ci = tmem + 3 * BN;
-      for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x, ++it) {
+      for (int t = g.t0 + blockIdx.x; t < g.t1 && ok; t += gridDim.x, ++it) {
         if (!mbar_wait(&tempty[0], (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < g.nkb; ++kb) {
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     int it = 0;
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x, ++it) {
+    for (int t = g.t0 + blockIdx.x; t < g.t1; t += gridDim.x, ++it) {
       const int mt = t % g.mtiles, nt = t / g.mtiles;
       if (!mbar_wait(&tfull[0], it & 1, g.err)) break;
       tc_fence_after();
@@ -373,15 +374,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
 // -------------------------------------------------------- tensor maps
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {   // thread-safe one-time initialisation
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -404,30 +405,27 @@ static int make_map(CUtensorMap *m, const float *base, int Kp, int64_t rows, int
 }
 
 static int num_sms() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
 }
 
 // C[Mp][ldc] (re, im planes) = A x B^T.  A: planes of Astride rows, rows
 // [Aoff, Aoff + Mp) of each; B: planes of Bstride rows, rows [Boff, Boff + Np).
 static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const float *Bp, int64_t Bstride,
-                 int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st) {
+                 int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st,
+                 int chunk_us = 0, const Yield &yield = Yield()) {
   if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
   if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
   CUtensorMap ta, tb;
   int rc;
   if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 4 * Bstride))) return rc;
-  static bool attr = false;
-  if (!attr) {
-    TCK(cudaFuncSetAttribute(k_cgemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(k_cgemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
   GemmArgs g;
   g.mtiles = Mp / BM;
   g.ntiles = Np / BN;
@@ -442,8 +440,17 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   g.err = err;
   int tiles = g.mtiles * g.ntiles;
   int grid = std::min(tiles, num_sms());
-  k_cgemm_3xtf32<<<grid, GEMM_THREADS, SMEM_BYTES, st>>>(ta, tb, g);
-  TCK(cudaGetLastError());
+  // chunk_us > 0: launches of about that length (a tile is ~0.4 us per 16 K positions) so
+  // that other streams' kernels get the SMs between them
+  const int per_cta = chunk_us > 0 ? std::max(1, (int)((int64_t)chunk_us * 16 * 5 / 2 / std::max(1, Kp))) : 0;
+  const int step = per_cta > 0 ? grid * per_cta : tiles;
+  for (int t0 = 0; t0 < tiles; t0 += step) {
+    if (t0 > 0) yield();
+    g.t0 = t0;
+    g.t1 = std::min(tiles, t0 + step);
+    k_cgemm_3xtf32<<<grid, GEMM_THREADS, SMEM_BYTES, st>>>(ta, tb, g);
+    TCK(cudaGetLastError());
+  }
   return 0;
 }
 
@@ -916,6 +923,7 @@ __host__ __device__ __forceinline__ int64_t blk32(int64_t i, int nf, int f) {
 
 struct FusedArgs {
   int mtiles, ntiles, nkb;
+  int t0, t1;                 // tile pairs [t0, t1) of this launch
   int64_t Astride, Bstride;   // rows between planes of the phase / state operand stacks
   int nwv, nst;
   int *err;
@@ -1095,7 +1103,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const int mpairs = g.mtiles >> 1;
-  const int ntile = mpairs * g.ntiles;           // tile pairs
+  (void)mpairs;
   const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
 
   if (warp == 0) {
@@ -1105,7 +1113,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = cid; t < ntile && ok; t += ncl) {
+      for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
         const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -1135,7 +1143,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t dm = tmem, dc = tmem + 256;   // main, correction (re | im each)
-      for (int t = cid; t < ntile && ok; t += ncl, ++it) {
+      for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl, ++it) {
         if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < g.nkb; ++kb) {
@@ -1173,7 +1181,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
     const int m0 = rp.mesh[0], m1 = rp.mesh[1], m2 = rp.mesh[2];
     int it = 0;
-    for (int t = cid; t < ntile; t += ncl, ++it) {
+    for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
       const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
       // ---- row and state data, before the accumulators are ready
       const int ip = mt * BM + quad * 32 + lane;      // < MpB
@@ -1266,9 +1274,13 @@ __global__ void __launch_bounds__(F_THREADS, 1)
 }
 
 // Launch a persistent kernel as clusters of 2 CTAs: as many pairs as can be
-// resident at once (at most one CTA per SM), at most `pairs`.
+// resident at once (at most one CTA per SM), at most `pairs` (work units).
+// chunk > 0 splits the work into launches of chunk units per cluster, so that
+// kernels of other streams (other requests of the serving loop) get the SMs
+// between launches; launch(cfg, t0, t1) issues the launch for units [t0, t1).
 template <class F>
-static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_t st, F launch) {
+static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_t st, int chunk, const Yield &yield,
+                        F launch) {
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1284,25 +1296,30 @@ static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_
   int ncl = 0;
   TCK(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
   if (ncl <= 0) return tfail(2, "no 2-CTA cluster fits on the device");
-  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(pairs, ncl)));
-  TCK(launch(cfg));
-  TCK(cudaGetLastError());
+  const int64_t nc = std::min<int64_t>(pairs, ncl);
+  cfg.gridDim = dim3((unsigned)(2 * nc));
+  const int64_t step = chunk > 0 ? nc * chunk : pairs;
+  for (int64_t t0 = 0; t0 < pairs; t0 += step) {
+    if (t0 > 0) yield();
+    TCK(launch(cfg, (int)t0, (int)std::min<int64_t>(pairs, t0 + step)));
+    TCK(cudaGetLastError());
+  }
   return 0;
 }
 
 static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2, int KpB, int nwv, int nst,
                           const RateParams &rp, const EpiData &ed, const FusedTabs &tabs, double *partial, int nblk,
-                          int *err, cudaStream_t st) {
+                          int *err, cudaStream_t st, int chunk, const Yield &yield) {
   if (MpB % BM || Np2 % FBN || KpB % BK) return tfail(1, "stage B: shapes not tile multiples");
   if (4 * (int64_t)MpB > INT32_MAX || 6 * Np2 > INT32_MAX) return tfail(1, "stage B: operand too tall for TMA coords");
   CUtensorMap ta, tb;
   int rc;
   if ((rc = make_map(&ta, PB, KpB, 4 * (int64_t)MpB)) || (rc = make_map(&tb, B2, KpB, 6 * Np2, FBN))) return rc;
-  static bool attr = false;
-  if (!attr) {
-    TCK(cudaFuncSetAttribute(k_stageB_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
-    attr = true;
-  }
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(k_stageB_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+  });
   FusedArgs g;
   g.mtiles = MpB / BM;
   g.ntiles = (nst + 1) / 2;
@@ -1318,9 +1335,12 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   if (g.mtiles % 2) return tfail(1, "stage B: row tiles must pair");
   const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
   if (pairs > INT32_MAX) return tfail(1, "stage B: too many tiles");
-  return launch_pairs((const void *)k_stageB_fused86, F_SMEM, pairs, st, [&](cudaLaunchConfig_t &cfg) {
-    return cudaLaunchKernelEx(&cfg, k_stageB_fused86, ta, tb, g, tabs, rp, ed);
-  });
+  return launch_pairs((const void *)k_stageB_fused86, F_SMEM, pairs, st, chunk, yield,
+                      [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
+                        g.t0 = t0;
+                        g.t1 = t1;
+                        return cudaLaunchKernelEx(&cfg, k_stageB_fused86, ta, tb, g, tabs, rp, ed);
+                      });
 }
 
 // ------------------------------- stage A fused with the initial-band rotation
@@ -1357,6 +1377,7 @@ __device__ __forceinline__ uint64_t sdesc32(const void *p) {
 
 struct FusedAArgs {
   int mtiles, ntiles, nkb, nkp16;   // nkp16: 16-position blocks of the state operand's K
+  int t0, t1;                        // tile pairs [t0, t1) of this launch
   int64_t Astride, Bstride;          // rows between planes: phase operand, stage-A operand
   int KpB;
   int64_t Np2;                       // rows per plane of the state operand
@@ -1453,7 +1474,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const int mpairs = g.mtiles >> 1;
-  const int ntile = mpairs * g.ntiles;           // tile pairs
+  (void)mpairs;
   const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
 
   if (warp == 0) {
@@ -1463,7 +1484,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = cid; t < ntile && ok; t += ncl) {
+      for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
         const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -1490,7 +1511,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t dm = tmem, dc = tmem + 256;
-      for (int t = cid; t < ntile && ok; t += ncl, ++it) {
+      for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl, ++it) {
         if (!mbar_wait(tempty, (it & 1) ^ 1, g.err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < g.nkb; ++kb) {
@@ -1521,7 +1542,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const int quad = warp & 3, half = (warp - 2) >> 2;
     const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
     int it = 0;
-    for (int t = cid; t < ntile; t += ncl, ++it) {
+    for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
       const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
       const int kpb = nt % g.nkp16, ns = nt / g.nkp16;
       const int col0 = (ns & 7) + 8 * (ns >> 3);      // n' + 8 s'
@@ -1588,18 +1609,18 @@ __global__ void __launch_bounds__(F_THREADS, 1)
 }
 
 static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA, int KpA, const FusedTabs &tabs,
-                          FusedAArgs g, cudaStream_t st) {
+                          FusedAArgs g, cudaStream_t st, int chunk, const Yield &yield) {
   if (MpA % BM || NA % BM || KpA % A_BK || g.KpB % 16) return tfail(1, "stage A: shapes not tile multiples");
   if (4 * (int64_t)MpA > INT32_MAX || 6 * NA > INT32_MAX) return tfail(1, "stage A: operand too tall for TMA coords");
   CUtensorMap ta, tb;
   int rc;
   if ((rc = make_map(&ta, PA, KpA, 4 * (int64_t)MpA, BM, A_BK)) || (rc = make_map(&tb, GA6, KpA, 6 * NA, BM, A_BK)))
     return rc;
-  static bool attr = false;
-  if (!attr) {
-    TCK(cudaFuncSetAttribute(k_stageA_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, A_SMEM));
-    attr = true;
-  }
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(k_stageA_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, A_SMEM);
+  });
   g.mtiles = MpA / BM;
   g.ntiles = (int)(NA / BM);
   g.nkb = KpA / A_BK;
@@ -1610,9 +1631,12 @@ static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA
   if (g.mtiles % 2) return tfail(1, "stage A: row tiles must pair");
   const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
   if (pairs > INT32_MAX) return tfail(1, "stage A: too many tiles");
-  return launch_pairs((const void *)k_stageA_fused86, A_SMEM, pairs, st, [&](cudaLaunchConfig_t &cfg) {
-    return cudaLaunchKernelEx(&cfg, k_stageA_fused86, ta, tb, g, tabs);
-  });
+  return launch_pairs((const void *)k_stageA_fused86, A_SMEM, pairs, st, chunk, yield,
+                      [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
+                        g.t0 = t0;
+                        g.t1 = t1;
+                        return cudaLaunchKernelEx(&cfg, k_stageA_fused86, ta, tb, g, tabs);
+                      });
 }
 
 // ------------------------------------------------------------ orchestration
@@ -1621,6 +1645,7 @@ void free_split(SplitOperands &s) {
   if (s.GA6) cudaFree(s.GA6);
   s.G = nullptr;
   s.GA6 = nullptr;
+  s.bytes = 0;
 }
 
 static inline int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
@@ -1654,13 +1679,17 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                const std::vector<int> &first_state, const int *Rk, const double *degk,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
-                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
+                               std::mutex *build_mu, int chunk_us, const Yield &yield) {
   int rc;
   const int KpA = (int)rup(nwsk, BK), KpB = (int)rup(nwsq, BK);
   const int64_t NpA = rup(Nn, BN);
   // g(Re,Rp) planes, built once per handle
+  {
+  std::lock_guard<std::mutex> build_lock(*build_mu);
   if (!s.G) {
     TCK(cudaMalloc(&s.G, (size_t)4 * NpA * KpA * sizeof(float)));
+    s.bytes += (int64_t)4 * NpA * KpA * sizeof(float);
     TCK(cudaMemsetAsync(s.G, 0, (size_t)4 * NpA * KpA * sizeof(float), st));
     dim3 grid((unsigned)((Nn + 31) / 32), (unsigned)((KpA + 31) / 32));
     k_gplanes<<<grid, dim3(32, 8), 0, st>>>(Nn, nwsk, G64, kposA, s.G, NpA, KpA);
@@ -1668,6 +1697,8 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     s.Nn = NpA;
     s.Kp = KpA;
     (*launches)++;
+    TCK(cudaStreamSynchronize(st));   // complete before other streams may read it
+  }
   }
   const int ncol = nw * nb;
   // stage A in k chunks of kc rows (multiple of BM)
@@ -1694,6 +1725,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   TCK(cudaGetLastError());
   *launches += 1;
   for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
+    if (i0 > 0) yield();
     const int n = (int)std::min<int64_t>(kc, nwv - i0);
     const int Mp = (int)rup(n, BM);
     TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
@@ -1702,17 +1734,17 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                                                  degk, kposA, roots, PA, Mp, KpA);
     TCK(cudaGetLastError());
     tA->begin(st);
-    if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st))) return rc;
+    if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st, chunk_us, yield))) return rc;
     tA->end(st);
     {
       const int per = nw * nw * nb;
       const size_t sm = ((sizeof(float2) * ROT_KT * per + 15) & ~(size_t)15) + sizeof(float2) * (nw * nw + ROT_KT);
       if (sm <= 160 * 1024) {
-        static bool rattr = false;
-        if (!rattr) {
-          TCK(cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-          rattr = true;
-        }
+        // once per process: changing a kernel attribute can wait for the device's queued work
+        static std::once_flag attr_once;
+        std::call_once(attr_once, [] {
+          cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+        });
         k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, widx, U, CAr, CAi, NpA, mesh[0], mesh[1],
                                       mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
         TCK(cudaGetLastError());
@@ -1759,7 +1791,9 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
-    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st))) return rc;
+    if (j0 > 0) yield();
+    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st, chunk_us, yield)))
+      return rc;
     tB->end(st);
     const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
     if (rp.delta_kind == 0 && esm > 200 * 1024) {
@@ -1770,11 +1804,11 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
       const int spb = 16;
       dim3 grid(nblk, (ns + spb - 1) / spb);
       const size_t sm = esm;
-      static bool eattr = false;
-      if (!eattr) {
-        TCK(cudaFuncSetAttribute(k_epilogue_split2<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        eattr = true;
-      }
+      // once per process: changing a kernel attribute can wait for the device's queued work
+      static std::once_flag attr_once;
+      std::call_once(attr_once, [] {
+        cudaFuncSetAttribute(k_epilogue_split2<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      });
       k_epilogue_split2<0, 0><<<grid, EPI_ROWS, sm, st>>>(nwv, (int)j0, (int)j0 + ns, spb, CBr, CBi, NpC, rp, ed, qt,
                                                          partial, nblk);
       TCK(cudaGetLastError());
@@ -1794,7 +1828,8 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                const int *widx, const int *st_code, const int *Rk, const double *degk,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
-                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+                               cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
+                               std::mutex *build_mu, int chunk_us, const Yield &yield) {
   int rc;
   const int ncol = 48;
   const int KpA = (int)rup(nwsk, 16), KpB = (int)rup(nwsq, 16);
@@ -1809,10 +1844,16 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   TCK(cudaGetLastError());
   (*launches)++;
   // stage-A operand, built once per handle
+  {
+  std::lock_guard<std::mutex> build_lock(*build_mu);
   if (!s.GA6 || s.NA != NA || s.KpA6 != KpA) {
-    if (s.GA6) cudaFree(s.GA6);
+    if (s.GA6) {
+      cudaFree(s.GA6);
+      s.bytes -= (int64_t)6 * s.NA * s.KpA6 * sizeof(float);
+    }
     s.GA6 = nullptr;
     TCK(cudaMalloc(&s.GA6, (size_t)6 * NA * KpA * sizeof(float)));
+    s.bytes += (int64_t)6 * NA * KpA * sizeof(float);
     TCK(cudaMemsetAsync(s.GA6, 0, (size_t)6 * NA * KpA * sizeof(float), st));
     const int64_t ne = NA * nwsk;
     k_gplanes_a6<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwsk, Nn, G64, kposA, kinvB, KpB, s.GA6, NA, KpA);
@@ -1820,6 +1861,8 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
     s.NA = NA;
     s.KpA6 = KpA;
     (*launches)++;
+    TCK(cudaStreamSynchronize(st));   // complete before other streams may read it
+  }
   }
   EpiTables et;
   if ((rc = epi_tables(ws, st, U, rp, ed_in, launches, &et))) return rc;
@@ -1877,7 +1920,10 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   ga.phk = phk;
   ga.err = err;
   tA->begin(st);
-  if ((rc = stageA_fused86(PA, Mp, s.GA6, NA, KpA, tabs, ga, st))) return rc;
+  if ((rc = stageA_fused86(PA, Mp, s.GA6, NA, KpA, tabs, ga, st, chunk_us > 0 ? std::max(1, chunk_us / 25) : 0,
+                           yield)))
+    return rc;
+  yield();
   tA->end(st);
   (*launches)++;
   TCK(cudaEventRecord(ev_stage_a, st));
@@ -1893,7 +1939,9 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   EpiData ed = ed_in;
   ed.Uf = et.Uf;
   tB->begin(st);
-  if ((rc = stageB_fused86(PB, Mp, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st))) return rc;
+  if ((rc = stageB_fused86(PB, Mp, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st,
+                           chunk_us > 0 ? std::max(1, chunk_us / 13) : 0, yield)))
+    return rc;
   tB->end(st);
   (*launches)++;
   return 0;
@@ -1904,7 +1952,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
                       const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
                       const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
-                      int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB) {
+                      int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
+                      std::mutex *build_mu, int chunk_us, const Yield &yield) {
   // The fused path packs mesh coordinates in 10 bits each.
   const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
                        mesh[2] <= 1024);
@@ -1920,11 +1969,11 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   if (fast86) {
     if ((rc = split_rates_fused86(s, ws, st, G64, nwsk, nwsq, Nn, nwv, nst, mesh, L, roots, widx, st_code, Rk, degk,
                                   kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err, ev_stage_a, launches, tA,
-                                  tB)))
+                                  tB, build_mu, chunk_us, yield)))
       return rc;
   } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, st_code,
                                        first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err,
-                                       ev_stage_a, launches, tA, tB))) {
+                                       ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield))) {
     return rc;
   }
   int herr = 0;

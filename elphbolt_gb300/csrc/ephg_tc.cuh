@@ -1,5 +1,7 @@
 // ephg_tc.cuh - split-precision (3xTF32) tensor-core path of the rate pipeline.
 #pragma once
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "ephg_kernels.cuh"
@@ -16,6 +18,7 @@ struct SplitOperands {
   float *GA6 = nullptr;    // the fused nw = 8, nb = 6 path's stage-A operand: six planes [6][NA][KpA6]
   int64_t NA = 0;
   int KpA6 = 0;
+  std::atomic<int64_t> bytes{0};   // device bytes held by G and GA6 (read by the serving loop's budget)
 };
 
 void free_split(SplitOperands &s);
@@ -25,8 +28,12 @@ const char *last_error();
 // partials [state][k'-block] like the FP64 path, using up to nblk_max k'
 // blocks (*nblk_used returns the count).  kposA / kposB give the contraction
 // position of each Re / Rp cell (cells ordered far to near).  Records
-// ev_stage_a after stage A.  Returns 0 or an EPHG_ERR_* code (message in
-// last_error()).
+// ev_stage_a after stage A.  The operand planes kept in s are built once,
+// under build_mu and completed before it is released, so that requests on
+// other streams may share them.  chunk_us > 0 splits the persistent
+// contraction kernels into launches of about that many microseconds, so that
+// other streams' kernels get the SMs between them.  Returns 0 or an EPHG_ERR_*
+// code (message in last_error()).
 int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64,
                       int nwsk, int nwsq, int64_t Nn, int nw, int nb, int nwv, int nst,
                       const int mesh[3], int L, const double2 *roots, const int *widx,
@@ -34,7 +41,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const double *degk, const int *kposA, const int *Rq, const double *degq,
                       const int *kposB, const double2 *U, const RateParams &rp, const EpiData &ed,
                       double *partial, int nblk_max, int *nblk_used, cudaEvent_t ev_stage_a,
-                      int64_t *launches, LaunchTimer *tA, LaunchTimer *tB);
+                      int64_t *launches, LaunchTimer *tA, LaunchTimer *tB, std::mutex *build_mu,
+                      int chunk_us = 0, const Yield &yield = Yield());
 
 }  // namespace tc
 }  // namespace ephg

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include <cstdio>
 #include <map>
 #include <string>
@@ -12,27 +14,65 @@ namespace ephg {
 
 // Named device buffers that grow on demand and are reused across calls, so a
 // repeated request pays no cudaMalloc.  get() returns 0 or EPHG_ERR_NOMEM (6)
-// and leaves the reason in msg.
+// and leaves the reason in msg: cudaMalloc failed, or growing the cache would
+// take its total past `limit` (the serving loop's share of the HBM budget).
+// Buffers are allocated and freed stream-ordered on `st` (cudaMallocAsync /
+// cudaFreeAsync): unlike cudaMalloc / cudaFree these do not wait for the other
+// streams of the device, so a request that grows its workspace does not stall
+// behind the kernels of other requests running concurrently.
 struct Workspace {
   std::map<std::string, std::pair<void *, size_t>> bufs;
   std::string msg;
+  size_t limit = (size_t)-1;
+  cudaStream_t st = nullptr;
+  // optional reservation hook (the serving loop's HBM budget): asked before the
+  // cache grows by delta > 0 bytes; false refuses the growth (EPHG_ERR_NOMEM).
+  // Growth that then fails to allocate is given back with a negative delta.
+  // release() does not call it: the owner accounts for released bytes.
+  bool (*grow)(void *ctx, int64_t delta) = nullptr;
+  void *grow_ctx = nullptr;
+  size_t total() const {
+    size_t t = 0;
+    for (auto &kv : bufs) t += kv.second.second;
+    return t;
+  }
   int get(const char *name, size_t bytes, void **out) {
     auto it = bufs.find(name);
     if (it != bufs.end() && it->second.second >= bytes) {
       *out = it->second.first;
       return 0;
     }
+    const size_t old_bytes = it != bufs.end() ? it->second.second : 0;
+    const int64_t delta = (int64_t)(bytes ? bytes : 16) - (int64_t)old_bytes;
+    {
+      const size_t want = total() - old_bytes + (bytes ? bytes : 16);
+      if (want > limit) {
+        char b[256];
+        snprintf(b, sizeof b, "workspace %s: %zu bytes in total would exceed the budget of %zu bytes", name, want,
+                 limit);
+        msg = b;
+        return 6;
+      }
+      if (grow && delta > 0 && !grow(grow_ctx, delta)) {
+        char b[256];
+        snprintf(b, sizeof b, "workspace %s: growing by %lld bytes would exceed the HBM budget", name,
+                 (long long)delta);
+        msg = b;
+        return 6;
+      }
+    }
     if (it != bufs.end()) {
-      cudaFree(it->second.first);
+      cudaFreeAsync(it->second.first, st);
       bufs.erase(it);
     }
     void *p = nullptr;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    cudaError_t e = cudaMallocAsync(&p, bytes, st);
     if (e != cudaSuccess) {
       cudaGetLastError();
+      if (grow) grow(grow_ctx, -(int64_t)bytes);   // the old buffer is gone too: give back all
       char b[256];
-      snprintf(b, sizeof b, "cudaMalloc(%s, %zu bytes): %s", name, bytes, cudaGetErrorString(e));
+      snprintf(b, sizeof b, "cudaMallocAsync(%s, %zu bytes): %s", name, bytes, cudaGetErrorString(e));
       msg = b;
       return 6;
     }
@@ -41,7 +81,7 @@ struct Workspace {
     return 0;
   }
   void release() {
-    for (auto &kv : bufs) cudaFree(kv.second.first);
+    for (auto &kv : bufs) cudaFreeAsync(kv.second.first, st);
     bufs.clear();
   }
 };
@@ -53,6 +93,17 @@ int wsget(Workspace &ws, const char *name, size_t count, T **out) {
   *out = (T *)p;
   return rc;
 }
+
+// Cooperative hand-over point of a long request (the serving loop): called
+// between launches; it may drain the caller's stream and block while a
+// smaller request owns the GPU.  A default-constructed hook does nothing.
+struct Yield {
+  void (*fn)(void *) = nullptr;
+  void *ctx = nullptr;
+  void operator()() const {
+    if (fn) fn(ctx);
+  }
+};
 
 // Device-time accumulator for a family of kernel launches: mark() before and
 // after each launch on the launching stream, total_ms() after a stream sync.

@@ -153,6 +153,58 @@ int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus,
                   double *xminus, int64_t cap);
 
+/* ---- Serving loop ----
+ * No counterpart in the reference, which answers one request per run from
+ * disk; this is the scope's serving form.  A server keeps the crystals of
+ * `crystals` (handles of ephg_create, on one device, which must outlive it and
+ * must not be used directly while it runs) resident and answers RTA-rate
+ * requests as they arrive, by continuous batching: it owns nslots execution
+ * slots (a stream, a request workspace and timers each); a free slot takes the
+ * oldest waiting request at once, and the requests of different slots run
+ * concurrently on the device.  A served result equals the same request run
+ * alone (ephg_el_rates).  Admission is by an HBM budget covering the crystals'
+ * resident data and the slots' workspaces, an equal share per slot:
+ * ephg_submit refuses (EPHG_ERR_NOMEM) a request whose set-up arrays alone
+ * cannot fit; a request that does not fit its slot's share waits for the other
+ * slots to go idle (no new request starts meanwhile), takes the whole budget,
+ * and fails with EPHG_ERR_NOMEM before allocating only if that is still too
+ * little.  A free slot takes the waiting request of least estimated work (the
+ * oldest once it has waited a second); a request much smaller than a running
+ * one runs on a high-priority stream, and served requests run their persistent
+ * kernels as launches of a few ms so that it gets the SMs at the next launch
+ * boundary.  Latency is the wall time from ephg_submit to completion. */
+typedef struct ephg_server ephg_server;
+
+#define EPHG_TICKET_QUEUED 0
+#define EPHG_TICKET_RUNNING 1
+#define EPHG_TICKET_DONE 2
+#define EPHG_TICKET_FAILED 3
+
+typedef struct {
+  int64_t submitted, completed, failed, rejected;
+  int64_t vertices;             /* |g|^2 vertices of the completed requests */
+  double p50_ms, p99_ms, max_ms, mean_ms;   /* submit -> completion, completed requests (nearest rank) */
+  double wall_s;                /* first submit -> last completion */
+  double vertices_per_s;        /* vertices / wall_s */
+  int64_t peak_device_bytes;    /* largest resident + workspace total seen after a request */
+} ephg_server_stats;
+
+int ephg_server_create(ephg_handle *const *crystals, int ncrystals, int64_t hbm_budget_bytes, int nslots,
+                       ephg_server **out);
+/* Stops the worker after the running request; queued requests fail. */
+int ephg_server_destroy(ephg_server *s);
+/* Queue a request for crystal index `crystal`; returns at once with a ticket. */
+int ephg_submit(ephg_server *s, int crystal, const ephg_rate_request *req, int64_t *ticket);
+/* Non-blocking: *state = EPHG_TICKET_QUEUED / RUNNING / DONE / FAILED. */
+int ephg_poll(ephg_server *s, int64_t ticket, int *state);
+/* Block until the ticket completes, then copy its results (buffers sized as
+ * for ephg_el_rates: rates (N,nw), indexlist (N), N = mesh points) and its
+ * latency (submit -> completion, ms), and retire the ticket; any output may
+ * be NULL.  Returns the request's status. */
+int ephg_wait(ephg_server *s, int64_t ticket, double *rates, int64_t *indexlist, ephg_rate_stats *stats,
+              double *latency_ms);
+int ephg_server_stats_get(ephg_server *s, ephg_server_stats *out);
+
 /* el_wann without any device allocation.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory where they need the
  * electrons -- a host code handing over buffers it already owns on the device

@@ -9,6 +9,8 @@
 #define EPHG_DEBUG_H
 #include <stdint.h>
 
+#include "ephg.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -19,6 +21,18 @@ extern "C" {
 int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A, const double *B, double *C);
 /* message of the last failure of the hook */
 const char *ephg_debug_last_error(void);
+
+/* The serving loop's slots, queue, admission, GPU hand-over and statistics run
+ * against a simulated executor (no GPU): two crystals of 1000 resident bytes
+ * each; request i for crystal i % 2 with a cubic mesh meshes[i] needs
+ * per_request_bytes * mesh^3 / 1000 bytes and service_ms * (mesh / 8)^3 of
+ * simulated device time in four parts with yield points between them; request
+ * 0 is submitted 0.2 ms before the others.  Fills *out with the server's
+ * statistics, *max_concurrent with the most requests seen in flight at once
+ * and lat_ms[i] (nullable) with each request's latency (-1: refused or
+ * failed); returns EPHG_ERR_INDEX if a result reached the wrong ticket. */
+int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t budget, int64_t per_request_bytes,
+                               const int64_t *meshes, ephg_server_stats *out, int *max_concurrent, double *lat_ms);
 
 #ifdef __cplusplus
 }
