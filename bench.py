@@ -264,6 +264,13 @@ def run_ours(args, ws, rank, local):
     peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
     tpg = traffic_per_gflop()
     cpu = cpu_sample(wd, req)
+    serving = None
+    if not args.no_serving and ws == 1:   # the metric's p99 latency: the serving loop under a Poisson stream
+        try:
+            from elphbolt_gb300 import serve_bench
+            serving = serve_bench.measure(wds=serve_bench.make_crystals(base=wd))
+        except Exception as e:   # the main line is still printed
+            serving = {"error": repr(e)}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (3xTF32 contractions) + f64 (eigensolves, sums)",
@@ -290,6 +297,8 @@ def run_ours(args, ws, rank, local):
                          "gemm_a": st["ms_gemm_a"], "gemm_b": st["ms_gemm_b"]},
             "wall_s": wall,
             "clocks": clk.summary()}
+    if serving is not None:
+        line["serving"] = serving
     print(json.dumps(line), flush=True)
     return 0
 
@@ -357,6 +366,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop (p50 / p99 latency) measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1 and args.impl == "ours":

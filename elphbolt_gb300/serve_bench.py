@@ -26,9 +26,10 @@ import numpy as np
 MESH_RANGE = {0: (8, 24), 1: (8, 24), 2: (8, 16)}
 
 
-def make_crystals():
+def make_crystals(base=None):
+    """The three resident crystals; `base` may supply the nw = 8 bench crystal already built."""
     from . import synthetic as S
-    return [S.si_like(nw=8),
+    return [base if base is not None else S.si_like(nw=8),
             S.make_wannier(S.make_crystal_si_like(), 16, supercell=(4, 4, 4), seed=20260116),
             S.make_wannier(S.make_crystal_si_like(), 32, supercell=(4, 4, 4), seed=20260132)]
 
