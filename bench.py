@@ -165,6 +165,45 @@ def cpu_sample(wd, req, seconds_target=20.0, states=None):
                 nstates_total=a["nstates_inwindow"])
 
 
+def cpu_sample_ph(wd, req, seconds_target=10.0):
+    """The CPU oracle's phonon side (ibzq loop: gReq per q, literal 'el' g2 per
+    vertex) on a bounded sample of q-points."""
+    from oracle import oracle as O
+    ncores = os.cpu_count() or 1
+    R = O.RatesRun(O.Wannier(wd), req, nthreads=ncores)
+    a = R.run_ph(1, 1)                     # calibrate on one q (not Gamma)
+    per_q_s = max(a["us_loop"] * 1e-6, 1e-3)
+    n = max(1, min(64, int(seconds_target / per_q_s)))
+    b = R.run_ph(2, n)
+    R.close()
+    t = b["us_loop"] * 1e-6
+    return dict(value=b["vertices"] / t, cores=ncores, qpoints=n, vertices=b["vertices"], seconds=t)
+
+
+def phonon_side(W, req, steps, el_ms, fp64_el_ms):
+    """ephg_ph_rates on the bench request: both sides in one sweep (split), its
+    cost over the electron side alone, and its phonon rates against the FP64 form."""
+    import numpy as np
+    from elphbolt_gb300 import _lib
+    ms = []
+    for _ in range(max(3, steps)):
+        s = W.ph_rates(req, precision=_lib.PREC_SPLIT_TF32, electrons=True)
+        ms.append(s["stats"]["ms_total"])
+    f = W.ph_rates(req, precision=_lib.PREC_FP64, electrons=True)
+    v = s["stats"]["vertices"]
+    t = float(np.median(ms))
+    ref = f["rates_phe"]
+    m = ref > 0
+    err = float(np.max(np.abs(s["rates_phe"][m] - ref[m]) / ref[m])) if m.any() else None
+    return {"value": v / (t * 1e-3), "unit": UNIT, "ms_per_step": t,
+            "el_only_ms_per_step": el_ms, "added_ms": t - el_ms,
+            "fp64_ms_per_step": f["stats"]["ms_total"], "fp64_el_only_ms_per_step": fp64_el_ms,
+            "split_speedup_vs_fp64": f["stats"]["ms_total"] / t,
+            "rates_phe_max_rel_vs_fp64": err, "rates_phe_positive": int(m.sum()), "rates_phe_size": int(ref.size),
+            "what": "ephg_ph_rates: ibzq 'g' + 'Y' + ph-e RTA rates (every q of the mesh x nb) and the electron "
+                    "rates of the same vertices in one sweep; value = vertices/s of that sweep"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -255,6 +294,7 @@ def run_ours(args, ws, rank, local):
     ref = f["rates"]
     mask = ref > 0
     rate_err = float(np.max(np.abs(split_rates[mask] - ref[mask]) / ref[mask])) if mask.any() else None
+    ph = phonon_side(W, req, args.steps, float(np.median(dev_ms)), fst["ms_total"]) if rank == 0 else None
     W.deallocate_wannier()
     if rank != 0:
         return 0
@@ -264,6 +304,11 @@ def run_ours(args, ws, rank, local):
     peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
     tpg = traffic_per_gflop()
     cpu = cpu_sample(wd, req)
+    cpu_ph = cpu_sample_ph(wd, req)
+    ph["cpu_baseline"] = {"value": cpu_ph["value"], "unit": UNIT, "cores": cpu_ph["cores"], "kind": "port",
+                          "sample": "%d q-points x %d branches, %d vertices in %.1f s (gReq per q, literal 'el' "
+                                    "g2 per vertex, OpenMP over k within each q)" % (cpu_ph["qpoints"], wd.numbranches,
+                                                                       cpu_ph["vertices"], cpu_ph["seconds"])}
     serving = None
     if not args.no_serving and ws == 1:   # the metric's p99 latency: the serving loop under a Poisson stream
         try:
@@ -297,6 +342,7 @@ def run_ours(args, ws, rank, local):
                          "gemm_a": st["ms_gemm_a"], "gemm_b": st["ms_gemm_b"]},
             "wall_s": wall,
             "clocks": clk.summary()}
+    line["phonon_side"] = ph
     if serving is not None:
         line["serving"] = serving
     print(json.dumps(line), flush=True)

@@ -613,8 +613,9 @@ static int check_err_view(const ExecView &x) {
 
 int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
                         int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus,
-                        int64_t cap) {
-  if (!h || !req || !rates || !indexlist) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
+                        int64_t cap, const PhOut *ph) {
+  if (!h || !req || (!ph && (!rates || !indexlist)) || (ph && !ph->rates_phe))
+    return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   for (int i = 0; i < 3; ++i)
     if (req->mesh[i] <= 0) return fail(EPHG_ERR_ARG, "el_rates: bad mesh");
   if (req->delta_kind < 0 || req->delta_kind > 2) return fail(EPHG_ERR_ARG, "el_rates: bad delta_kind");
@@ -766,17 +767,28 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   ed.uf = uf;
   ed.bose = bose;
   ed.per_state = (int64_t)nin * nb;
-  double *g2d = nullptr, *xpd = nullptr, *xmd = nullptr;
+  double *g2d = nullptr, *xpd = nullptr, *xmd = nullptr, *yd = nullptr, *phr = nullptr;
   int64_t vtot = (int64_t)nst * nin * nb;
   int64_t vcap = std::min<int64_t>(cap, vtot);
-  if (g2 && vcap > 0) {
+  const bool want_y = ph && ph->y;
+  const bool lists = (g2 || want_y) && vcap > 0;
+  if (lists) {
     if ((rc = wsget((*x.ws), "r_vg2", (size_t)vcap, &g2d)) || (rc = wsget((*x.ws), "r_vxp", (size_t)vcap, &xpd)) ||
-        (rc = wsget((*x.ws), "r_vxm", (size_t)vcap, &xmd)))
+        (rc = wsget((*x.ws), "r_vxm", (size_t)vcap, &xmd)) ||
+        (want_y && (rc = wsget((*x.ws), "r_vy", (size_t)vcap, &yd))))
       return WSFAILX(rc);
     ed.g2 = g2d;
     ed.xp = xpd;
     ed.xm = xmd;
+    ed.yv = yd;
     ed.cap = vcap;
+  }
+  if (ph) {
+    // the phonon states' rates, summed by the epilogues' atomics (ibzq 'Y' + ph-e rates)
+    if ((rc = wsget((*x.ws), "r_phr", (size_t)N * nb, &phr))) return WSFAILX(rc);
+    CK(cudaMemsetAsync(phr, 0, (size_t)N * nb * sizeof(double), st));
+    ed.phr = phr;
+    ed.ph_scale = ph->spindeg;
   }
   int nblk = (nwv + 127) / 128;                 // k'-row blocks of the rate partials
   const int nblk_max = std::max((nwv + 15) / 16, (nwv + 255) / 256 * 8);
@@ -830,13 +842,16 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   launch_rate_final(nst, nblk, partial, st_code, nw, N, rates_d, st);
   (*x.launches) += 1;
   CK(cudaEventRecord(ev.e[3], st));
-  CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (rates) CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (ph) CK(cudaMemcpyAsync(ph->rates_phe, phr, (size_t)N * nb * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  for (int i = 0; i < nwv; ++i) indexlist[i] = (int64_t)widx_h[i] + 1;
-  if (g2 && vcap > 0) {
-    CK(cudaMemcpyAsync(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (xplus) CK(cudaMemcpyAsync(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (xminus) CK(cudaMemcpyAsync(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (indexlist)
+    for (int i = 0; i < nwv; ++i) indexlist[i] = (int64_t)widx_h[i] + 1;
+  if (lists) {
+    if (g2) CK(cudaMemcpyAsync(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (g2 && xplus) CK(cudaMemcpyAsync(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (g2 && xminus) CK(cudaMemcpyAsync(xminus, xmd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (want_y) CK(cudaMemcpyAsync(ph->y, yd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
   if ((rc = check_err_view(x))) return rc;
@@ -872,4 +887,15 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   if (!h) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
   return el_rates_view(h, x, req, rates, indexlist, stats, g2, xplus, xminus, cap);
+}
+
+extern "C" int ephg_ph_rates(ephg_handle *h, const ephg_rate_request *req, int64_t spindeg, double *rates_phe,
+                             double *el_rates, int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *y,
+                             int64_t cap) {
+  if (!h || !rates_phe) return fail(EPHG_ERR_ARG, "ph_rates: bad arguments");
+  // "spindeg can be 1 or 2.", electron.f90:164-166
+  if (spindeg < 1 || spindeg > 2) return fail(EPHG_ERR_ARG, "ph_rates: spindeg must be 1 or 2");
+  const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
+  const PhOut ph{rates_phe, y, (double)spindeg};
+  return el_rates_view(h, x, req, el_rates, indexlist, stats, g2, nullptr, nullptr, cap, &ph);
 }

@@ -55,8 +55,18 @@ struct ExecView {
   int chunk_us = 0;   // > 0: persistent kernels run as launches of about this length (serving)
   Yield yield;        // called between chunks and stages (serving); no-op by default
 };
+// The phonon side of a rate request (ephg_ph_rates): the ph-e rates (N, nb) and
+// the optional per-vertex Y list, formed in the same sweep as the electron side.
+struct PhOut {
+  double *rates_phe;
+  double *y;
+  double spindeg;
+};
+// ph == nullptr: the electron side only (ephg_el_rates); otherwise rates and
+// indexlist may be NULL.
 int el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
-                  int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus, int64_t cap);
+                  int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus, int64_t cap,
+                  const PhOut *ph = nullptr);
 // record a failure message for ephg_last_error() and return code
 int api_fail(int code, const char *fmt, ...);
 // read, clear and translate the handle's device error word

@@ -107,6 +107,11 @@ struct EpiData {
   int64_t per_state;    // vertices per initial state
   double *g2, *xp, *xm; // optional vertex lists
   int64_t cap;
+  // phonon side (ibzq 'Y' + the ph-e rates), both nullable: phr (N, nb)
+  // column-major receives ph_scale * Y summed over the vertices of each (q, s)
+  // (device atomics); yv is the optional per-vertex Y list in the order of g2
+  double *phr, *yv;
+  double ph_scale;      // el%spindeg
 };
 // per (k', state) epilogue on an FP64 C chunk: rates partial sums [j][iblk]
 void launch_epilogue_fp64(int nwv, int j0, int j1, const double2 *C, int64_t ldc,

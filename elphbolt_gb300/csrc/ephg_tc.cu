@@ -673,6 +673,29 @@ __global__ void k_to_f2(int64_t n, const double2 *a, float2 *b) {
   if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
+// Occupation factor of the phonon-side Y, f(x) (1 - f(x + y)) / (1 + n(y)) with
+// x = (E - mu)/kT, y = omega/kT (interactions.f90:1838-1839, 1866), in FP32
+// from exponentials taken in FP64: 1 - f(x + y) = 1 / (1 + e^-x e^-y),
+// 1 / (1 + n) = 1 - e^-y and e^-y = n / (1 + n).  No exponent argument is
+// rounded to FP32, so the exponentially small tails away from mu keep their
+// relative accuracy.  YOcc holds the per-state part.
+struct YOcc {
+  float f1;    // f(x)
+  float emx;   // e^-x, finite
+};
+__device__ __forceinline__ YOcc y_occ(double E, double chempot, double kT) {
+  const double ex = exp(-(E - chempot) / kT);
+  YOcc o;
+  o.f1 = (float)(1.0 / (1.0 + 1.0 / ex));
+  o.emx = (float)fmin(ex, 3.0e38);
+  return o;
+}
+// Y / (|g|^2 cx delta) of one vertex, bose = n(y): f1 * ib / (1 + emx e^-y)
+__device__ __forceinline__ float y_factor(const YOcc &o, float bose) {
+  const float ib = 1.0f / (1.0f + bose);
+  return o.f1 * ib / (1.0f + o.emx * (bose * ib));
+}
+
 // One thread per (k', initial state): G(n',s') from the FP32 GEMM output, the
 // U_k' and phonon rotations in FP32, the Gaussian delta and occupations from
 // FP64 energy differences scaled to O(1) before rounding, X+- and the pair sum.
@@ -696,6 +719,8 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
     const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
                         rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
     const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    const bool ph = d.phr || d.yv;
+    const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
     float acc = 0.0f;
     int rank_n = 0;
     for (int n = 0; n < nw; ++n) {
@@ -725,6 +750,9 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
         const float xp = g2c * (qt.bose[qs] + fp) * dp;
         const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
         acc += xp + xm;
+        // Y: the Gaussian is even, so delta(E' - omega - E) is dp
+        const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
+        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
         if (d.g2) {
           int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
           if (off < d.cap) {
@@ -732,6 +760,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
             d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
             d.xp[off] = xp;
             d.xm[off] = xm;
+            if (d.yv) d.yv[off] = y;
           }
         }
       }
@@ -807,6 +836,8 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
       const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
                           rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
       const float *gr = sr + row * ld, *gi = si + row * ld;
+      const bool ph = d.phr || d.yv;
+      const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
       float acc = 0.0f;
       int rank_n = 0;
       for (int n = 0; n < nw; ++n) {
@@ -845,6 +876,8 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
           const float xp = g2c * (qt.bose[qs] + fp) * dp;
           const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
           acc += xp + xm;
+          const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
+          if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
           if (d.g2) {
             int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
             if (off < d.cap) {
@@ -852,6 +885,7 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
               d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
               d.xp[off] = xp;
               d.xm[off] = xm;
+              if (d.yv) d.yv[off] = y;
             }
           }
         }
@@ -903,6 +937,7 @@ struct StateRec {      // per initial state j
   double E;            // eV
   float a_occ;         // (E - mu) / kT
   int apack;           // mesh coordinates of k: a1 | a2 << 10 | a3 << 20
+  YOcc yo;             // per-state part of the phonon-side occupation factor
 };
 
 // The row and q tables are blocked by 32: entry (i, field) sits at
@@ -967,6 +1002,7 @@ __global__ void k_fused_states(int nst, const int *st_code, const int *widx, con
   StateRec r;
   r.E = ens[(size_t)p * 8 + (code & 7)];
   r.a_occ = (float)((r.E - chempot) / kT);
+  r.yo = y_occ(r.E, chempot, kT);
   const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
   r.apack = a1 | (a2 << 10) | (a3 << 20);
   out[j] = r;
@@ -1029,9 +1065,14 @@ __device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const 
 }
 
 // the six vertices (s) of one (k', n) final state for one initial state; returns X+ + X-
-// rec = the lane's entry of field 0 of q's block: fields 32 float4 apart
+// rec = the lane's entry of field 0 of q's block: fields 32 float4 apart.
+// PH: also ys[s] += |g|^2 cx delta, the n-dependent part of Y; its occupation
+// factor depends on the initial state and the mode only and is applied once per
+// pair (y_factor).
+template <bool PH>
 __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ,
-                                                float dnorm, const EpiData &d, int64_t voff, int q) {
+                                                float dnorm, const EpiData &d, int64_t voff, int q,
+                                                const YOcc &yo, float *ys) {
   float acc = 0.f;
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
@@ -1053,6 +1094,7 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
     const float xp = g2c * (sc.y + fp) * dp;
     const float xm = g2c * (1.0f + sc.y - fm) * dm;
     acc += xp + xm;
+    if (PH) ys[s] = fmaf(g2c, dp, ys[s]);   // the Gaussian is even: delta(E' - omega - E) is dp
     if (d.g2) {
       const int64_t off = voff + s;
       if (off < d.cap) {
@@ -1060,12 +1102,15 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
         d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
         d.xp[off] = xp;
         d.xm[off] = xm;
+        if (PH && d.yv) d.yv[off] = (g2c * dp) * y_factor(yo, sc.y);
       }
     }
   }
   return acc;
 }
 
+// PH: the phonon side too (Y of every vertex into the ph-e rate of its (q, s)).
+template <bool PH>
 __global__ void __launch_bounds__(F_THREADS, 1)
     k_stageB_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedArgs g,
                      FusedTabs tb, RateParams rp, EpiData d) {
@@ -1192,10 +1237,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       int q = 0;
       double E = 0.0;
       float a_occ = 0.f;
+      YOcc yo{0.f, 0.f};
       if (jvalid) {
         const StateRec sr = tb.state[j];
         E = sr.E;
         a_occ = sr.a_occ;
+        yo = sr.yo;
         wmask = (unsigned)ri.y;
         const int a1 = sr.apack & 1023, a2 = (sr.apack >> 10) & 1023, a3 = sr.apack >> 20;
         const int b1 = ri.w & 1023, b2 = (ri.w >> 10) & 1023, b3 = ri.w >> 20;
@@ -1213,6 +1260,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       if (nbw > 1) load_urow(ub, n1, u1);
       const int64_t vbase = (nbw > 0 && d.g2) ? (int64_t)j * d.per_state + (int64_t)ri.z * 6 : 0;
       float acc = 0.f;
+      float ys[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (!mbar_wait(tfull, it & 1, g.err)) break;
       tc_fence_after();
       // ---- drain: h for the first two window bands
@@ -1244,7 +1292,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           }
           if (mine) {
             const float dn = (float)((E - __ldg(eb + nb_ * 32)) * inv_sig);
-            acc += fused_vertices(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q);
+            acc += fused_vertices<PH>(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys);
           }
         }
       }
@@ -1254,15 +1302,22 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       float acc01 = 0.f;
       if (nbw > 0) {
         const float dn = (float)((E - __ldg(eb + n0 * 32)) * inv_sig);
-        acc01 += fused_vertices(h0, rq, dn, a_occ, dnorm, d, vbase, q);
+        acc01 += fused_vertices<PH>(h0, rq, dn, a_occ, dnorm, d, vbase, q, yo, ys);
       }
       if (nbw > 1) {
         const float dn = (float)((E - __ldg(eb + n1 * 32)) * inv_sig);
-        acc01 += fused_vertices(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q);
+        acc01 += fused_vertices<PH>(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q, yo, ys);
       }
       double v = (double)acc01 + (double)acc;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0 && jvalid) g.partial[(size_t)j * g.nblk + mt * 4 + quad] = v;
+      if (PH && jvalid && nbw > 0 && d.phr) {   // this pair's Y into the rates of (q, s), s = 0..5
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+          const float y = ys[s] * y_factor(yo, __ldg(rq + (4 * s + 3) * 32).y);
+          if (y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+        }
+      }
     }
   }
   __syncthreads();
@@ -1318,8 +1373,10 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   // once per process: changing a kernel attribute can wait for the device's queued work
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(k_stageB_fused86, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
   });
+  const bool ph = ed.phr || ed.yv;
   FusedArgs g;
   g.mtiles = MpB / BM;
   g.ntiles = (nst + 1) / 2;
@@ -1335,11 +1392,18 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   if (g.mtiles % 2) return tfail(1, "stage B: row tiles must pair");
   const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
   if (pairs > INT32_MAX) return tfail(1, "stage B: too many tiles");
-  return launch_pairs((const void *)k_stageB_fused86, F_SMEM, pairs, st, chunk, yield,
+  if (ph)
+    return launch_pairs((const void *)k_stageB_fused86<true>, F_SMEM, pairs, st, chunk, yield,
+                        [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
+                          g.t0 = t0;
+                          g.t1 = t1;
+                          return cudaLaunchKernelEx(&cfg, k_stageB_fused86<true>, ta, tb, g, tabs, rp, ed);
+                        });
+  return launch_pairs((const void *)k_stageB_fused86<false>, F_SMEM, pairs, st, chunk, yield,
                       [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
                         g.t0 = t0;
                         g.t1 = t1;
-                        return cudaLaunchKernelEx(&cfg, k_stageB_fused86, ta, tb, g, tabs, rp, ed);
+                        return cudaLaunchKernelEx(&cfg, k_stageB_fused86<false>, ta, tb, g, tabs, rp, ed);
                       });
 }
 

@@ -37,6 +37,19 @@ def _p(a, t=c_dp):
     return a.ctypes.data_as(t) if a is not None else None
 
 
+def _vecs(a, what, n=None):
+    """Wave vectors (n, 3) in crystal coordinates as a column-major float64
+    array; refuses a missing or misshaped array (the library reads n x 3)."""
+    if a is None:
+        raise ValueError("%s: wave vectors missing" % what)
+    v = _f(np.atleast_2d(a))
+    if v.ndim != 2 or v.shape[1] != 3:
+        raise ValueError("%s: wave vectors must be (n, 3), got %s" % (what, v.shape))
+    if n is not None and int(n) > v.shape[0]:
+        raise ValueError("%s: %d wave vectors requested, %d given" % (what, int(n), v.shape[0]))
+    return v
+
+
 class Wannier:
     """Wannier data resident on the GPU behind one library handle."""
 
@@ -72,7 +85,7 @@ class Wannier:
     # ---- wannier.f90:430 ----
     def el_wann(self, crys=None, nk=None, kvecs=None, velocities=False, evecs=False, scissor=None):
         """Energies (nk,nw) eV [, velocities (nk,nw,3) km/s] [, evecs (nk,nw,nw)]."""
-        k = _f(np.atleast_2d(kvecs))
+        k = _vecs(kvecs, "el_wann", nk)
         nk = k.shape[0] if nk is None else int(nk)
         nw = self.numwannbands
         e = np.zeros((nk, nw), order="F")
@@ -90,7 +103,7 @@ class Wannier:
     # ---- wannier.f90:585 ----
     def ph_wann(self, crys=None, nq=None, qvecs=None, evecs=False, velocities=False):
         """Energies (nq,nb) eV [, evecs (nq,nb,nb)] [, velocities (nq,nb,3) km/s]."""
-        q = _f(np.atleast_2d(qvecs))
+        q = _vecs(qvecs, "ph_wann", nq)
         nq = q.shape[0] if nq is None else int(nq)
         nb = self.numbranches
         e = np.zeros((nq, nb), order="F")
@@ -107,7 +120,7 @@ class Wannier:
     # ---- wannier.f90:1073 ----
     def gkRp(self, num=None, ik=None, kvec=None):
         """g(k,Rp) = gmixed(nw,nw,nb,nwsq) for one k, or (...,nk) for kvec (nk,3)."""
-        k = _f(np.atleast_2d(kvec))
+        k = _vecs(kvec, "gkRp")
         nk = k.shape[0]
         nw, nb = self.numwannbands, self.numbranches
         out = np.zeros((nw, nw, nb, self.nwsq, nk), dtype=np.complex128, order="F")
@@ -117,7 +130,7 @@ class Wannier:
     # ---- wannier.f90:1134 ----
     def gReq(self, num=None, iq=None, qvec=None):
         """g(Re,q) = gmixed(nw,nw,nb,nwsk) for one q, or (...,nq)."""
-        q = _f(np.atleast_2d(qvec))
+        q = _vecs(qvec, "gReq")
         nq = q.shape[0]
         nw, nb = self.numwannbands, self.numbranches
         out = np.zeros((nw, nw, nb, self.nwsk, nq), dtype=np.complex128, order="F")
@@ -131,7 +144,7 @@ class Wannier:
         ws = {"ph": _lib.WANNSPACE_PH, "el": _lib.WANNSPACE_EL}.get(wannspace)
         if ws is None:
             raise _lib.EphgError(_lib.EPHG_ERR_ARG, "Invalid value of wannspace in call to g2_epw. Exiting.")
-        kv, qv = _f(np.atleast_2d(kvecs)), _f(np.atleast_2d(qvecs))
+        kv, qv = _vecs(kvecs, "g2"), _vecs(qvecs, "g2")
         nv = qv.shape[0]
         a = _f(np.atleast_2d(el_evec_k), np.complex128)
         b = _f(np.atleast_2d(el_evec_kp), np.complex128)
@@ -141,6 +154,10 @@ class Wannier:
         if gm.ndim == 4:
             gm = gm[..., None]
         gi = np.ascontiguousarray(np.atleast_1d(gm_index), dtype=np.int64)
+        nw, nb = self.numwannbands, self.numbranches
+        if (kv.shape[0] != nv or a.shape != (nv, nw) or b.shape != (nv, nw) or c.shape != (nv, nb)
+                or en.shape != (nv,) or gi.shape != (nv,) or gm.shape[:4] != (nw, nw, nb, gm.shape[3])):
+            raise ValueError("g2_batch: inconsistent shapes for %d vertices" % nv)
         out = np.zeros(nv)
         check(self._L.ephg_g2(self._h, ws, nv, _p(kv), _p(qv), _p(a), _p(b), _p(c), _p(en),
                               gm.shape[-1], _p(gm), _p(gi, c_i64p), _p(out)))
@@ -185,6 +202,41 @@ class Wannier:
         if vertices:
             nv = min(int(st.vertices), c)
             out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
+        return out
+
+    def ph_rates(self, req, precision=_lib.PREC_FP64, spindeg=2, electrons=False, vertices=False, cap=None):
+        """Fused ibzq 'g' + 'Y' + ph-e RTA rates (``ephg_ph_rates``).
+
+        Returns rates_phe (N, nb) in THz, row iq - 1 = the phonon of muxed q index
+        iq; with ``electrons`` also the electron rates and window index list of
+        the same sweep; with ``vertices`` the |g|^2 and Y lists in the electron
+        side's vertex order (``interactions.ibzq_order`` maps them to the
+        reference's phonon order)."""
+        r = _lib.RateRequest()
+        for i in range(3):
+            r.mesh[i] = int(req.mesh[i])
+        r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+        r.delta_kind, r.sigma, r.precision = int(req.delta_kind), float(req.sigma), int(precision)
+        N = int(np.prod(req.mesh))
+        nw, nb = self.numwannbands, self.numbranches
+        rph = np.zeros((N, nb), order="F")
+        rates = np.zeros((N, nw), order="F") if electrons else None
+        idx = np.zeros(N, dtype=np.int64) if electrons else None
+        st = _lib.RateStats()
+        g2 = y = None
+        c = 0
+        if vertices:
+            c = int(cap) if cap is not None else N * nw * N * nw * nb
+            g2, y = np.zeros(c), np.zeros(c)
+        check(self._L.ephg_ph_rates(self._h, ct.byref(r), int(spindeg), _p(rph), _p(rates), _p(idx, c_i64p),
+                                    ct.byref(st), _p(g2), _p(y), c))
+        nwv = int(st.nwv)
+        out = dict(nwv=nwv, rates_phe=rph, stats=st.as_dict(), vertices=int(st.vertices))
+        if electrons:
+            out.update(indexlist=idx[:nwv].copy(), rates=np.asfortranarray(rates[:nwv]))
+        if vertices:
+            nv = min(int(st.vertices), c)
+            out.update(g2=g2[:nv], y=y[:nv])
         return out
 
     def deallocate_wannier(self, num=None):

@@ -1,8 +1,8 @@
 /*
  * ephg.h - C ABI of the GB300 (sm_103a) e-ph vertex library.
  *
- * Drop-in for elphbolt's Wannier-interpolation procedures and the electron
- * e-ph rate drivers, callable from Fortran through ISO_C_BINDING (see
+ * Drop-in for elphbolt's Wannier-interpolation procedures and the electron-
+ * and phonon-side e-ph rate drivers, callable from Fortran through ISO_C_BINDING (see
  * INTEGRATION.md for the bind(C) interfaces).  Every entry point names the
  * reference procedure it replaces.
  *
@@ -152,6 +152,22 @@ int ephg_kq_index(ephg_handle *h, const int64_t mesh[3], int64_t nk, const int64
 int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus,
                   double *xminus, int64_t cap);
+
+/* calculate_eph_interaction_ibzq 'g' + 'Y' (interactions.f90:1673-1930, the 'Y'
+ * pass as calculate_Y_OTF :1932-2093) fused with the ph-e part of
+ * calculate_ph_rta_rates (interactions.f90:2723-2828), identity point group,
+ * q mesh = k mesh, no disk.  rates_phe (N_q,nb) column-major: row iq - 1 is
+ * the phonon of muxed q index iq (every q of the mesh: the phonon side has no
+ * window); spindeg is el%spindeg, 1 or 2 (electron.f90:164).  The vertices are
+ * those of ephg_el_rates -- vertex (k, m, k + q, n, s) of phonon state (q, s) is
+ * vertex (k, m, k', n, s) of the electron side with k' = k + q -- so one sweep
+ * forms both sides: el_rates (N_k,nw) and indexlist (N_k), if not NULL,
+ * receive what ephg_el_rates returns.  Optional per-vertex lists in the order
+ * of ephg_el_rates, capacity cap: g2 (eV^2) and y (Y in THz, before the
+ * spindeg factor).  stats may be NULL. */
+int ephg_ph_rates(ephg_handle *h, const ephg_rate_request *req, int64_t spindeg, double *rates_phe,
+                  double *el_rates, int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *y,
+                  int64_t cap);
 
 /* ---- Serving loop ----
  * No counterpart in the reference, which answers one request per run from

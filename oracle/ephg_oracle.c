@@ -1065,3 +1065,161 @@ int or_el_rates(const or_wannier *w, const or_request *req, int64_t max_states,
   or_rates_free(cx);
   return rc;
 }
+
+/*
+ * calculate_eph_interaction_ibzq ('g' then 'Y', interactions.f90:1673-1930; the
+ * 'Y' pass as calculate_Y_OTF, :1932-2093) and the ph-e part of
+ * calculate_ph_rta_rates (interactions.f90:2723-2828), with the identity point
+ * group (the IBZ phonons are all q of the mesh), q mesh = k mesh and no disk.
+ * Per q, g(Re,q) from gReq (calculate_gReq, interactions.f90:1603-1630); per
+ * phonon state (q, s) the loops over window k, k + q (vec_add + binsearch,
+ * :1813-1822), m and n (:1825-1880) with the literal 'el' g2 (:1847-1852),
+ * Y = g2 f(E)(1 - f(E + w)) / (1 + n(w)) delta(E' - w at (k, m)) for w >= 0.5 meV
+ * (:1857-1870), times 2 pi / hbar (:1897), and the rate sum spindeg * Y in
+ * list order (:2811-2813).  Phonon states of q in [q_begin, q_begin + nq).
+ */
+int or_ph_rates_run(or_rates_ctx *cx, int64_t q_begin, int64_t nq, int nthreads, double spindeg,
+                    double *rates_phe, int64_t *info, double *g2out, double *yout, int64_t cap) {
+  const or_wannier *w = cx->w;
+  const or_request *req = &cx->req;
+  const int64_t nw = w->nw, nb = w->nb, nwsk = w->nwsk, nwsg = w->nwsg;
+  const int64_t *mesh = req->mesh;
+  const int64_t N = cx->N, nwv = cx->nwv;
+  const double const_tp = TWOPI / HBAR_EVPS;
+  const double *kw = cx->kw, *ens = cx->ens, *evecs = cx->evecs, *phe = cx->phe, *phv = cx->phv;
+  const int64_t *indexlist = cx->indexlist;
+  const delta_ctx dc = cx->dc;
+  for (int i = 0; i < 8; ++i) info[i] = 0;
+  info[0] = nwv;
+  info[1] = cx->nin;
+  info[5] = cx->status;
+  info[6] = cx->us_setup;
+  for (int64_t i = 0; i < N * nb; ++i) rates_phe[i] = 0.0;
+  if (cx->status == 2) return 2;
+  const int64_t q0 = q_begin < 0 ? 0 : (q_begin > N ? N : q_begin);
+  const int64_t q1 = nq < 0 ? N : (q0 + nq < N ? q0 + nq : N);
+  const int nt = nthreads > 0 ? nthreads : 1;
+  double t_loop = wall_us();
+  int64_t *nin_k = (int64_t *)malloc(sizeof(int64_t) * (nwv > 0 ? nwv : 1));
+  for (int64_t ik = 0; ik < nwv; ++ik) {
+    int64_t c = 0;
+    for (int64_t b = 0; b < nw; ++b) c += fabs(ens[ik + nwv * b] - req->enref) <= req->fsthick;
+    nin_k[ik] = c;
+  }
+  const int64_t blk = nw * nw * nb;
+  double *gm = (double *)malloc(sizeof(double) * 2 * blk * nwsk);   /* gReq(iq) */
+  cplx *phase = (cplx *)malloc(sizeof(cplx) * (nwsg > 0 ? nwsg : 1));
+  int64_t *kpw = (int64_t *)malloc(sizeof(int64_t) * (nwv > 0 ? nwv : 1));
+  int64_t *koff = (int64_t *)malloc(sizeof(int64_t) * (nwv + 1));
+  double *ybuf = (double *)malloc(sizeof(double) * (nwv * nw * nw > 0 ? nwv * nw * nw : 1));
+  double *gbuf = (double *)malloc(sizeof(double) * (nwv * nw * nw > 0 ? nwv * nw * nw : 1));
+  int64_t voff = 0, npairs = 0;
+  for (int64_t iq = q0 + 1; iq <= q1; ++iq) {   /* muxed 1-based = IBZ index (identity group) */
+    const double prim[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    int64_t qi[3];
+    or_demux_vector(iq, qi, mesh, 0);
+    double qf[3];
+    for (int d = 0; d < 3; ++d) qf[d] = (double)qi[d] / (double)mesh[d];
+    /* gReq (wannier.f90:1134-1188), each element summed over Rp in or_gReq's order */
+    for (int64_t iuc = 0; iuc < nwsg; ++iuc) {
+      double dot = 0.0;
+      for (int d = 0; d < 3; ++d) dot += qf[d] * (double)w->rcells_g[iuc + nwsg * d];
+      phase[iuc] = expi(TWOPI * dot) / (double)w->gwsdeg[iuc];
+    }
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int64_t re = 0; re < nwsk; ++re)
+      for (int64_t s = 0; s < nb; ++s)
+        for (int64_t j = 0; j < nw; ++j)
+          for (int64_t i = 0; i < nw; ++i) {
+            cplx acc = 0.0;
+            for (int64_t iuc = 0; iuc < nwsg; ++iuc)
+              acc += phase[iuc] * cget(w->gwann, i + nw * (j + nw * (re + nwsk * (s + nb * iuc))));
+            cset(gm, i + nw * (j + nw * (s + nb * re)), acc);
+          }
+    /* k + q in the window (vec_add + binsearch, interactions.f90:1813-1822) and the
+     * first list position of each k's vertices */
+    koff[0] = 0;
+    for (int64_t ik = 0; ik < nwv; ++ik) {
+      int64_t iv[3], kpmux;
+      double f[3], cc[3];
+      or_vector_addsub(indexlist[ik], iq, +1, mesh, prim, iv, &kpmux, f, cc);
+      const int64_t ikp = or_binsearch(indexlist, nwv, kpmux);
+      kpw[ik] = ikp;
+      npairs += ikp > 0;
+      koff[ik + 1] = koff[ik] + (ikp > 0 ? nin_k[ik] * nin_k[ikp - 1] : 0);
+    }
+    const int64_t count_q = koff[nwv];
+    for (int64_t s = 1; s <= nb; ++s) {
+      const double en_ph = phe[(iq - 1) + N * (s - 1)];
+      double evq[2 * 64];
+      for (int64_t c = 0; c < nb; ++c) {
+        evq[2 * c] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c))];
+        evq[2 * c + 1] = phv[2 * ((iq - 1) + N * ((s - 1) + nb * c)) + 1];
+      }
+      const double invboseplus1 = (en_ph != 0.0) ? 1.0 / (1.0 + or_Bose(en_ph, req->T)) : 0.0;
+#pragma omp parallel num_threads(nt)
+      {
+        double *evk = (double *)malloc(sizeof(double) * 2 * nw);
+        double *evkp = (double *)malloc(sizeof(double) * 2 * nw);
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t ik = 1; ik <= nwv; ++ik) {
+          const int64_t ikp = kpw[ik - 1];
+          if (ikp < 0) continue;
+          const double kv[3] = {kw[ik - 1], kw[(ik - 1) + nwv], kw[(ik - 1) + 2 * nwv]};
+          int64_t count = koff[ik - 1];
+          for (int64_t m = 1; m <= nw; ++m) {
+            const double en_el = ens[(ik - 1) + nwv * (m - 1)];
+            if (fabs(en_el - req->enref) > req->fsthick) continue;
+            const double fermi1 = or_Fermi(en_el, req->chempot, req->T);
+            const double fermi2 = or_Fermi(en_el + en_ph, req->chempot, req->T);
+            for (int64_t c = 0; c < nw; ++c) {
+              evk[2 * c] = evecs[2 * ((ik - 1) + nwv * ((m - 1) + nw * c))];
+              evk[2 * c + 1] = evecs[2 * ((ik - 1) + nwv * ((m - 1) + nw * c)) + 1];
+            }
+            for (int64_t n = 1; n <= nw; ++n) {
+              const double en_elp = ens[(ikp - 1) + nwv * (n - 1)];
+              if (fabs(en_elp - req->enref) > req->fsthick) continue;
+              for (int64_t c = 0; c < nw; ++c) {
+                evkp[2 * c] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c))];
+                evkp[2 * c + 1] = evecs[2 * ((ikp - 1) + nwv * ((n - 1) + nw * c)) + 1];
+              }
+              const double g2 = or_g2(w, kv, qf, evk, evkp, evq, en_ph, gm, 0);
+              const double delta = delta_eval(&dc, en_elp - en_ph, ik, m);
+              const double occup_fac = fermi1 * (1.0 - fermi2) * invboseplus1;
+              double y = 0.0;
+              if (en_ph >= 0.5e-3) y = g2 * occup_fac * delta;
+              gbuf[count] = g2;
+              ybuf[count] = const_tp * y;
+              count++;
+            }
+          }
+        }
+        free(evk); free(evkp);
+      }
+      double acc = 0.0;
+      for (int64_t i = 0; i < count_q; ++i) {
+        acc = acc + spindeg * ybuf[i];
+        if (voff + i < cap) {
+          if (g2out) g2out[voff + i] = gbuf[i];
+          if (yout) yout[voff + i] = ybuf[i];
+        }
+      }
+      rates_phe[(iq - 1) + N * (s - 1)] = acc;
+      voff += count_q;
+    }
+  }
+  info[2] = (q1 - q0) * nb;
+  info[3] = voff;
+  info[4] = npairs;
+  free(nin_k); free(gm); free(phase); free(kpw); free(koff); free(ybuf); free(gbuf);
+  info[7] = (int64_t)(wall_us() - t_loop);
+  return (int)info[5];
+}
+
+int or_ph_rates(const or_wannier *w, const or_request *req, double spindeg, int nthreads,
+                double *rates_phe, int64_t *info, double *g2, double *y, int64_t cap) {
+  or_rates_ctx *cx = or_rates_setup(w, req, nthreads);
+  int rc = or_ph_rates_run(cx, 0, -1, nthreads, spindeg, rates_phe, info, g2, y, cap);
+  or_rates_free(cx);
+  return rc;
+}

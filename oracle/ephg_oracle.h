@@ -13,6 +13,8 @@
  *   gReq                  src/wannier.f90:1134-1188
  *   ibzk 'g' + 'X'        src/interactions.f90:2095-2400
  *   el RTA rates          src/interactions.f90:2958-3063
+ *   ibzq 'g' + 'Y'        src/interactions.f90:1673-1930, 1932-2093
+ *   ph-e RTA rates        src/interactions.f90:2723-2828
  *   triangles / tetra     src/delta.f90:61-225,494-646,648-881
  *   index helpers         src/misc.f90:588-610,738-763,906-1019, src/vector.f90:38-120
  *   window                src/electron.f90:597-636
@@ -144,6 +146,24 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
                  int literal, double *rates, int64_t *indexlist, int64_t *info,
                  double *g2, double *xp, double *xm, int64_t cap);
 void or_rates_free(or_rates_ctx *cx);
+
+/* ---- phonon side: ibzq 'g' + 'Y' + the ph-e RTA rates ----
+ * calculate_eph_interaction_ibzq (interactions.f90:1673-1930), calculate_Y_OTF
+ * (:1932-2093) and the ph-e part of calculate_ph_rta_rates (:2723-2828) with
+ * g(Re,q) from gReq (:1603-1630), identity point group, q mesh = k mesh.
+ * info[0] nwv, [1] window final states, [2] phonon states (q, s) processed,
+ * [3] vertices (the count of :1850), [4] (q, k) pairs with k, k + q in the
+ * window, [5] status, [6] us set-up, [7] us loop.
+ * rates_phe: (N, nb) column-major, row iq - 1 = the q-point of muxed index iq
+ *            (the phonon side has no window: every q of the mesh); rows of q
+ *            outside [q_begin, q_begin + nq) are zero.
+ * g2/y:      optional per-vertex lists in the reference's order (phonon state
+ *            (iq - 1) * nb + s, then k, m, n), capacity cap; y in THz.
+ * spindeg:   el%spindeg (electron.f90), the factor of each Y in the rate sum. */
+int or_ph_rates_run(or_rates_ctx *cx, int64_t q_begin, int64_t nq, int nthreads, double spindeg,
+                    double *rates_phe, int64_t *info, double *g2, double *y, int64_t cap);
+int or_ph_rates(const or_wannier *w, const or_request *req, double spindeg, int nthreads,
+                double *rates_phe, int64_t *info, double *g2, double *y, int64_t cap);
 
 #ifdef __cplusplus
 }

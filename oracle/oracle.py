@@ -190,6 +190,41 @@ class Wannier:
         return out
 
 
+    def ph_rates(self, req, spindeg=2, nthreads=1, vertices=False, cap=None):
+        """ibzq 'g' + 'Y' and the ph-e RTA rates (or_ph_rates); rates_phe (N, nb)."""
+        L = lib()
+        L.or_ph_rates.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_double, ct.c_int, c_dp, c_i64p, c_dp, c_dp,
+                                  ct.c_int64]
+        r = _request(req)
+        N = int(np.prod(req.mesh))
+        rates = np.zeros((N, self.nb), order="F")
+        info = np.zeros(8, dtype=np.int64)
+        g2 = y = None
+        c = 0
+        if vertices:
+            c = int(cap) if cap is not None else N * self.nb * N * self.nw * self.nw
+            g2, y = np.zeros(c), np.zeros(c)
+        st = L.or_ph_rates(ct.byref(self.s), ct.byref(r), float(spindeg), int(nthreads), _p(rates),
+                           _p(info, c_i64p), _p(g2) if g2 is not None else None,
+                           _p(y) if y is not None else None, ct.c_int64(c))
+        out = dict(status=int(st), nwv=int(info[0]), nstates_inwindow=int(info[1]), nstates=int(info[2]),
+                   vertices=int(info[3]), pairs=int(info[4]), rates_phe=rates, us_setup=int(info[6]),
+                   us_loop=int(info[7]))
+        if vertices:
+            nv = min(int(info[3]), c)
+            out.update(g2=g2[:nv], y=y[:nv])
+        return out
+
+
+def _request(req):
+    r = OrRequest()
+    for i in range(3):
+        r.mesh[i] = int(req.mesh[i])
+    r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+    r.delta_kind, r.sigma = int(req.delta_kind), req.sigma
+    return r
+
+
 # ---- misc.f90 / vector.f90 restatements ----
 def mux_vector(v, mesh, base):
     a = (ct.c_int64 * 3)(*v)
@@ -311,6 +346,18 @@ class RatesRun:
         return dict(nwv=nwv, nstates_inwindow=int(info[1]), nstates=int(info[2]), vertices=int(info[3]),
                     status=int(info[5]), us_setup=int(info[6]), us_loop=int(info[7]),
                     rates=np.asfortranarray(rates[:nwv]), indexlist=idx[:nwv].copy())
+
+    def run_ph(self, q_begin, nq, spindeg=2):
+        """Phonon-side states of the q-points [q_begin, q_begin + nq) (or_ph_rates_run)."""
+        L = lib()
+        L.or_ph_rates_run.argtypes = [ct.c_void_p, ct.c_int64, ct.c_int64, ct.c_int, ct.c_double, c_dp, c_i64p,
+                                      c_dp, c_dp, ct.c_int64]
+        rates = np.zeros((self.N, self.W.nb), order="F")
+        info = np.zeros(8, dtype=np.int64)
+        L.or_ph_rates_run(self.ctx, q_begin, nq, self.nthreads, float(spindeg), _p(rates), _p(info, c_i64p),
+                          None, None, 0)
+        return dict(nwv=int(info[0]), nstates=int(info[2]), vertices=int(info[3]), pairs=int(info[4]),
+                    status=int(info[5]), us_setup=int(info[6]), us_loop=int(info[7]), rates_phe=rates)
 
     def close(self):
         if self.ctx:

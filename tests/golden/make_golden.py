@@ -1,6 +1,6 @@
 """Generate the golden fixtures of tests/golden/ (run from the repository root).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [el | ph | all]
 
 For each small seeded workload this script computes the e-ph path twice:
 - with the C oracle (oracle/ephg_oracle.c, literal per-vertex g2);
@@ -131,6 +131,71 @@ def np_rates(wd, req):
                 xp=np.concatenate(xp_all), xm=np.concatenate(xm_all))
 
 
+def np_ph_rates(wd, req, spindeg=2):
+    """ibzq 'g' + 'Y' and the ph-e rates for a Gaussian delta, q-major as the
+    reference walks them: g(Re,q) by an Rp sum (gReq), the 'el' Re sum per k,
+    vertices in the order (q, s, k, m, n)."""
+    mesh = np.asarray(req.mesh)
+    N = int(np.prod(mesh))
+    ks = S.mesh_kvecs(mesh)
+    e_all, _ = np_el_wann(wd, ks)
+    idx = np.nonzero(np.any(np.abs(e_all - req.enref) <= req.fsthick, axis=1))[0]
+    ens, U = np_el_wann(wd, ks[idx])
+    om, V = np_ph_wann(wd, ks)
+    u = V / np.sqrt(np.repeat(wd.crystal.masses, 3))[None, None, :]
+    nw, nb = wd.numwannbands, wd.numbranches
+    pos = -np.ones(N, dtype=np.int64)
+    pos[idx] = np.arange(len(idx))
+    kint = np.stack([idx % mesh[0], (idx // mesh[0]) % mesh[1], idx // (mesh[0] * mesh[1])], 1)
+    g = np.asarray(wd.gwann)                                       # (n', m', Re, s, Rp)
+    phk = np.exp(2j * np.pi * (ks[idx] @ wd.rcells_k.T)) / wd.elwsdeg[None, :]
+    win = np.abs(ens - req.enref) <= req.fsthick
+    kT = C.kB * req.T
+    fermi = lambda e: 1.0 / (np.exp((e - req.chempot) / kT) + 1.0)
+    rates = np.zeros((N, nb))
+    g2_all, y_all = [], []
+    for iq in range(N):
+        qi = np.array([iq % mesh[0], (iq // mesh[0]) % mesh[1], iq // (mesh[0] * mesh[1])])
+        phq = np.exp(2j * np.pi * (wd.rcells_g @ (qi / mesh))) / wd.gwsdeg
+        gReq = np.einsum("p,ijrsp->ijsr", phq, g)                  # (n', m', s, Re)
+        kp = (kint + qi) % mesh
+        ikp_all = pos[kp[:, 0] + mesh[0] * (kp[:, 1] + mesh[1] * kp[:, 2])]
+        g2q, occ_delta = [], []                                    # per vertex: (nb,) arrays
+        o = om[iq]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            invb = np.where(o != 0, 1.0 / (1.0 + 1.0 / np.expm1(np.where(o != 0, o, 1.0) / kT)), 0.0)
+        for ik in range(len(idx)):
+            ikp = ikp_all[ik]
+            if ikp < 0:
+                continue
+            gk = np.einsum("r,ijsr->ijs", phk[ik], gReq)
+            for m in range(nw):
+                if not win[ik, m]:
+                    continue
+                E = ens[ik, m]
+                for n in range(nw):
+                    if not win[ikp, n]:
+                        continue
+                    h = np.einsum("i,ijs,j->s", np.conj(U[ikp, n]), gk, U[ik, m])
+                    gs = u[iq] @ h
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        g2 = np.where(o == 0, 0.0, 0.5 * np.abs(gs) ** 2 / o * C.g2unitfactor)
+                    x = (ens[ikp, n] - o - E) / req.sigma
+                    delta = (1 / math.sqrt(2 * math.pi)) / req.sigma * np.exp(-0.5 * x * x) / N
+                    occ = fermi(E) * (1.0 - fermi(E + o)) * invb
+                    g2q.append(g2)
+                    occ_delta.append(np.where(o >= 0.5e-3, occ * delta, 0.0))
+        if not g2q:
+            continue
+        g2q = np.array(g2q)                                       # (count, nb)
+        yq = g2q * np.array(occ_delta) * (2 * math.pi / C.hbar_eVps)
+        for s in range(nb):
+            g2_all.append(g2q[:, s])
+            y_all.append(yq[:, s])
+            rates[iq, s] = np.sum(spindeg * yq[:, s])
+    return dict(indexlist=idx + 1, rates_phe=rates, g2=np.concatenate(g2_all), y=np.concatenate(y_all))
+
+
 CASES = {
     "tiny": dict(nw=4, supercell=(2, 2, 2), seed=11, mesh=(4, 4, 4), window=1.0, shift=0.3),
     "si8": dict(nw=8, supercell=(3, 3, 3), seed=12, mesh=(4, 4, 4), window=0.5, shift=0.6),
@@ -142,6 +207,27 @@ def build_case(name):
     wd = S.make_wannier(S.make_crystal_si_like(), c["nw"], supercell=c["supercell"], seed=c["seed"])
     req = S.si_like_request(wd, c["mesh"], window=c["window"], shift=c["shift"])
     return wd, req
+
+
+def main_ph():
+    """golden_ph_<case>.npz: the phonon side (ibzq 'g' + 'Y', ph-e rates), spindeg 2."""
+    from oracle import oracle as O
+    for name in CASES:
+        wd, req = build_case(name)
+        ref = np_ph_rates(wd, req, spindeg=2)
+        o = O.Wannier(wd).ph_rates(req, spindeg=2, nthreads=os.cpu_count(), vertices=True)
+        rel = lambda a, b: np.max(np.abs(a - b)) / max(np.abs(b).max(), 1e-300)
+        assert o["vertices"] == len(ref["g2"]), name
+        assert rel(o["g2"], ref["g2"]) < 1e-10, (name, rel(o["g2"], ref["g2"]))
+        assert rel(o["y"], ref["y"]) < 1e-10, (name, rel(o["y"], ref["y"]))
+        assert rel(o["rates_phe"], ref["rates_phe"]) < 1e-10, (name, rel(o["rates_phe"], ref["rates_phe"]))
+        sel = np.arange(0, len(ref["g2"]), 7)
+        np.savez_compressed(os.path.join(HERE, "golden_ph_%s.npz" % name), spindeg=2,
+                            mesh=np.asarray(req.mesh), indexlist=ref["indexlist"], rates_phe=ref["rates_phe"],
+                            vsel=sel, g2=ref["g2"][sel], y=ref["y"][sel], nvert=len(ref["g2"]))
+        print(name, "ph vertices", len(ref["g2"]), "max|rate_phe|", ref["rates_phe"].max(),
+              "oracle-vs-numpy g2 %.2e y %.2e rates %.2e" % (rel(o["g2"], ref["g2"]), rel(o["y"], ref["y"]),
+                                                             rel(o["rates_phe"], ref["rates_phe"])))
 
 
 def main():
@@ -167,4 +253,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    what = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if what in ("el", "all"):
+        main()
+    if what in ("ph", "all"):
+        main_ph()

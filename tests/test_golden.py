@@ -53,6 +53,33 @@ def test_oracle_reproduces_golden(oracle_lib, name):
     assert np.max(np.abs(om - z["om"])) < 1e-10
 
 
+def load_ph(name):
+    return np.load(os.path.join(HERE, "golden_ph_%s.npz" % name))
+
+
+def check_ph(rates_phe, g2, y, z, rel, absfrac, g2_rel, g2_absfrac):
+    """Phonon side: ph-e rates per element within rel (plus absfrac of the
+    largest, for the split form's FP32 floor), and the |g|^2 / Y vertex
+    sample in the reference's phonon order."""
+    rz = z["rates_phe"]
+    assert np.all(np.abs(rates_phe - rz) <= rel * rz + absfrac * rz.max()), \
+        np.max(np.abs(rates_phe - rz) / np.maximum(rz, 1e-300))
+    if g2 is not None:
+        s = z["vsel"]
+        assert np.all(np.abs(g2[s] - z["g2"]) <= g2_rel * np.abs(z["g2"]) + g2_absfrac * np.abs(z["g2"]).max())
+        assert np.all(np.abs(y[s] - z["y"]) <= g2_rel * np.abs(z["y"]) + g2_absfrac * np.abs(z["y"]).max())
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_oracle_reproduces_golden_ph(oracle_lib, name):
+    """The oracle's ibzq 'g' + 'Y' + ph-e rates against the numpy restatement's fixtures."""
+    wd, req, _ = load(name)
+    z = load_ph(name)
+    out = oracle_lib.Wannier(wd).ph_rates(req, spindeg=int(z["spindeg"]), nthreads=4, vertices=True)
+    assert out["vertices"] == int(z["nvert"])
+    check_ph(out["rates_phe"], out["g2"], out["y"], z, 1e-10, 0.0, 1e-10, 1e-12)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("prec", [_lib.PREC_FP64, _lib.PREC_SPLIT_TF32])
@@ -70,3 +97,35 @@ def test_library_reproduces_golden(name, prec):
         check(out, z, 1e-10, 1e-10)
     else:
         check(out, z, 1e-5, 1e-6, g2_absfrac=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("prec", [_lib.PREC_FP64, _lib.PREC_SPLIT_TF32])
+def test_library_reproduces_golden_ph(name, prec):
+    """ephg_ph_rates against the phonon-side fixtures: FP64 1e-10 relative; split
+    1e-5 relative on every rate (+1e-12 of the largest).  A phonon rate is one
+    mode's sum, and the split form's |g|^2 carries an error of ~1e-7 of the
+    crystal's largest coupling (FP32 accumulation), so weakly coupled modes of
+    these small random crystals show up to ~3e-6; the electron rates, summed
+    over all modes, keep 1e-6, as do the phonon rates of the bench workload
+    (test_gpu_ph.test_full_size_split_vs_fp64)."""
+    from elphbolt_gb300.build import build
+    from elphbolt_gb300.interactions import ibzq_order
+    from elphbolt_gb300.wannier import Wannier
+    build()
+    wd, req, zel = load(name)
+    z = load_ph(name)
+    W = Wannier(wd)
+    try:
+        out = W.ph_rates(req, precision=prec, spindeg=int(z["spindeg"]), electrons=True, vertices=True)
+    finally:
+        W.deallocate_wannier()
+    assert out["vertices"] == int(z["nvert"])
+    win = np.abs(zel["ens"] - req.enref) <= req.fsthick
+    order, _, _, _ = ibzq_order(out["indexlist"], win, req.mesh, wd.numbranches)
+    g2, y = out["g2"][order], out["y"][order]
+    if prec == _lib.PREC_FP64:
+        check_ph(out["rates_phe"], g2, y, z, 1e-10, 0.0, 1e-10, 1e-12)
+    else:
+        check_ph(out["rates_phe"], g2, y, z, 1e-5, 1e-12, 1e-5, 1e-6)

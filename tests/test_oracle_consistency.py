@@ -110,3 +110,74 @@ def test_triangle_delta_linear_band(oracle_lib):
                 for ik in range(1, nk + 1))
         tot.append(s)
     assert np.all(np.array(tot) > 0)
+
+
+def _oracle_window(W, req, indexlist):
+    i = np.asarray(indexlist) - 1
+    m = np.asarray(req.mesh)
+    k = np.stack([i % m[0], (i // m[0]) % m[1], i // (m[0] * m[1])], 1) / m
+    e, _, _ = W.el_wann(k)
+    return np.abs(e - req.enref) <= req.fsthick
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("delta", [0, 1, 2])
+def test_ph_side_visits_el_vertices(oracle_lib, name, delta):
+    """The ibzq loop (gReq + 'el' g2, phonon-state order) and the ibzk loop
+    (gkRp + 'ph' g2, electron-state order) visit the same vertices with the same
+    |g|^2: the electron-order list, reordered by ibzq_order, is the phonon-order
+    list.  The library forms both sides in one sweep on this identity."""
+    from elphbolt_gb300.interactions import ibzq_order
+    wd, req = case(name)
+    req = S.RateRequest(**{**req.__dict__, "delta_kind": delta})
+    W = oracle_lib.Wannier(wd)
+    el = W.el_rates(req, literal=False, vertices=True)
+    ph = W.ph_rates(req, spindeg=2, nthreads=4, vertices=True)
+    assert el["vertices"] == ph["vertices"] > 0
+    win = _oracle_window(W, req, el["indexlist"])
+    assert win.sum() == el["nstates_inwindow"]
+    order, istate_ph, i1, i2 = ibzq_order(el["indexlist"], win, req.mesh, wd.numbranches)
+    scale = np.abs(ph["g2"]).max()
+    assert np.max(np.abs(el["g2"][order] - ph["g2"])) <= 1e-12 * scale
+    # the phonon states run in demux_state order and every q of the mesh appears
+    assert np.all(np.diff(istate_ph) >= 0)
+    # rates: spindeg * sum of Y per phonon state, in list order
+    N = int(np.prod(req.mesh))
+    acc = np.zeros(N * wd.numbranches)
+    np.add.at(acc, istate_ph - 1, 2 * ph["y"])
+    r = ph["rates_phe"].reshape(-1, order="C")           # row-major (q, s) = istate order
+    assert np.allclose(acc, r, rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", ["si8"])
+def test_ph_rates_spindeg_and_detailed_balance(oracle_lib, name):
+    """rates_phe is linear in spindeg, and each vertex obeys Y = X+ f(1 - f) / (n (1 + n))
+    (f = f(E_km), n = n(omega_qs)): absorption by the electron and emission seen
+    from the phonon are tied by detailed balance."""
+    from elphbolt_gb300.interactions import ibzq_order
+    from elphbolt_gb300 import constants as C
+    wd, req = case(name)
+    W = oracle_lib.Wannier(wd)
+    a = W.ph_rates(req, spindeg=1, nthreads=4)
+    b = W.ph_rates(req, spindeg=2, nthreads=4, vertices=True)
+    assert np.allclose(2 * a["rates_phe"], b["rates_phe"], rtol=1e-14, atol=0)
+    el = W.el_rates(req, literal=False, vertices=True)
+    win = _oracle_window(W, req, el["indexlist"])
+    order, istate_ph, i1, i2 = ibzq_order(el["indexlist"], win, req.mesh, wd.numbranches)
+    i = np.asarray(el["indexlist"]) - 1
+    m = np.asarray(req.mesh)
+    k = np.stack([i % m[0], (i // m[0]) % m[1], i // (m[0] * m[1])], 1) / m
+    e, _, _ = W.el_wann(k)
+    E = e.reshape(-1)[i1 - 1]
+    qs = S.mesh_kvecs(req.mesh)
+    om, _, _, _ = W.ph_wann(qs)
+    w = om.reshape(-1)[istate_ph - 1]
+    kT = C.kB * req.T
+    f = 1.0 / (np.exp((E - req.chempot) / kT) + 1.0)
+    keep = w >= 0.5e-3
+    n = 1.0 / np.expm1(w[keep] / kT)
+    xp = el["xp"][order][keep]
+    y = b["y"][keep]
+    assert np.all(b["y"][~keep] == 0)
+    pred = xp * f[keep] * (1 - f[keep]) / (n * (1 + n))
+    assert np.max(np.abs(pred - y)) <= 1e-10 * np.abs(y).max()
