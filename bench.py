@@ -108,10 +108,13 @@ def replica_value(dist, world, steps, vertices_per_step, local_ms):
     return world * steps * vertices_per_step / (t * 1e-3), t
 
 
+MESH = (24, 24, 24)
+
+
 def workload():
     from elphbolt_gb300 import synthetic as S
     wd = S.si_like()                                   # seed 20260101, 6^3 WS supercell
-    req = S.si_like_request(wd, (24, 24, 24))          # 24^3, +-0.5 eV at mid-gap+0.6 eV, 10 meV
+    req = S.si_like_request(wd, MESH)                  # 24^3, +-0.5 eV at mid-gap+0.6 eV, 10 meV
     return wd, req
 
 
@@ -202,6 +205,45 @@ def phonon_side(W, req, steps, el_ms, fp64_el_ms):
             "rates_phe_max_rel_vs_fp64": err, "rates_phe_positive": int(m.sum()), "rates_phe_size": int(ref.size),
             "what": "ephg_ph_rates: ibzq 'g' + 'Y' + ph-e RTA rates (every q of the mesh x nb) and the electron "
                     "rates of the same vertices in one sweep; value = vertices/s of that sweep"}
+
+
+def polar_side(steps):
+    """The polar long-range terms (dyn_nonanalytic, long_range_prefac) on a
+    SiC-like crystal (3C-SiC's lattice, masses, dielectric constant and Born
+    charges; nw 8, 6^3 WS sets) with the bench request's mesh and window: both
+    sides in one split sweep, its cost over the same crystal without the
+    long-range terms, and its rates against the FP64 form."""
+    import numpy as np
+    from elphbolt_gb300 import _lib, synthetic as S
+    from elphbolt_gb300.wannier import Wannier
+    wd = S.make_wannier(S.make_crystal_sic_like(), 8, supercell=(6, 6, 6), seed=20260105)
+    req = S.si_like_request(wd, MESH)
+    W = Wannier(wd)
+    try:
+        split = lambda: W.ph_rates(req, precision=_lib.PREC_SPLIT_TF32, electrons=True)
+        split()
+        runs = [split() for _ in range(max(3, steps))]
+        t = float(np.median([r["stats"]["ms_total"] for r in runs]))
+        s = runs[-1]
+        W.set_polar(None, None)
+        W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+        t0 = float(np.median([W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)["stats"]["ms_total"]
+                              for _ in range(max(3, steps))]))
+        W.set_polar(wd.crystal.epsilon, wd.crystal.born)
+        f = W.ph_rates(req, precision=_lib.PREC_FP64, electrons=True)
+    finally:
+        W.deallocate_wannier()
+    v = s["stats"]["vertices"]
+    m, mp = f["rates"] > 0, f["rates_phe"] > 0
+    rel_el = np.abs(s["rates"][m] - f["rates"][m]) / f["rates"][m]
+    rel_ph = np.abs(s["rates_phe"][mp] - f["rates_phe"][mp]) / f["rates_phe"][mp]
+    return {"workload": "SiC-like polar crystal (epsilon 7.419, Z* +-2.7515, nw 8, 6^3 WS), %dx%dx%d mesh" % MESH,
+            "value": v / (t * 1e-3), "unit": UNIT, "vertices": v, "ms_per_step": t,
+            "nonpolar_el_ms_per_step": t0, "setup_ms": s["stats"]["ms_setup"],
+            "fp64_ms_per_step": f["stats"]["ms_total"], "split_speedup_vs_fp64": f["stats"]["ms_total"] / t,
+            "rates_max_rel_vs_fp64": float(rel_el.max()), "rates_phe_max_rel_vs_fp64": float(rel_ph.max()),
+            "rates_phe_p999_rel_vs_fp64": float(np.quantile(rel_ph, 0.999)),
+            "what": "ephg_ph_rates with ephg_set_polar: both rate sets in one split sweep, long-range terms on"}
 
 
 def run_reference(args, ws, rank):
@@ -343,6 +385,11 @@ def run_ours(args, ws, rank, local):
             "wall_s": wall,
             "clocks": clk.summary()}
     line["phonon_side"] = ph
+    if not args.no_polar:
+        try:
+            line["polar"] = polar_side(args.steps)
+        except Exception as e:   # the main line is still printed
+            line["polar"] = {"error": repr(e)}
     if serving is not None:
         line["serving"] = serving
     print(json.dumps(line), flush=True)
@@ -413,6 +460,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop (p50 / p99 latency) measurement")
+    ap.add_argument("--no-polar", action="store_true", help="skip the polar-crystal measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1 and args.impl == "ours":

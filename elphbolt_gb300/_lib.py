@@ -33,7 +33,7 @@ c_dp = ct.POINTER(ct.c_double)
 EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count", "ephg_el_wann",
            "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates",
            "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
-           "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates"]
+           "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates", "ephg_set_polar"]
 
 TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
 
@@ -111,6 +111,7 @@ def load(path: str = LIB_PATH):
                                 c_dp, c_dp, c_dp, ct.c_int64]
     L.ephg_ph_rates.argtypes = [vp, ct.POINTER(RateRequest), ct.c_int64, c_dp, c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, ct.c_int64]
+    L.ephg_set_polar.argtypes = [vp, c_dp, c_dp]
     L.ephg_el_wann_noalloc.argtypes = [vp, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     L.ephg_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_int64, ct.c_int, ct.POINTER(vp)]
     L.ephg_server_destroy.argtypes = [vp]

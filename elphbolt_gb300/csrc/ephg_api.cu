@@ -142,7 +142,8 @@ int ephg_destroy(ephg_handle *h) {
   if (!h) return EPHG_OK;
   void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->graw, h->G64,
                   h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_rden,
-                  h->rcartq, h->D, h->err, h->kposk, h->kposq};
+                  h->rcartq, h->D, h->err, h->kposk, h->kposq, h->polar_G, h->polar_Gcell,
+                  h->polar_born, h->polar_tau, h->polar_Da};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   h->ws.release();
@@ -190,6 +191,7 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
   for (int i = 0; i < 3; ++i) h->cq[i] = (int)d->coarse_qmesh[i];
   for (int i = 0; i < 9; ++i) h->lattvecs[i] = d->lattvecs[i];
   h->masses_h.assign(d->masses, d->masses + h->nat);
+  h->basis_h.assign(d->basis, d->basis + 3 * h->nat);
   const int nw = h->nw, nb = h->nb, nwsk = h->nwsk, nwsq = h->nwsq;
   h->Nn = (int64_t)nw * nw * nb * nwsq;
   // R lists as (n,3) int rows and degeneracies as doubles
@@ -328,6 +330,99 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
   return EPHG_OK;
 }
 
+// ------------------------------------------------------------- polar
+// The crystal fields of a polar crystal (crys%polar, epsilon, born;
+// crystal.f90:45-49) and what the long-range terms derive from them:
+// reciprocal vectors and volume (crystal.f90:282-293), the Cartesian basis in
+// bohr, the box of reciprocal-lattice vectors and the q-independent part of
+// dyn_nonanalytic (wannier.f90:843-867), formed once.
+int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born) {
+  if (!h) return fail(EPHG_ERR_ARG, "set_polar: bad arguments");
+  if (epsilon && !born) return fail(EPHG_ERR_ARG, "set_polar: born effective charges are required");
+  CK(cudaStreamSynchronize(h->st));
+  for (void *p : {(void *)h->polar_G, (void *)h->polar_Gcell, (void *)h->polar_born, (void *)h->polar_tau,
+                  (void *)h->polar_Da})
+    if (p) cudaFree(p);
+  h->polar_G = h->polar_Gcell = h->polar_born = h->polar_tau = nullptr;
+  h->polar_Da = nullptr;
+  h->polar_on = false;
+  if (!epsilon) return EPHG_OK;   // non-polar
+  const double bohr2nm = 0.052917721092, pi = 4.0 * atan(1.0), twopi = 2.0 * pi;   // params.f90
+  const int nat = h->nat, nb = h->nb;
+  const double *a = h->lattvecs;
+  ephg::PolarDev P;
+  for (int i = 0; i < 3; ++i) {
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    P.rec[0 + 3 * i] = a[1 + 3 * j] * a[2 + 3 * k] - a[2 + 3 * j] * a[1 + 3 * k];
+    P.rec[1 + 3 * i] = a[2 + 3 * j] * a[0 + 3 * k] - a[0 + 3 * j] * a[2 + 3 * k];
+    P.rec[2 + 3 * i] = a[0 + 3 * j] * a[1 + 3 * k] - a[1 + 3 * j] * a[0 + 3 * k];
+  }
+  const double vol = fabs(a[0] * P.rec[0] + a[1] * P.rec[1] + a[2] * P.rec[2]);
+  for (double &r : P.rec) r *= twopi / vol;
+  const double a1 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  const double tpiba = twopi / a1 * bohr2nm;
+  P.alph = tpiba * tpiba;
+  P.gmax = 14.0;
+  P.fac = 8.0 * pi / (vol / (bohr2nm * bohr2nm * bohr2nm));
+  for (int i = 0; i < 9; ++i) P.eps[i] = epsilon[i];
+  std::vector<double> G, tau(3 * (size_t)nat);
+  for (int m1 = -h->cq[0]; m1 <= h->cq[0]; ++m1)
+    for (int m2 = -h->cq[1]; m2 <= h->cq[1]; ++m2)
+      for (int m3 = -h->cq[2]; m3 <= h->cq[2]; ++m3)
+        for (int d = 0; d < 3; ++d) G.push_back((m1 * P.rec[d] + m2 * P.rec[d + 3] + m3 * P.rec[d + 6]) * bohr2nm);
+  for (int at = 0; at < nat; ++at)
+    for (int d = 0; d < 3; ++d) {
+      const double *b = &h->basis_h[3 * (size_t)at];
+      tau[3 * at + d] = (a[d] * b[0] + a[d + 3] * b[1] + a[d + 6] * b[2]) / bohr2nm;
+    }
+  // The box vectors that can pass the cut qeq < 4 alph gmax for some q of the
+  // first cell (the mesh q): qeq >= lmin |G + q|^2 >= lmin (|G| - qmax)^2, with
+  // lmin a Gershgorin lower bound of the symmetric part of epsilon and qmax the
+  // longest corner of the cell.  Without a positive bound nothing is dropped.
+  double lmin = INFINITY, qmax = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    double off = 0.0;
+    for (int j = 0; j < 3; ++j)
+      if (j != i) off += fabs(0.5 * (epsilon[i + 3 * j] + epsilon[j + 3 * i]));
+    lmin = std::min(lmin, epsilon[i + 3 * i] - off);
+  }
+  for (int c = 0; c < 8; ++c) {
+    double v[3];
+    for (int d = 0; d < 3; ++d)
+      v[d] = ((c & 1) * P.rec[d] + ((c >> 1) & 1) * P.rec[d + 3] + ((c >> 2) & 1) * P.rec[d + 6]) * bohr2nm;
+    qmax = std::max(qmax, sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+  }
+  std::vector<double> Gc;
+  const double rcut = lmin > 0.0 ? sqrt(4.0 * P.alph * P.gmax / lmin) * (1.0 + 1e-9) + qmax : INFINITY;
+  for (size_t i = 0; i < G.size(); i += 3) {
+    const double n = sqrt(G[i] * G[i] + G[i + 1] * G[i + 1] + G[i + 2] * G[i + 2]);
+    if (n < rcut) Gc.insert(Gc.end(), {G[i], G[i + 1], G[i + 2]});
+  }
+  P.nat = nat;
+  P.nb = nb;
+  P.M = (int)(G.size() / 3);
+  P.Mcell = (int)(Gc.size() / 3);
+  P.masses = h->masses;
+  int rc;
+  if ((rc = upload(&h->polar_G, G.data(), G.size(), h->st)) ||
+      (rc = upload(&h->polar_Gcell, Gc.data(), Gc.size(), h->st)) ||
+      (rc = upload(&h->polar_born, born, 9 * (size_t)nat, h->st)) ||
+      (rc = upload(&h->polar_tau, tau.data(), tau.size(), h->st)))
+    return rc;
+  CK(cudaMalloc(&h->polar_Da, (size_t)nb * nb * sizeof(double2)));
+  P.G = h->polar_G;
+  P.Gcell = h->polar_Gcell;
+  P.born = h->polar_born;
+  P.tau = h->polar_tau;
+  launch_polar_da(P, h->polar_Da, h->st);
+  CKL();
+  CK(cudaStreamSynchronize(h->st));
+  P.Da = h->polar_Da;
+  h->polar = P;
+  h->polar_on = true;
+  return EPHG_OK;
+}
+
 // ------------------------------------------------------------- el_wann
 int ephg_el_wann(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
                  double *velocities, double *evecs, const double *scissor) {
@@ -390,6 +485,8 @@ int ephg_ph_wann(ephg_handle *h, int64_t nq, const double *qvecs, double *energi
     return WSFAIL(rc);
   CK(cudaMemcpyAsync(qv, qvecs, (size_t)nq * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
   launch_dbuild((int)nq, nullptr, nullptr, 1, nullptr, qv, h->terms, with_vel, Dq, dDq, h->st);
+  if (h->polar_on)   // non-analytic correction (wannier.f90:684-705)
+    launch_polar_q(h->polar, (int)nq, nullptr, nullptr, qv, Dq, with_vel ? dDq : nullptr, nullptr, h->st);
   launch_heig((int)nq, nb, Dq, nn, w, V, h->err, h->st);
   launch_ph_post((int)nq, nb, nullptr, qv, w, V, dDq, with_vel, h->masses, ens,
                  evecs ? ev : nullptr, with_vel ? vel : nullptr, nullptr, nullptr, nullptr, h->err,
@@ -496,8 +593,19 @@ int ephg_g2(ephg_handle *h, int64_t wannspace, int64_t nv, const double *kvecs,
   CK(cudaMemcpyAsync(gi, gm_index, (size_t)nv * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
   const int *R = wannspace == EPHG_WANNSPACE_PH ? h->Rq : h->Rk;
   const double *deg = wannspace == EPHG_WANNSPACE_PH ? h->degq : h->degk;
+  double2 *Lv = nullptr;
+  if (h->polar_on) {   // the long-range term of each vertex's q (wannier.f90:998-1006)
+    double *qp = qv;
+    if (wannspace != EPHG_WANNSPACE_PH) {
+      if ((rc = wsget(h->ws, "g2_qp", (size_t)nv * 3, &qp))) return WSFAIL(rc);
+      CK(cudaMemcpyAsync(qp, qvecs, (size_t)nv * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    }
+    if ((rc = wsget(h->ws, "g2_L", (size_t)nv * nb, &Lv))) return WSFAIL(rc);
+    launch_polar_q(h->polar, (int)nv, nullptr, nullptr, qp, nullptr, nullptr, Lv, h->st);
+    h->launches += 1;
+  }
   launch_g2_batch((int)nv, nw, nb, nws, qv, R, deg, ek, ekp, eq, en, h->masses, gm, gi, gstride,
-                  out, h->st);
+                  Lv, out, h->st);
   h->launches += 1;
   CKL();
   CK(cudaMemcpyAsync(g2_out, out, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -682,12 +790,25 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   if (nwv == 0) return fail(EPHG_ERR_EMPTY_WINDOW, "No states found within Fermi window.");
   // ---- phonons on the q mesh (phonon.f90:208-214) ----
   launch_dbuild(N, iota, mesh, L, roots, nullptr, h->terms, 0, Dq, nullptr, st);
+  double2 *Lq = nullptr, *glp = nullptr;
+  float2 *glpf = nullptr;
+  if (h->polar_on) {   // dyn_nonanalytic into D(q) and the long-range vector of every mesh q
+    if ((rc = wsget((*x.ws), "r_Lq", (size_t)N * nb, &Lq)) || (rc = wsget((*x.ws), "r_glp", (size_t)N * nb, &glp)) ||
+        (split && (rc = wsget((*x.ws), "r_glpf", (size_t)N * nb, &glpf))))
+      return WSFAILX(rc);
+    launch_polar_q(h->polar, N, iota, mesh, nullptr, Dq, nullptr, Lq, st);
+    (*x.launches) += 1;
+  }
   launch_heig(N, nb, Dq, (int64_t)nb * nb, wq, Vq, x.err, st);
   float2 *uf = nullptr;
   if (split && (rc = wsget((*x.ws), "r_uf", (size_t)N * nb * nb, &uf))) return WSFAILX(rc);
   launch_ph_post(N, nb, iota, nullptr, wq, Vq, nullptr, 0, h->masses, nullptr, nullptr, nullptr, om,
                  u, uf, x.err, st);
   launch_bose(N, nb, om, req->T, bose, st);
+  if (h->polar_on) {   // long_range_prefac(q, u_s) for every (q, s)
+    launch_glprefac(N, nb, Lq, u, glp, glpf, st);
+    (*x.launches) += 1;
+  }
   // ---- initial states (demux_state order, interactions.f90:2169-2191) ----
   launch_state_flags(nwv, nw, widx, ens, req->enref, req->fsthick, sflag, nin_k, st);
   CK(cudaMemsetAsync(nin_k + nwv, 0, sizeof(int), st));
@@ -766,6 +887,8 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   ed.u = u;
   ed.uf = uf;
   ed.bose = bose;
+  ed.glp = glp;
+  ed.glpf = glpf;
   ed.per_state = (int64_t)nin * nb;
   double *g2d = nullptr, *xpd = nullptr, *xmd = nullptr, *yd = nullptr, *phr = nullptr;
   int64_t vtot = (int64_t)nst * nin * nb;

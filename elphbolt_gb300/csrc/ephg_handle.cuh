@@ -17,6 +17,7 @@ struct ephg_handle {
   int cq[3] = {0, 0, 0};
   double lattvecs[9];
   std::vector<double> masses_h;
+  std::vector<double> basis_h;   // (3,nat) crystal coordinates
   int64_t Nn = 0;   // nw*nw*nb*nwsg, the stage-A row length
   // resident device data
   int *Rk = nullptr, *Rq = nullptr, *Rg = nullptr;         // (n,3) int
@@ -38,6 +39,11 @@ struct ephg_handle {
   int64_t launches = 0;
   int64_t resident_bytes = 0;   // device bytes taken by ephg_create (Wannier data, tables)
   std::mutex split_mu;          // guards the one-time build of `split`
+  // polar crystals (ephg_set_polar): the long-range terms' device data
+  bool polar_on = false;
+  ephg::PolarDev polar;
+  double *polar_G = nullptr, *polar_Gcell = nullptr, *polar_born = nullptr, *polar_tau = nullptr;
+  double2 *polar_Da = nullptr;
 };
 
 namespace ephg {

@@ -608,7 +608,7 @@ __global__ void k_g2_batch(int nv, int nw, int nb, int nws, const double *qv, co
                            const double *deg, const double2 *ek, const double2 *ekp,
                            const double2 *eq, const double *ph_en, const double *masses,
                            const double2 *gm, const int64_t *gm_index, int64_t gm_stride,
-                           double *g2) {
+                           const double2 *Lv, double *g2) {
   const int lane = threadIdx.x & 31;
   const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (v >= nv) return;
@@ -646,17 +646,29 @@ __global__ void k_g2_batch(int nv, int nw, int nb, int nws, const double *qv, co
     gb.x += __shfl_xor_sync(0xffffffffu, gb.x, o);
     gb.y += __shfl_xor_sync(0xffffffffu, gb.y, o);
   }
-  if (lane == 0) g2[v] = 0.5 * (gb.x * gb.x + gb.y * gb.y) / en * g2unitfactor;
+  if (lane == 0) {
+    if (Lv) {   // polar: + long_range_prefac(q, u) * dot_product(el_evec_kp, el_evec_k) (wannier.f90:998-1006)
+      double2 gl = make_double2(0.0, 0.0), unm = make_double2(0.0, 0.0);
+      for (int sp = 0; sp < nb; ++sp) {
+        double2 u = eq[v + (int64_t)nv * sp];
+        u = make_double2(u.x / sqrt(masses[sp / 3]), u.y / sqrt(masses[sp / 3]));
+        cfma(gl, Lv[(size_t)v * nb + sp], u);
+      }
+      for (int c = 0; c < nw; ++c) cfma_cj(unm, ekp[v + (int64_t)nv * c], ek[v + (int64_t)nv * c]);
+      cfma(gb, gl, unm);
+    }
+    g2[v] = 0.5 * (gb.x * gb.x + gb.y * gb.y) / en * g2unitfactor;
+  }
 }
 
 void launch_g2_batch(int nv, int nw, int nb, int nws, const double *qv, const int *R,
                      const double *deg, const double2 *ek, const double2 *ekp,
                      const double2 *eq, const double *ph_en, const double *masses,
                      const double2 *gm, const int64_t *gm_index, int64_t gm_stride,
-                     double *g2, cudaStream_t st) {
+                     const double2 *Lv, double *g2, cudaStream_t st) {
   if (nv <= 0) return;
   k_g2_batch<<<(nv + 3) / 4, 128, 0, st>>>(nv, nw, nb, nws, qv, R, deg, ek, ekp, eq, ph_en,
-                                           masses, gm, gm_index, gm_stride, g2);
+                                           masses, gm, gm_index, gm_stride, Lv, g2);
 }
 
 // ============================================================ q indices
@@ -904,11 +916,17 @@ __device__ void pair_epilogue(int ip, int j, GV Gv, const RateParams &rp, const 
       for (int np = 0; np < nw; ++np) cfma_cj(a, Ukp[np], Gv(np + nw * s));
       h[s] = a;
     }
+    double2 unm = make_double2(0.0, 0.0);   // dot_product(el_evec_kp, el_evec_k), polar crystals
+    if (d.glp) {
+      const double2 *Uk = d.U + ((size_t)p * nw + m) * nw;
+      for (int c = 0; c < nw; ++c) cfma_cj(unm, Ukp[c], Uk[c]);
+    }
     for (int s = 0; s < nb; ++s) {
       double om = d.om[(size_t)q * nb + s];
       double2 gsum = make_double2(0.0, 0.0);
       const double2 *u = d.u + ((size_t)q * nb + s) * nb;
       for (int sp = 0; sp < nb; ++sp) cfma(gsum, u[sp], h[sp]);
+      if (d.glp) cfma(gsum, d.glp[(size_t)q * nb + s], unm);   // long-range term (wannier.f90:998-1006)
       double g2 = (om == 0.0) ? 0.0 : 0.5 * (gsum.x * gsum.x + gsum.y * gsum.y) / om * g2unitfactor;
       double bose = d.bose[(size_t)q * nb + s];
       double xp = 0.0, xm = 0.0, y = 0.0;

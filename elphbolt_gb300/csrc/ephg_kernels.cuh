@@ -65,11 +65,41 @@ void launch_permute_greq(int nq, int nw, int nb, int nwsk, const double2 *in, do
                          cudaStream_t st);
 
 // ---- g2 batched (wannier.f90:903-1011) ----
+// Lv (nv, nb), nullable: the polar long-range vector of each vertex's q (launch_polar_q)
 void launch_g2_batch(int nv, int nw, int nb, int nws, const double *qv, const int *R,
                      const double *deg, const double2 *ek, const double2 *ekp,
                      const double2 *eq, const double *ph_en, const double *masses,
                      const double2 *gm, const int64_t *gm_index, int64_t gm_stride,
-                     double *g2, cudaStream_t st);
+                     const double2 *Lv, double *g2, cudaStream_t st);
+
+// ---- polar long-range terms (wannier.f90:784-901, 1013-1071) ----
+// Crystal data of a polar crystal on the device (ephg_set_polar).  The Ewald
+// sums run over the box of reciprocal-lattice vectors m1 b1 + m2 b2 + m3 b3,
+// |m_i| <= coarse_qmesh(i), with the cut qeq / (4 alph) < gmax.
+struct PolarDev {
+  int nat = 0, nb = 0, M = 0;
+  const double *G = nullptr;      // [M][3] box vectors, Cartesian 1/bohr, in the reference's loop order
+  const double *Gcell = nullptr;  // [Mcell][3] those of them that can pass the cut for q in the first cell
+  int Mcell = 0;
+  const double *born = nullptr;   // born(x, ipol, at) at x + 3 ipol + 9 at
+  const double *tau = nullptr;    // [nat][3] Cartesian basis, bohr
+  const double2 *Da = nullptr;    // (nb,nb) column-major: the q-independent sum (before fac)
+  const double *masses = nullptr; // per atom, amu
+  double eps[9];                  // dielectric tensor, column-major
+  double rec[9];                  // reciprocal vectors (columns, 1/nm, with 2 pi)
+  double alph = 0, gmax = 14.0, fac = 0;   // tpiba^2 (1/bohr^2), cut, 8 pi / volume (1/bohr^3)
+};
+// Per q (mesh index qp[q] on `mesh`, else crystal coordinates qv (nq,3)
+// column-major): Dq[q] += massnorm * dyn_l(q) (nullable; layout of
+// launch_dbuild), dDq[q] += massnorm * ddyn_l(q) * bohr2nm (nullable), and
+// Lq[q][c] (nullable) with long_range_prefac(q, u) = sum_c Lq[q][c] u[c].
+void launch_polar_q(const PolarDev &P, int nq, const int *qp, const int mesh[3], const double *qv,
+                    double2 *Dq, double2 *dDq, double2 *Lq, cudaStream_t st);
+// The q-independent part of dyn_nonanalytic into Da (nb,nb), once per crystal.
+void launch_polar_da(const PolarDev &P, double2 *Da, cudaStream_t st);
+// glp[q][s] = sum_c Lq[q][c] u[q][s][c] (u = evec / sqrt(M)), and its fp32 copy (nullable)
+void launch_glprefac(int nq, int nb, const double2 *Lq, const double2 *u, double2 *glp, float2 *glpf,
+                     cudaStream_t st);
 
 // ---- q index table (vector.f90:86-102 on integers) ----
 void launch_kq_index(const int mesh[3], int nk, const int64_t *k_idx, int nkp,
@@ -112,6 +142,10 @@ struct EpiData {
   // (device atomics); yv is the optional per-vertex Y list in the order of g2
   double *phr, *yv;
   double ph_scale;      // el%spindeg
+  // polar crystals: glp[q][s] = long_range_prefac(q, u_s), added to each vertex
+  // as glp * <U_k'[n]|U_k[m]> (wannier.f90:998-1006); nullable
+  const double2 *glp;
+  const float2 *glpf;   // same in fp32 (split path)
 };
 // per (k', state) epilogue on an FP64 C chunk: rates partial sums [j][iblk]
 void launch_epilogue_fp64(int nwv, int j0, int j1, const double2 *C, int64_t ldc,

@@ -736,12 +736,18 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
         }
         h[s] = a;
       }
+      float2 unm = make_float2(0.f, 0.f);   // <U_k'[n]|U_k[m]>, polar crystals
+      if (d.glpf) {
+        const float2 *Uk = d.Uf + ((size_t)p * nw + m) * nw;
+        for (int c = 0; c < nw; ++c) cfmaf_cj(unm, Ukp[c], Uk[c]);
+      }
       const float dn = (float)((E - eps) * inv_sig);
       for (int s = 0; s < nb; ++s) {
         const int qs = q * nb + s;
         const float2 *u = d.uf + (size_t)qs * nb;
         float2 g = make_float2(0.f, 0.f);
         for (int sp = 0; sp < nb; ++sp) cfmaf(g, u[sp], h[sp]);
+        if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
         const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
         const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
         const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
@@ -848,6 +854,13 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
 #pragma unroll
         for (int np = 0; np < AW; ++np)
           if (np < nw) uk[np] = Ukp[np];
+        float2 unm = make_float2(0.f, 0.f);   // <U_k'[n]|U_k[m]>, polar crystals
+        if (d.glpf) {
+          const float2 *Uk = d.Uf + ((size_t)p * nw + m) * nw;
+#pragma unroll
+          for (int c = 0; c < AW; ++c)
+            if (c < nw) cfmaf_cj(unm, uk[c], Uk[c]);
+        }
         float2 h[AB];
 #pragma unroll
         for (int s = 0; s < AB; ++s) {
@@ -868,6 +881,7 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
 #pragma unroll
           for (int sp = 0; sp < AB; ++sp)
             if (sp < nb) cfmaf(g, u[sp], h[sp]);
+          if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
           const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
           const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
           const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
@@ -938,6 +952,7 @@ struct StateRec {      // per initial state j
   float a_occ;         // (E - mu) / kT
   int apack;           // mesh coordinates of k: a1 | a2 << 10 | a3 << 20
   YOcc yo;             // per-state part of the phonon-side occupation factor
+  int urow;            // p * 8 + m: the state's U_k row in the fp32 eigenvector table
 };
 
 // The row and q tables are blocked by 32: entry (i, field) sits at
@@ -949,6 +964,7 @@ struct FusedTabs {
   const float4 *U4;        // row-blocked, fields n * 4 + h: U_k'[n][2h], U_k'[n][2h + 1] (fp32 complex)
   const double *ensw;      // row-blocked, fields n: window-k' band energies
   const float4 *rec;       // q-blocked, fields s * 4 + f: u[s][0..1], u[s][2..3], u[s][4..5], (cx, bose, w, v)
+  const float2 *glb;       // polar crystals: q-blocked, fields s: long_range_prefac(q, u_s) (else null)
   int MpB, N;
 };
 
@@ -1003,6 +1019,7 @@ __global__ void k_fused_states(int nst, const int *st_code, const int *widx, con
   r.E = ens[(size_t)p * 8 + (code & 7)];
   r.a_occ = (float)((r.E - chempot) / kT);
   r.yo = y_occ(r.E, chempot, kT);
+  r.urow = p * 8 + (code & 7);
   const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
   r.apack = a1 | (a2 << 10) | (a3 << 20);
   out[j] = r;
@@ -1018,6 +1035,12 @@ __global__ void k_fused_recs(int N, const float2 *uf, const float *cx, const flo
   rec[blk32(q, 24, s * 4 + 1)] = make_float4(u[2].x, u[2].y, u[3].x, u[3].y);
   rec[blk32(q, 24, s * 4 + 2)] = make_float4(u[4].x, u[4].y, u[5].x, u[5].y);
   rec[blk32(q, 24, s * 4 + 3)] = make_float4(cx[i], bs[i], w[i], v[i]);
+}
+
+__global__ void k_fused_glp(int N, const float2 *glpf, float2 *glb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;   // (q, s)
+  if (i >= N * 6) return;
+  glb[blk32(i / 6, 6, i % 6)] = glpf[i];
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -1069,10 +1092,12 @@ __device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const 
 // PH: also ys[s] += |g|^2 cx delta, the n-dependent part of Y; its occupation
 // factor depends on the initial state and the mode only and is applied once per
 // pair (y_factor).
-template <bool PH>
+// POLAR: g += long_range_prefac(q, u_s) * <U_k'[n]|U_k[m]> (glb = the lane's
+// entry of field 0 of q's block of the prefactor table, unm the overlap).
+template <bool PH, bool POLAR>
 __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ,
                                                 float dnorm, const EpiData &d, int64_t voff, int q,
-                                                const YOcc &yo, float *ys) {
+                                                const YOcc &yo, float *ys, const float2 *glb, float2 unm) {
   float acc = 0.f;
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
@@ -1085,6 +1110,7 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
     cfmaf(g, make_float2(u23.z, u23.w), h[3]);
     cfmaf(g, make_float2(u45.x, u45.y), h[4]);
     cfmaf(g, make_float2(u45.z, u45.w), h[5]);
+    if (POLAR) cfmaf(g, __ldg(glb + s * 32), unm);
     // sc = (cx, bose, w, v)
     const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
     const float tp = dn + sc.z, tm = dn - sc.z;
@@ -1110,7 +1136,8 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
 }
 
 // PH: the phonon side too (Y of every vertex into the ph-e rate of its (q, s)).
-template <bool PH>
+// POLAR: the long-range term of polar crystals in every vertex.
+template <bool PH, bool POLAR>
 __global__ void __launch_bounds__(F_THREADS, 1)
     k_stageB_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedArgs g,
                      FusedTabs tb, RateParams rp, EpiData d) {
@@ -1238,11 +1265,13 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       double E = 0.0;
       float a_occ = 0.f;
       YOcc yo{0.f, 0.f};
+      const float2 *Uk = nullptr;   // the state's U_k[m] (polar)
       if (jvalid) {
         const StateRec sr = tb.state[j];
         E = sr.E;
         a_occ = sr.a_occ;
         yo = sr.yo;
+        if (POLAR) Uk = d.Uf + (size_t)sr.urow * 8;
         wmask = (unsigned)ri.y;
         const int a1 = sr.apack & 1023, a2 = (sr.apack >> 10) & 1023, a3 = sr.apack >> 20;
         const int b1 = ri.w & 1023, b2 = (ri.w >> 10) & 1023, b3 = ri.w >> 20;
@@ -1258,6 +1287,16 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       float2 u0[8], u1[8];
       if (nbw > 0) load_urow(ub, n0, u0);
       if (nbw > 1) load_urow(ub, n1, u1);
+      const float2 *glb = POLAR ? tb.glb + blk32(q, 6, 0) : nullptr;
+      float2 unm0 = make_float2(0.f, 0.f), unm1 = make_float2(0.f, 0.f);
+      if (POLAR && nbw > 0) {   // <U_k'[n]|U_k[m]> of the first two window bands
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float2 uk = __ldg(Uk + c);
+          cfmaf_cj(unm0, u0[c], uk);
+          if (nbw > 1) cfmaf_cj(unm1, u1[c], uk);
+        }
+      }
       const int64_t vbase = (nbw > 0 && d.g2) ? (int64_t)j * d.per_state + (int64_t)ri.z * 6 : 0;
       float acc = 0.f;
       float ys[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1292,7 +1331,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           }
           if (mine) {
             const float dn = (float)((E - __ldg(eb + nb_ * 32)) * inv_sig);
-            acc += fused_vertices<PH>(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys);
+            float2 unmx = make_float2(0.f, 0.f);
+            if (POLAR)
+#pragma unroll
+              for (int c = 0; c < 8; ++c) cfmaf_cj(unmx, ux[c], __ldg(Uk + c));
+            acc += fused_vertices<PH, POLAR>(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys, glb,
+                                             unmx);
           }
         }
       }
@@ -1302,11 +1346,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       float acc01 = 0.f;
       if (nbw > 0) {
         const float dn = (float)((E - __ldg(eb + n0 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH>(h0, rq, dn, a_occ, dnorm, d, vbase, q, yo, ys);
+        acc01 += fused_vertices<PH, POLAR>(h0, rq, dn, a_occ, dnorm, d, vbase, q, yo, ys, glb, unm0);
       }
       if (nbw > 1) {
         const float dn = (float)((E - __ldg(eb + n1 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH>(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q, yo, ys);
+        acc01 += fused_vertices<PH, POLAR>(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q, yo, ys, glb, unm1);
       }
       double v = (double)acc01 + (double)acc;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1373,10 +1417,12 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   // once per process: changing a kernel attribute can wait for the device's queued work
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(k_stageB_fused86<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
-    cudaFuncSetAttribute(k_stageB_fused86<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
   });
-  const bool ph = ed.phr || ed.yv;
+  const bool ph = ed.phr || ed.yv, polar = tabs.glb != nullptr;
   FusedArgs g;
   g.mtiles = MpB / BM;
   g.ntiles = (nst + 1) / 2;
@@ -1392,19 +1438,16 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   if (g.mtiles % 2) return tfail(1, "stage B: row tiles must pair");
   const int64_t pairs = (int64_t)(g.mtiles / 2) * g.ntiles;
   if (pairs > INT32_MAX) return tfail(1, "stage B: too many tiles");
-  if (ph)
-    return launch_pairs((const void *)k_stageB_fused86<true>, F_SMEM, pairs, st, chunk, yield,
+  auto run = [&](auto kernel) {
+    return launch_pairs((const void *)kernel, F_SMEM, pairs, st, chunk, yield,
                         [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
                           g.t0 = t0;
                           g.t1 = t1;
-                          return cudaLaunchKernelEx(&cfg, k_stageB_fused86<true>, ta, tb, g, tabs, rp, ed);
+                          return cudaLaunchKernelEx(&cfg, kernel, ta, tb, g, tabs, rp, ed);
                         });
-  return launch_pairs((const void *)k_stageB_fused86<false>, F_SMEM, pairs, st, chunk, yield,
-                      [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
-                        g.t0 = t0;
-                        g.t1 = t1;
-                        return cudaLaunchKernelEx(&cfg, k_stageB_fused86<false>, ta, tb, g, tabs, rp, ed);
-                      });
+  };
+  if (polar) return ph ? run(k_stageB_fused86<true, true>) : run(k_stageB_fused86<false, true>);
+  return ph ? run(k_stageB_fused86<true, false>) : run(k_stageB_fused86<false, false>);
 }
 
 // ------------------------------- stage A fused with the initial-band rotation
@@ -1946,7 +1989,14 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, et.cx, et.bs, et.w, et.v, trec);
   TCK(cudaGetLastError());
   *launches += 3;
-  const FusedTabs tabs{trow, tst, tU4, tens, trec, Mp, N};
+  float2 *tglb = nullptr;   // polar: long_range_prefac(q, u_s), q-blocked
+  if (ed_in.glpf) {
+    if ((rc = wsget(ws, "tc_fglb", (size_t)6 * rup(N, 32), &tglb))) return tfail(6, ws.msg.c_str());
+    k_fused_glp<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.glpf, tglb);
+    TCK(cudaGetLastError());
+    *launches += 1;
+  }
+  const FusedTabs tabs{trow, tst, tU4, tens, trec, tglb, Mp, N};
   // state operand: whole 8-state groups (8 x 48 = 384 rows), six planes; padding rows zero
   const int64_t Np2 = rup(nst, 8) * ncol;
   float *PA, *PB, *B2;

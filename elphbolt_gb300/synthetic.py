@@ -44,6 +44,9 @@ class Crystal:
     basis: np.ndarray           # (3, numatoms) crystal coordinates
     masses: np.ndarray          # (numatoms,) amu, one per atom
     T: float = 300.0            # K
+    polar: bool = False         # crys%polar: add the long-range dipole terms
+    epsilon: np.ndarray = None  # (3,3) high-frequency dielectric tensor
+    born: np.ndarray = None     # (3,3,numatoms) Born effective charges, born(:, ipol, iat)
 
     @property
     def numatoms(self) -> int:
@@ -273,6 +276,18 @@ def make_crystal_si_like() -> Crystal:
     return Crystal(lattvecs=fcc_lattvecs(5.43),
                    basis=np.array([[0.0, 0.25], [0.0, 0.25], [0.0, 0.25]]),
                    masses=np.array([28.0, 28.0]), T=300.0)
+
+
+def make_crystal_sic_like() -> Crystal:
+    """Zincblende SiC-like polar fcc cell: the lattice, masses, dielectric
+    constant and Born charges of 3C-SiC's input (test/3C-SiC/input.nml)."""
+    born = np.zeros((3, 3, 2))
+    born[:, :, 0] = 2.7514963 * np.eye(3)
+    born[:, :, 1] = -2.7514963 * np.eye(3)
+    return Crystal(lattvecs=fcc_lattvecs(4.33909462),
+                   basis=np.array([[0.0, 0.25], [0.0, 0.25], [0.0, 0.25]]),
+                   masses=np.array([28.0855, 12.011]), T=300.0,
+                   polar=True, epsilon=7.4190074 * np.eye(3), born=np.asfortranarray(born))
 
 
 def make_crystal_multi(natoms: int, rng, mass_range=(12.0, 60.0)) -> Crystal:

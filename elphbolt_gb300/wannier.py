@@ -81,6 +81,20 @@ class Wannier:
         check(L.ephg_create(ct.byref(d), ct.byref(h)))
         self._h = h
         self._L = L
+        if getattr(c, "polar", False):
+            self.set_polar(c.epsilon, c.born)
+
+    def set_polar(self, epsilon, born):
+        """crys%polar, epsilon (3,3), born (3,3,numatoms) (``ephg_set_polar``);
+        epsilon None switches the long-range terms off."""
+        if epsilon is None:
+            check(self._L.ephg_set_polar(self._h, None, None))
+            return
+        e = _f(epsilon)
+        b = _f(born)
+        if e.shape != (3, 3) or b.shape != (3, 3, self.crystal.numatoms):
+            raise ValueError("set_polar: epsilon must be (3,3) and born (3,3,numatoms)")
+        check(self._L.ephg_set_polar(self._h, _p(e), _p(b)))
 
     # ---- wannier.f90:430 ----
     def el_wann(self, crys=None, nk=None, kvecs=None, velocities=False, evecs=False, scissor=None):

@@ -109,6 +109,14 @@ const char *ephg_last_error(void);
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int ephg_device_count(void);
 
+/* The crystal fields of a polar crystal (crys%polar = .true.; crystal.f90:45-49):
+ * epsilon (3,3) the high-frequency dielectric tensor and born (3,3,numatoms)
+ * the Born effective charges, born(:, ipol, iat) as the reference reads them.
+ * From then on ph_wann adds dyn_nonanalytic (wannier.f90:784-901) to D(q) and
+ * every |g|^2 (g2, el_rates, ph_rates) adds long_range_prefac (:1013-1071)
+ * times the electron overlap (:998-1006).  epsilon NULL: non-polar again. */
+int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born);
+
 /* el_wann (wannier.f90:430-524): kvecs (nk,3) crystal coords -> energies
  * (nk,nw) eV; optional velocities (nk,nw,3) km/s, evecs (nk,nw,nw) with
  * evecs(k,b,:) the eigenvector of band b, scissor (nw) eV.  NULL = absent. */

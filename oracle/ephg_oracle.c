@@ -38,6 +38,7 @@ static const double hbar = 1.05457172647e-22;
 #define RYD2RADTHZ (0.5 * HARTREE2RADTHZ)
 #define RYD2EV (0.5 * 27.2116)
 #define RYD2AMU (2.0 * me / amu)
+#define BOHR2NM 0.052917721092   /* params.f90:53 */
 
 static inline cplx cget(const double *p, int64_t i) { return p[2 * i] + I * p[2 * i + 1]; }
 static inline void cset(double *p, int64_t i, cplx v) { p[2 * i] = creal(v); p[2 * i + 1] = cimag(v); }
@@ -312,6 +313,158 @@ int or_ws_wrapping_vectors(const double lvec[9], const double vl[3], double eps,
 
 /* ph_wann (non-polar branch): wannier.f90:585-782.  Returns 1 on a large
  * negative phonon energy (the reference stops there), else 0. */
+/* ======================= polar long-range terms ======================= */
+
+/* Reciprocal vectors (columns, 1/nm, with 2 pi) and cell volume (nm^3):
+ * crystal.f90:284-293.  Cartesian basis (nm): crystal.f90:282. */
+static void polar_cell(const or_wannier *w, double rec[9], double *vol, double *bc) {
+  const double *a = w->lattvecs;
+  for (int i = 0; i < 3; ++i) {
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    rec[0 + 3 * i] = a[1 + 3 * j] * a[2 + 3 * k] - a[2 + 3 * j] * a[1 + 3 * k];
+    rec[1 + 3 * i] = a[2 + 3 * j] * a[0 + 3 * k] - a[0 + 3 * j] * a[2 + 3 * k];
+    rec[2 + 3 * i] = a[0 + 3 * j] * a[1 + 3 * k] - a[1 + 3 * j] * a[0 + 3 * k];
+  }
+  *vol = fabs(a[0] * rec[0] + a[1] * rec[1] + a[2] * rec[2]);
+  for (int i = 0; i < 9; ++i) rec[i] *= TWOPI / *vol;
+  for (int64_t at = 0; at < w->natoms; ++at) matvec3(a, w->basis + 3 * at, bc + 3 * at);
+}
+
+/* q in crystal coordinates -> Cartesian 1/bohr: matmul(reclattvecs, q) * bohr2nm */
+void or_q_cart_bohr(const or_wannier *w, const double qf[3], double qc[3]) {
+  double rec[9], vol, bc[3 * 64];
+  polar_cell(w, rec, &vol, bc);
+  matvec3(rec, qf, qc);
+  for (int d = 0; d < 3; ++d) qc[d] *= BOHR2NM;
+}
+
+/* z(j) = sum_i g(i) born(i, j, at): matmul(g, born(:,:,at)) */
+static void gdotz(const double *born, int64_t at, const double g[3], double z[3]) {
+  for (int j = 0; j < 3; ++j) z[j] = g[0] * born[0 + 3 * j + 9 * at] + g[1] * born[1 + 3 * j + 9 * at] +
+                                     g[2] * born[2 + 3 * j + 9 * at];
+}
+
+static double geg(const double *eps, const double g[3]) {   /* dot_product(g, matmul(epsilon, g)) */
+  double acc = 0.0;
+  for (int i = 0; i < 3; ++i) acc += g[i] * (eps[i] * g[0] + eps[i + 3] * g[1] + eps[i + 6] * g[2]);
+  return acc;
+}
+
+/* dyn_nonanalytic: wannier.f90:784-901.  q Cartesian (1/bohr); dyn_l (nb,nb)
+ * complex, ddyn_l (nb,nb,3) complex or NULL, both in Ry / bohr units. */
+void or_dyn_nonanalytic(const or_wannier *w, const double q[3], double *dyn_l, double *ddyn_l) {
+  const int64_t nat = w->natoms, nb = 3 * nat;
+  const double *born = w->born, *eps = w->epsilon;
+  double rec[9], vol, bc[3 * 64];
+  polar_cell(w, rec, &vol, bc);
+  const double a1 = sqrt(w->lattvecs[0] * w->lattvecs[0] + w->lattvecs[1] * w->lattvecs[1] +
+                         w->lattvecs[2] * w->lattvecs[2]);
+  const double tpiba = TWOPI / a1 * BOHR2NM;
+  const double gmax = 14.0, alph = tpiba * tpiba;
+  const double fac = 8.0 * PI / (vol / (BOHR2NM * BOHR2NM * BOHR2NM));
+  cplx *D = (cplx *)calloc(nb * nb, sizeof(cplx));
+  cplx *dD = (cplx *)calloc(nb * nb * 3, sizeof(cplx));
+  const int64_t n1 = w->coarse_qmesh[0], n2 = w->coarse_qmesh[1], n3 = w->coarse_qmesh[2];
+  for (int64_t m1 = -n1; m1 <= n1; ++m1)
+    for (int64_t m2 = -n2; m2 <= n2; ++m2)
+      for (int64_t m3 = -n3; m3 <= n3; ++m3) {
+        double g[3];
+        for (int d = 0; d < 3; ++d)
+          g[d] = ((double)m1 * rec[d] + (double)m2 * rec[d + 3] + (double)m3 * rec[d + 6]) * BOHR2NM;
+        double qeq = geg(eps, g);
+        if (qeq > 0.0 && qeq / alph / 4.0 < gmax) {     /* the q-independent term (:843-867) */
+          const double facqd = exp(-qeq / alph / 4.0) / qeq;
+          for (int64_t iat = 0; iat < nat; ++iat) {
+            double zig[3], zjg[3];
+            gdotz(born, iat, g, zig);
+            cplx fnat[3] = {0, 0, 0};
+            for (int64_t jat = 0; jat < nat; ++jat) {
+              double rr[3];
+              for (int d = 0; d < 3; ++d) rr[d] = (bc[d + 3 * iat] - bc[d + 3 * jat]) / BOHR2NM;
+              const double arg = g[0] * rr[0] + g[1] * rr[1] + g[2] * rr[2];
+              gdotz(born, jat, g, zjg);
+              for (int d = 0; d < 3; ++d) fnat[d] += zjg[d] * expi(arg);
+            }
+            for (int ip = 0; ip < 3; ++ip)
+              for (int jp = 0; jp < 3; ++jp) D[(3 * iat + ip) + nb * (3 * iat + jp)] -= facqd * zig[ip] * fnat[jp];
+          }
+        }
+        for (int d = 0; d < 3; ++d) g[d] += q[d];
+        qeq = geg(eps, g);
+        if (qeq > 0.0 && qeq / alph / 4.0 < gmax) {     /* the G + q term (:869-897) */
+          const double facqd = exp(-qeq / alph / 4.0) / qeq;
+          double dgeg[3];
+          for (int i = 0; i < 3; ++i)
+            dgeg[i] = (eps[i] + eps[3 * i]) * g[0] + (eps[i + 3] + eps[3 * i + 1]) * g[1] +
+                      (eps[i + 6] + eps[3 * i + 2]) * g[2];
+          const double dgeg_coeff = 0.25 / alph + 1.0 / qeq;
+          for (int64_t iat = 0; iat < nat; ++iat) {
+            double zig[3], zjg[3];
+            gdotz(born, iat, g, zig);
+            for (int64_t jat = 0; jat < nat; ++jat) {
+              double rr[3];
+              for (int d = 0; d < 3; ++d) rr[d] = (bc[d + 3 * iat] - bc[d + 3 * jat]) / BOHR2NM;
+              gdotz(born, jat, g, zjg);
+              const double arg = g[0] * rr[0] + g[1] * rr[1] + g[2] * rr[2];
+              const cplx facq = facqd * expi(arg);
+              for (int ip = 0; ip < 3; ++ip)
+                for (int jp = 0; jp < 3; ++jp) {
+                  const int64_t ij = (3 * iat + ip) + nb * (3 * jat + jp);
+                  D[ij] += facq * zig[ip] * zjg[jp];
+                  if (ddyn_l)
+                    for (int x = 0; x < 3; ++x)
+                      dD[ij + nb * nb * x] += facq * (zjg[jp] * born[x + 3 * ip + 9 * iat] +
+                                                      zig[ip] * born[x + 3 * jp + 9 * jat] +
+                                                      zig[ip] * zjg[jp] * (I * rr[x] - dgeg_coeff * dgeg[x]));
+                }
+            }
+          }
+        }
+      }
+  for (int64_t i = 0; i < nb * nb; ++i) cset(dyn_l, i, D[i] * fac);
+  if (ddyn_l)
+    for (int64_t i = 0; i < 3 * nb * nb; ++i) cset(ddyn_l, i, dD[i] * fac);
+  free(D);
+  free(dD);
+}
+
+/* long_range_prefac: wannier.f90:1013-1071.  q Cartesian (1/bohr), uqs (nb)
+ * complex = the mass-scaled phonon eigenvector; returns glprefac (Ry units). */
+void or_long_range_prefac(const or_wannier *w, const double q[3], const double *uqs, double *glprefac) {
+  const int64_t nat = w->natoms;
+  const double *born = w->born, *eps = w->epsilon;
+  double rec[9], vol, bc[3 * 64];
+  polar_cell(w, rec, &vol, bc);
+  const double a1 = sqrt(w->lattvecs[0] * w->lattvecs[0] + w->lattvecs[1] * w->lattvecs[1] +
+                         w->lattvecs[2] * w->lattvecs[2]);
+  const double tpiba = TWOPI / a1 * BOHR2NM;
+  const double gmax = 14.0, alph = tpiba * tpiba;
+  const cplx fac = 8.0 * PI / (vol / (BOHR2NM * BOHR2NM * BOHR2NM)) * I;
+  cplx acc = 0.0;
+  const int64_t n1 = w->coarse_qmesh[0], n2 = w->coarse_qmesh[1], n3 = w->coarse_qmesh[2];
+  for (int64_t m1 = -n1; m1 <= n1; ++m1)
+    for (int64_t m2 = -n2; m2 <= n2; ++m2)
+      for (int64_t m3 = -n3; m3 <= n3; ++m3) {
+        double g[3];
+        for (int d = 0; d < 3; ++d)
+          g[d] = ((double)m1 * rec[d] + (double)m2 * rec[d + 3] + (double)m3 * rec[d + 6]) * BOHR2NM + q[d];
+        const double qeq = geg(eps, g);
+        if (qeq > 0.0 && qeq / alph / 4.0 < gmax) {
+          const double facqd = exp(-qeq / alph / 4.0) / qeq;
+          for (int64_t na = 0; na < nat; ++na) {
+            const double arg = -(g[0] * bc[3 * na] + g[1] * bc[3 * na + 1] + g[2] * bc[3 * na + 2]) / BOHR2NM;
+            const cplx facq = facqd * expi(arg);
+            for (int ip = 0; ip < 3; ++ip) {
+              const double zaq = g[0] * born[0 + 3 * ip + 9 * na] + g[1] * born[1 + 3 * ip + 9 * na] +
+                                 g[2] * born[2 + 3 * ip + 9 * na];
+              acc += facq * zaq * cget(uqs, 3 * na + ip);
+            }
+          }
+        }
+      }
+  cset(glprefac, 0, acc * fac);
+}
+
 int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *energies,
                double *evecs, double *velocities) {
   const int64_t nb = w->nb, nwsq = w->nwsq, nat = w->natoms;
@@ -320,7 +473,7 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
   cplx *dyn = (cplx *)malloc(sizeof(cplx) * nb * nb);
   cplx *ddyn = (cplx *)malloc(sizeof(cplx) * nb * nb * 3);
   double *Dd = (double *)malloc(sizeof(double) * 2 * nb * nb);
-  double *V = (double *)malloc(sizeof(double) * 2 * nb * nb);
+  double *V = (double *)malloc(sizeof(double) * 2 * nb * nb * 3);
   double *om2 = (double *)malloc(sizeof(double) * nb);
   int64_t wr[3 * 512];
   for (int64_t iq = 0; iq < nq; ++iq) {
@@ -359,6 +512,16 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
           if (velocities)
             for (int p = 0; p < 3; ++p) ddyn[i + nb * (j + nb * p)] += I * rcart[p] * t;
         }
+    }
+    /* non-analytic correction (:684-705) */
+    if (w->polar) {
+      const double qf[3] = {qvecs[iq], qvecs[iq + nq], qvecs[iq + 2 * nq]};
+      double qc[3];
+      or_q_cart_bohr(w, qf, qc);
+      or_dyn_nonanalytic(w, qc, Dd, velocities ? V : NULL);   /* Dd, V as scratch */
+      if (velocities)
+        for (int64_t i = 0; i < 3 * nb * nb; ++i) ddyn[i] += cget(V, i) * BOHR2NM;
+      for (int64_t i = 0; i < nb * nb; ++i) dyn[i] += cget(Dd, i);
     }
     /* force Hermiticity (:708-713) */
     for (int64_t ib = 0; ib < nb; ++ib)
@@ -495,6 +658,15 @@ double or_g2(const or_wannier *w, const double kvec[3], const double qvec[3],
     gbloch += caux * ukgu;
   }
   free(ukg);
+  if (w->polar) {   /* long-range correction (:998-1006) */
+    cplx unm = 0.0;   /* dot_product(el_evec_kp, el_evec_k) */
+    for (int64_t c = 0; c < nw; ++c) unm += conj(cget(el_evec_kp, c)) * cget(el_evec_k, c);
+    double qc[3], uu[128], gl[2];
+    or_q_cart_bohr(w, qvec, qc);
+    for (int64_t ip = 0; ip < nb; ++ip) cset(uu, ip, u[ip]);
+    or_long_range_prefac(w, qc, uu, gl);
+    gbloch += (gl[0] + I * gl[1]) * unm;
+  }
   return 0.5 * creal(gbloch * conj(gbloch)) / ph_en * g2unitfactor;
 }
 
@@ -1014,6 +1186,15 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
               } else {
                 cplx gb = 0.0;
                 for (int64_t sp = 0; sp < nb; ++sp) gb += cget(evq, sp) / sqrt(w->masses[sp / 3]) * hs[sp];
+                if (w->polar) {   /* long-range term of g2 (wannier.f90:998-1006) */
+                  cplx unm = 0.0;
+                  for (int64_t c = 0; c < nw; ++c) unm += conj(cget(evkp, c)) * cget(evk, c);
+                  double qc[3], uu[128], gl[2];
+                  or_q_cart_bohr(w, qv, qc);
+                  for (int64_t sp = 0; sp < nb; ++sp) cset(uu, sp, cget(evq, sp) / sqrt(w->masses[sp / 3]));
+                  or_long_range_prefac(w, qc, uu, gl);
+                  gb += (gl[0] + I * gl[1]) * unm;
+                }
                 g2 = 0.5 * creal(gb * conj(gb)) / en_ph * g2unitfactor;
               }
               /* 'X' (:2278-2332) */

@@ -7,8 +7,10 @@
  * It restates, function by function, the reference's Fortran (all FP64):
  *   el_wann               src/wannier.f90:430-524
  *   ws_wrapping_vectors   src/wannier.f90:532-582
- *   ph_wann (non-polar)   src/wannier.f90:585-782
- *   g2 (non-polar)        src/wannier.f90:903-1011
+ *   ph_wann               src/wannier.f90:585-782
+ *   dyn_nonanalytic       src/wannier.f90:784-901
+ *   g2                    src/wannier.f90:903-1011
+ *   long_range_prefac     src/wannier.f90:1013-1071
  *   gkRp                  src/wannier.f90:1073-1132
  *   gReq                  src/wannier.f90:1134-1188
  *   ibzk 'g' + 'X'        src/interactions.f90:2095-2400
@@ -56,6 +58,9 @@ typedef struct {
   const double *Hwann;      /* complex (nwsk,nw,nw) Ry */
   const double *Dphwann;    /* complex (nwsq,nb,nb) Ry/bohr^2 */
   const double *gwann;      /* complex (nw,nw,nwsk,nb,nwsg) Ry/bohr */
+  int64_t polar;            /* crys%polar: add the long-range terms */
+  const double *epsilon;    /* (3,3) high-frequency dielectric tensor */
+  const double *born;       /* (3,3,natoms) Born effective charges */
 } or_wannier;
 
 typedef struct {
@@ -96,6 +101,11 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
                double *evecs, double *velocities);
 void or_gkRp(const or_wannier *w, const double kvec[3], double *gmixed);
 void or_gReq(const or_wannier *w, const double qvec[3], double *gmixed);
+/* polar: dyn_nonanalytic (wannier.f90:784-901) and long_range_prefac
+ * (:1013-1071), q Cartesian in 1/bohr (or_q_cart_bohr converts crystal q) */
+void or_q_cart_bohr(const or_wannier *w, const double qf[3], double qc[3]);
+void or_dyn_nonanalytic(const or_wannier *w, const double q[3], double *dyn_l, double *ddyn_l);
+void or_long_range_prefac(const or_wannier *w, const double q[3], const double *uqs, double *glprefac);
 double or_g2(const or_wannier *w, const double kvec[3], const double qvec[3],
              const double *el_evec_k, const double *el_evec_kp, const double *ph_evec_q,
              double ph_en, const double *gmixed, int wannspace_ph);

@@ -28,7 +28,8 @@ class OrWannier(ct.Structure):
                 ("lattvecs", c_dp), ("basis", c_dp), ("masses", c_dp),
                 ("rcells_k", c_i64p), ("rcells_q", c_i64p), ("rcells_g", c_i64p),
                 ("elwsdeg", c_i64p), ("phwsdeg", c_i64p), ("gwsdeg", c_i64p),
-                ("Hwann", c_dp), ("Dphwann", c_dp), ("gwann", c_dp)]
+                ("Hwann", c_dp), ("Dphwann", c_dp), ("gwann", c_dp),
+                ("polar", ct.c_int64), ("epsilon", c_dp), ("born", c_dp)]
 
 
 class OrRequest(ct.Structure):
@@ -112,6 +113,10 @@ class Wannier:
         s.rcells_k, s.rcells_q, s.rcells_g = _p(self.rk, c_i64p), _p(self.rq, c_i64p), _p(self.rg, c_i64p)
         s.elwsdeg, s.phwsdeg, s.gwsdeg = _p(self.dk, c_i64p), _p(self.dq, c_i64p), _p(self.dg, c_i64p)
         s.Hwann, s.Dphwann, s.gwann = _p(self.H), _p(self.D), _p(self.G)
+        if getattr(c, "polar", False):
+            self.eps = keep(_f64(c.epsilon))
+            self.born = keep(_f64(c.born))
+            s.polar, s.epsilon, s.born = 1, _p(self.eps), _p(self.born)
         self.s = s
         self.nw, self.nb = wd.numwannbands, wd.numbranches
 
@@ -137,6 +142,33 @@ class Wannier:
         st = lib().or_ph_wann(ct.byref(self.s), ct.c_int64(nq), _p(q), _p(e),
                               _p(v) if v is not None else None, _p(vel) if vel is not None else None)
         return e, v, vel, st
+
+    def dyn_nonanalytic(self, q_cart_bohr, velocities=False):
+        """dyn_l (nb,nb) [, ddyn_l (nb,nb,3)] for q Cartesian in 1/bohr."""
+        L = lib()
+        L.or_dyn_nonanalytic.argtypes = [ct.c_void_p, c_dp, c_dp, c_dp]
+        q = np.ascontiguousarray(q_cart_bohr, dtype=np.float64)
+        d = np.zeros((self.nb, self.nb), dtype=np.complex128, order="F")
+        dd = np.zeros((self.nb, self.nb, 3), dtype=np.complex128, order="F") if velocities else None
+        L.or_dyn_nonanalytic(ct.byref(self.s), _p(q), _p(d), _p(dd) if dd is not None else None)
+        return (d, dd) if velocities else d
+
+    def long_range_prefac(self, q_cart_bohr, uqs):
+        L = lib()
+        L.or_long_range_prefac.argtypes = [ct.c_void_p, c_dp, c_dp, c_dp]
+        q = np.ascontiguousarray(q_cart_bohr, dtype=np.float64)
+        u = np.ascontiguousarray(uqs, dtype=np.complex128)
+        out = np.zeros(1, dtype=np.complex128)
+        L.or_long_range_prefac(ct.byref(self.s), _p(q), _p(u), _p(out))
+        return complex(out[0])
+
+    def q_cart_bohr(self, qf):
+        L = lib()
+        L.or_q_cart_bohr.argtypes = [ct.c_void_p, c_dp, c_dp]
+        q = np.ascontiguousarray(qf, dtype=np.float64)
+        out = np.zeros(3)
+        L.or_q_cart_bohr(ct.byref(self.s), _p(q), _p(out))
+        return out
 
     def gkRp(self, kvec):
         out = np.zeros((self.nw, self.nw, self.nb, self.wd.nwsq), dtype=np.complex128, order="F")

@@ -18,6 +18,9 @@ def case(name):
     elif name == "si8":         # nw 8, 2 atoms, 3^3 WS supercell, odd mesh
         wd = S.make_wannier(S.make_crystal_si_like(), 8, supercell=(3, 3, 3), seed=12)
         mesh, win, shift = (5, 5, 5), 0.5, 0.6
+    elif name == "sic":         # polar SiC-like crystal: the long-range terms on, nw 8, 3^3 WS supercell
+        wd = S.make_wannier(S.make_crystal_sic_like(), 8, supercell=(3, 3, 3), seed=14)
+        mesh, win, shift = (4, 4, 4), 0.6, 0.5
     elif name == "odd":         # nw 5 (odd Jacobi), 3 atoms (nb 9), non-cubic mesh
         rng = np.random.Generator(np.random.PCG64(7))
         crys = S.make_crystal_multi(3, rng)
@@ -29,4 +32,4 @@ def case(name):
     return wd, req
 
 
-CASES = ["tiny", "si8", "odd"]
+CASES = ["tiny", "si8", "odd", "sic"]

@@ -1,6 +1,6 @@
 """Generate the golden fixtures of tests/golden/ (run from the repository root).
 
-    python tests/golden/make_golden.py [el | ph | all]
+    python tests/golden/make_golden.py [el | ph | polar | all]
 
 For each small seeded workload this script computes the e-ph path twice:
 - with the C oracle (oracle/ephg_oracle.c, literal per-vertex g2);
@@ -45,8 +45,58 @@ def np_el_wann(wd, k):
     return w * C.Ryd2eV, np.transpose(V, (0, 2, 1))
 
 
+def np_polar(crys, nqc):
+    """The polar long-range terms, vectorised over the G box (wannier.f90:784-901,
+    1013-1071): returns dyn(q) -> (nb, nb) and lvec(q) -> (nb,), q Cartesian in
+    1/bohr, with long_range_prefac(q, u) = lvec(q) @ u."""
+    rec, vol = crys.reclattvecs, crys.volume
+    bc = crys.lattvecs @ crys.basis                                # nm
+    nat = crys.numatoms
+    nb = 3 * nat
+    tpiba = 2 * math.pi / np.linalg.norm(crys.lattvecs[:, 0]) * C.bohr2nm
+    alph, gmax = tpiba ** 2, 14.0
+    fac = 8 * math.pi / (vol / C.bohr2nm ** 3)
+    r = [np.arange(-n, n + 1) for n in nqc]
+    m = np.stack(np.meshgrid(*r, indexing="ij"), -1).reshape(-1, 3)
+    G = (m @ rec.T) * C.bohr2nm
+    eps, born = np.asarray(crys.epsilon), np.asarray(crys.born)
+    rr = (bc[:, :, None] - bc[:, None, :]) / C.bohr2nm              # rr[:, i, j]
+
+    def terms(g):
+        qeq = np.einsum("gi,ij,gj->g", g, eps, g)
+        sel = (qeq > 0) & (qeq / alph / 4 < gmax)
+        g, qeq = g[sel], qeq[sel]
+        f = np.exp(-qeq / alph / 4) / qeq
+        Z = np.einsum("gi,ija->gaj", g, born)                        # (g, atom, j)
+        ph = np.exp(1j * np.einsum("gd,dij->gij", g, rr))            # e^{i g.r_ij}
+        return g, f, Z, ph
+
+    _, fa, Za, pha = terms(G)
+    fnat = np.einsum("gbj,gab->gaj", Za, pha)
+    Da = np.zeros((nb, nb), dtype=complex)
+    for a in range(nat):
+        Da[3 * a:3 * a + 3, 3 * a:3 * a + 3] -= np.einsum("g,gi,gj->ij", fa, Za[:, a, :], fnat[:, a, :])
+
+    def dyn(q):
+        _, f, Z, ph = terms(G + q)
+        Db = np.einsum("g,gab,gai,gbj->aibj", f, ph, Z, Z).reshape(nb, nb)
+        return (Da + Db) * fac
+
+    def lvec(q):
+        g, f, Z, _ = terms(G + q)
+        pa = np.exp(-1j * (g @ bc) / C.bohr2nm)                       # (g, atom)
+        return (1j * fac) * np.einsum("g,ga,gaj->aj", f, pa, Z).reshape(nb)
+
+    return dyn, lvec
+
+
+def q_cart(crys, qf):
+    return (np.atleast_2d(qf) @ crys.reclattvecs.T) * C.bohr2nm
+
+
 def np_ph_wann(wd, q):
-    """D(q) with WS wrapping (wannier.f90:631-665), mass-normalised, LAPACK eigen."""
+    """D(q) with WS wrapping (wannier.f90:631-665), the non-analytic term for a
+    polar crystal (:684-705), mass-normalised, LAPACK eigen."""
     c = wd.crystal
     nat, nb = c.numatoms, wd.numbranches
     D = np.zeros((len(q), nb, nb), dtype=complex)
@@ -62,7 +112,10 @@ def np_ph_wann(wd, q):
                 cs /= (wd.phwsdeg[iuc] * len(wr))
                 D[:, 3 * iat:3 * iat + 3, 3 * jat:3 * jat + 3] += cs[:, None, None] * \
                     np.asarray(wd.Dphwann)[iuc, 3 * iat:3 * iat + 3, 3 * jat:3 * jat + 3]
-    Du = np.triu(D, 1)
+    if getattr(c, "polar", False):
+        dyn, _ = np_polar(c, wd.coarse_qmesh)
+        D = D + np.array([dyn(qc) for qc in q_cart(c, q)])
+    Du = np.triu(0.5 * (D + np.conj(np.transpose(D, (0, 2, 1)))), 1)
     D = Du + np.conj(np.transpose(Du, (0, 2, 1))) + np.einsum("kii->ki", D).real[:, :, None] * np.eye(nb)
     m = np.repeat(c.masses, 3)
     D = D / np.sqrt(np.outer(m, m))[None] * C.Ryd2amu
@@ -90,6 +143,10 @@ def np_rates(wd, req):
     g = np.asarray(wd.gwann)
     ph_k = np.exp(2j * np.pi * (ks[idx] @ wd.rcells_k.T)) / wd.elwsdeg[None, :]
     kT = C.kB * req.T
+    polar = getattr(wd.crystal, "polar", False)
+    if polar:   # long_range_prefac(q, u_s) for every q of the mesh and mode s
+        _, lvec = np_polar(wd.crystal, wd.coarse_qmesh)
+        glp = np.array([u[i] @ lvec(qc) for i, qc in enumerate(q_cart(wd.crystal, ks))])   # (N, nb)
     rates = np.zeros((len(idx), nw))
     g2_all, xp_all, xm_all = [], [], []
     win_kp = np.abs(ens - req.enref) <= req.fsthick
@@ -111,6 +168,8 @@ def np_rates(wd, req):
                         continue
                     h = np.conj(U[ikp, n]) @ G[ikp]            # (s')
                     gs = u[iq[ikp]] @ h                         # (s)
+                    if polar:                                   # + glprefac * unm (wannier.f90:998-1006)
+                        gs = gs + glp[iq[ikp]] * (np.conj(U[ikp, n]) @ U[ik, m])
                     o = om[iq[ikp]]
                     with np.errstate(divide="ignore", invalid="ignore"):
                         g2 = np.where(o == 0, 0.0, 0.5 * np.abs(gs) ** 2 / o * C.g2unitfactor)
@@ -152,6 +211,9 @@ def np_ph_rates(wd, req, spindeg=2):
     win = np.abs(ens - req.enref) <= req.fsthick
     kT = C.kB * req.T
     fermi = lambda e: 1.0 / (np.exp((e - req.chempot) / kT) + 1.0)
+    polar = getattr(wd.crystal, "polar", False)
+    if polar:
+        _, lvec = np_polar(wd.crystal, wd.coarse_qmesh)
     rates = np.zeros((N, nb))
     g2_all, y_all = [], []
     for iq in range(N):
@@ -162,6 +224,7 @@ def np_ph_rates(wd, req, spindeg=2):
         ikp_all = pos[kp[:, 0] + mesh[0] * (kp[:, 1] + mesh[1] * kp[:, 2])]
         g2q, occ_delta = [], []                                    # per vertex: (nb,) arrays
         o = om[iq]
+        glp = u[iq] @ lvec(q_cart(wd.crystal, qi / mesh)[0]) if polar else None
         with np.errstate(divide="ignore", invalid="ignore"):
             invb = np.where(o != 0, 1.0 / (1.0 + 1.0 / np.expm1(np.where(o != 0, o, 1.0) / kT)), 0.0)
         for ik in range(len(idx)):
@@ -178,6 +241,8 @@ def np_ph_rates(wd, req, spindeg=2):
                         continue
                     h = np.einsum("i,ijs,j->s", np.conj(U[ikp, n]), gk, U[ik, m])
                     gs = u[iq] @ h
+                    if polar:
+                        gs = gs + glp * (np.conj(U[ikp, n]) @ U[ik, m])
                     with np.errstate(divide="ignore", invalid="ignore"):
                         g2 = np.where(o == 0, 0.0, 0.5 * np.abs(gs) ** 2 / o * C.g2unitfactor)
                     x = (ens[ikp, n] - o - E) / req.sigma
@@ -200,19 +265,24 @@ CASES = {
     "tiny": dict(nw=4, supercell=(2, 2, 2), seed=11, mesh=(4, 4, 4), window=1.0, shift=0.3),
     "si8": dict(nw=8, supercell=(3, 3, 3), seed=12, mesh=(4, 4, 4), window=0.5, shift=0.6),
 }
+# polar (SiC-like, long-range terms on): written by "polar", not by "el" / "ph"
+POLAR_CASES = {
+    "sic": dict(nw=8, supercell=(3, 3, 3), seed=14, mesh=(4, 4, 4), window=0.6, shift=0.5, crystal="sic"),
+}
 
 
 def build_case(name):
-    c = CASES[name]
-    wd = S.make_wannier(S.make_crystal_si_like(), c["nw"], supercell=c["supercell"], seed=c["seed"])
+    c = CASES[name] if name in CASES else POLAR_CASES[name]
+    crys = S.make_crystal_sic_like() if c.get("crystal") == "sic" else S.make_crystal_si_like()
+    wd = S.make_wannier(crys, c["nw"], supercell=c["supercell"], seed=c["seed"])
     req = S.si_like_request(wd, c["mesh"], window=c["window"], shift=c["shift"])
     return wd, req
 
 
-def main_ph():
+def main_ph(names=tuple(CASES)):
     """golden_ph_<case>.npz: the phonon side (ibzq 'g' + 'Y', ph-e rates), spindeg 2."""
     from oracle import oracle as O
-    for name in CASES:
+    for name in names:
         wd, req = build_case(name)
         ref = np_ph_rates(wd, req, spindeg=2)
         o = O.Wannier(wd).ph_rates(req, spindeg=2, nthreads=os.cpu_count(), vertices=True)
@@ -230,9 +300,9 @@ def main_ph():
                                                              rel(o["rates_phe"], ref["rates_phe"])))
 
 
-def main():
+def main(names=tuple(CASES)):
     from oracle import oracle as O
-    for name in CASES:
+    for name in names:
         wd, req = build_case(name)
         ref = np_rates(wd, req)
         o = O.Wannier(wd).el_rates(req, literal=True, vertices=True)
@@ -258,3 +328,6 @@ if __name__ == "__main__":
         main()
     if what in ("ph", "all"):
         main_ph()
+    if what in ("polar", "all"):
+        main(tuple(POLAR_CASES))
+        main_ph(tuple(POLAR_CASES))

@@ -17,13 +17,15 @@ import pytest
 from elphbolt_gb300 import _lib, synthetic as S
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = {"tiny": dict(nw=4, supercell=(2, 2, 2), seed=11), "si8": dict(nw=8, supercell=(3, 3, 3), seed=12)}
+CASES = {"tiny": dict(nw=4, supercell=(2, 2, 2), seed=11), "si8": dict(nw=8, supercell=(3, 3, 3), seed=12),
+         "sic": dict(nw=8, supercell=(3, 3, 3), seed=14, polar=True)}
 
 
 def load(name):
     z = np.load(os.path.join(HERE, "golden_%s.npz" % name))
     c = CASES[name]
-    wd = S.make_wannier(S.make_crystal_si_like(), c["nw"], supercell=c["supercell"], seed=c["seed"])
+    crys = S.make_crystal_sic_like() if c.get("polar") else S.make_crystal_si_like()
+    wd = S.make_wannier(crys, c["nw"], supercell=c["supercell"], seed=c["seed"])
     req = S.RateRequest(mesh=tuple(int(x) for x in z["mesh"]), enref=float(z["enref"]), fsthick=float(z["fsthick"]),
                         chempot=float(z["chempot"]), T=float(z["T"]), delta_kind=0, sigma=float(z["sigma"]))
     return wd, req, z

@@ -181,3 +181,61 @@ def test_ph_rates_spindeg_and_detailed_balance(oracle_lib, name):
     assert np.all(b["y"][~keep] == 0)
     pred = xp * f[keep] * (1 - f[keep]) / (n * (1 + n))
     assert np.max(np.abs(pred - y)) <= 1e-10 * np.abs(y).max()
+
+
+def test_polar_terms_vs_numpy(oracle_lib):
+    """dyn_nonanalytic and long_range_prefac (wannier.f90:784-901, 1013-1071): the
+    oracle's loops against the vectorised numpy restatement of the golden
+    generator, at random q and for random mode vectors."""
+    from tests.golden.make_golden import np_polar, q_cart
+    wd, _ = case("sic")
+    W = oracle_lib.Wannier(wd)
+    dyn, lvec = np_polar(wd.crystal, wd.coarse_qmesh)
+    rng = np.random.default_rng(5)
+    qfs = np.concatenate([rng.uniform(-1, 1, (6, 3)), [[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]]])
+    # one scale for all q: at Gamma the vector is rounding noise (its G and -G terms cancel)
+    lscale = max(np.abs(lvec(q_cart(wd.crystal, qf)[0])).sum() for qf in qfs)
+    for qf in qfs:
+        qc = W.q_cart_bohr(qf)
+        assert np.allclose(qc, q_cart(wd.crystal, qf)[0], rtol=1e-14, atol=0)
+        d = W.dyn_nonanalytic(qc)
+        ref = dyn(qc)
+        assert np.max(np.abs(d - ref)) <= 1e-12 * np.abs(ref).max()
+        u = rng.standard_normal(wd.numbranches) + 1j * rng.standard_normal(wd.numbranches)
+        gl = W.long_range_prefac(qc, u)
+        glr = lvec(qc) @ u
+        assert abs(gl - glr) <= 1e-12 * abs(glr) + 1e-13 * lscale * np.abs(u).max()
+
+
+def test_polar_velocity_term_is_the_derivative(oracle_lib):
+    """ddyn_l of dyn_nonanalytic is d(dyn_l)/dq (Cartesian): central differences."""
+    wd, _ = case("sic")
+    W = oracle_lib.Wannier(wd)
+    rng = np.random.default_rng(6)
+    h = 1e-5
+    for qf in rng.uniform(-1, 1, (4, 3)):
+        qc = W.q_cart_bohr(qf)
+        _, dd = W.dyn_nonanalytic(qc, velocities=True)
+        for x in range(3):
+            e = np.zeros(3)
+            e[x] = h
+            fd = (W.dyn_nonanalytic(qc + e) - W.dyn_nonanalytic(qc - e)) / (2 * h)
+            assert np.max(np.abs(fd - dd[:, :, x])) <= 1e-6 * np.abs(dd).max()
+
+
+def test_polar_phonons(oracle_lib):
+    """The polar crystal's phonons: the long-range term is Hermitian and keeps
+    the acoustic sum rule (three zero modes at Gamma), and it changes the
+    optical branches against the same crystal without it."""
+    wd, req = case("sic")
+    W = oracle_lib.Wannier(wd)
+    for qf in [[0.1, 0.2, 0.3], [0.5, 0.5, 0.0]]:
+        d = W.dyn_nonanalytic(W.q_cart_bohr(qf))
+        assert np.max(np.abs(d - d.conj().T)) <= 1e-12 * np.abs(d).max()
+    qs = S.mesh_kvecs(req.mesh)
+    e, _, _, st = W.ph_wann(qs)
+    assert st == 0 and np.all(e[0, :3] == 0) and np.all(e >= 0)
+    c = wd.crystal
+    wd0 = S.make_wannier(S.Crystal(c.lattvecs, c.basis, c.masses), 8, supercell=(3, 3, 3), seed=14)
+    e0, _, _, _ = oracle_lib.Wannier(wd0).ph_wann(qs)
+    assert np.abs(e - e0)[1:, 3:].max() > 1e-3
