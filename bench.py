@@ -246,6 +246,44 @@ def polar_side(steps):
             "what": "ephg_ph_rates with ephg_set_polar: both rate sets in one split sweep, long-range terms on"}
 
 
+def symmetry_side(steps):
+    """Crystal symmetry (ephg_set_symmetry): a symmetric model of the bench
+    crystal -- Si-like fcc 2-atom cell, 4 s-like Wannier functions per atom
+    (nw 8), central springs, bond-stretching e-ph coupling, 6^3 WS sets -- with
+    the bench request's mesh and window.  The electron rates over the full
+    zone and over the irreducible wedge (48 rotations), and the wedge's split
+    rates against its FP64 form."""
+    import numpy as np
+    from elphbolt_gb300 import _lib, synthetic as S, symmetry as Y
+    from elphbolt_gb300.wannier import Wannier
+    wd = S.make_wannier_symmetric(S.make_crystal_si_like(), 4, supercell=(6, 6, 6), seed=20260106)
+    req = S.si_like_request(wd, MESH)
+    R, _ = Y.crystal_symmetry(wd.crystal)
+    W = Wannier(wd)
+    try:
+        split = lambda: W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+        split()
+        full = [split() for _ in range(max(3, steps))]
+        W.set_symmetry(R)
+        split()
+        ibz = [split() for _ in range(max(3, steps))]
+        f = W.el_rates(req, precision=_lib.PREC_FP64)
+    finally:
+        W.deallocate_wannier()
+    tf = float(np.median([r["stats"]["ms_total"] for r in full]))
+    ti = float(np.median([r["stats"]["ms_total"] for r in ibz]))
+    s, st = ibz[-1], ibz[-1]["stats"]
+    m = f["rates"] > 0
+    err = float(np.max(np.abs(s["rates"][m] - f["rates"][m]) / f["rates"][m])) if m.any() else None
+    return {"workload": "symmetric Si-like model (4 s orbitals per atom, nw 8, 6^3 WS), %dx%dx%d mesh" % MESH,
+            "rotations": len(R), "full_zone_ms_per_step": tf, "ibz_ms_per_step": ti, "speedup": tf / ti,
+            "full_zone_rows": full[-1]["nwv"], "ibz_rows": s["nwv"], "full_zone_vertices": full[-1]["stats"]["vertices"],
+            "ibz_vertices": st["vertices"], "ibz_stage_ms": {"setup": st["ms_setup"], "stage_a": st["ms_stage_a"],
+                                                             "stage_bc": st["ms_stage_bc"]},
+            "fp64_ibz_ms_per_step": f["stats"]["ms_total"], "ibz_rates_max_rel_vs_fp64": err,
+            "what": "ephg_set_symmetry + ephg_el_rates: initial states on the irreducible window points"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -390,6 +428,11 @@ def run_ours(args, ws, rank, local):
             line["polar"] = polar_side(args.steps)
         except Exception as e:   # the main line is still printed
             line["polar"] = {"error": repr(e)}
+    if not args.no_symmetry:
+        try:
+            line["symmetry"] = symmetry_side(args.steps)
+        except Exception as e:   # the main line is still printed
+            line["symmetry"] = {"error": repr(e)}
     if serving is not None:
         line["serving"] = serving
     print(json.dumps(line), flush=True)
@@ -461,6 +504,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop (p50 / p99 latency) measurement")
     ap.add_argument("--no-polar", action="store_true", help="skip the polar-crystal measurement")
+    ap.add_argument("--no-symmetry", action="store_true", help="skip the crystal-symmetry measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1 and args.impl == "ours":

@@ -17,6 +17,7 @@
 #include "ephg_tc.cuh"
 #include "ephg_ws.cuh"
 #include "ephg_handle.cuh"
+#include "ephg_sym.cuh"
 
 using namespace ephg;
 
@@ -423,6 +424,101 @@ int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born) {
   return EPHG_OK;
 }
 
+// ------------------------------------------------------------- symmetry
+int ephg_crystal_symmetry(const double *lattvecs, int64_t natoms, const double *basis, const int64_t *atomtypes,
+                          double symprec, int64_t maxops, int64_t *nops, int64_t *rotations, double *translations) {
+  if (!lattvecs || natoms < 1 || !basis || !atomtypes || !nops || (maxops > 0 && !rotations))
+    return fail(EPHG_ERR_ARG, "crystal_symmetry: bad arguments");
+  std::vector<ephg::SymOp> ops;
+  if (ephg::crystal_symmetry(lattvecs, (int)natoms, basis, atomtypes, symprec, ops))
+    return fail(EPHG_ERR_ARG, "crystal_symmetry: no symmetry found (symprec must be > 0)");
+  *nops = (int64_t)ops.size();
+  if ((int64_t)ops.size() > maxops)
+    return fail(EPHG_ERR_ARG, "crystal_symmetry: %lld operations, room for %lld", (long long)ops.size(),
+                (long long)maxops);
+  for (size_t o = 0; o < ops.size(); ++o) {
+    for (int k = 0; k < 9; ++k) rotations[9 * o + k] = ops[o].W[k];
+    if (translations)
+      for (int d = 0; d < 3; ++d) translations[3 * o + d] = ops[o].t[d];
+  }
+  return EPHG_OK;
+}
+
+int ephg_set_symmetry(ephg_handle *h, int64_t nsymm, const int64_t *rotations) {
+  if (!h || nsymm < 0 || (nsymm > 0 && !rotations) || nsymm > 192)
+    return fail(EPHG_ERR_ARG, "set_symmetry: bad arguments");
+  h->sym_rot.assign(rotations, rotations + 9 * nsymm);
+  if (nsymm > 0) {   // every rotation must be a lattice symmetry (an integer reciprocal rotation)
+    const int m1[3] = {1, 1, 1};
+    std::vector<int> K;
+    const char *why = "";
+    if (ephg::mesh_qrotations(h->lattvecs, (int)nsymm, rotations, m1, K, &why)) {
+      h->sym_rot.clear();
+      return fail(EPHG_ERR_ARG, "set_symmetry: %s", why);
+    }
+  }
+  return EPHG_OK;
+}
+
+int ephg_irred_wedge(const double *lattvecs, int64_t nsymm, const int64_t *rotations, const int64_t mesh[3],
+                     int64_t nk, const int64_t *indexlist, int64_t *nirred, int64_t *indexlist_irred, int64_t *nequiv,
+                     int64_t *fbz2ibz) {
+  if (!lattvecs || nsymm < 0 || (nsymm > 0 && !rotations) || !mesh || !nirred || !indexlist_irred)
+    return fail(EPHG_ERR_ARG, "irred_wedge: bad arguments");
+  for (int i = 0; i < 3; ++i)
+    if (mesh[i] <= 0 || mesh[i] > 1024) return fail(EPHG_ERR_ARG, "irred_wedge: bad mesh");
+  const int m[3] = {(int)mesh[0], (int)mesh[1], (int)mesh[2]};
+  const int64_t N = mesh[0] * mesh[1] * mesh[2];
+  const int64_t n = indexlist ? nk : N;
+  std::vector<int> K;
+  const char *why = "";
+  if (nsymm > 0 && ephg::mesh_qrotations(lattvecs, (int)nsymm, rotations, m, K, &why))
+    return fail(EPHG_ERR_ARG, "irred_wedge: %s", why);
+  const int nops = (int)(K.size() / 9);
+  // points of the list by muxed index (0-based); -1 outside it
+  std::vector<int64_t> pos(N, -1);
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p = indexlist ? indexlist[i] - 1 : i;
+    if (p < 0 || p >= N) return fail(EPHG_ERR_ARG, "irred_wedge: index out of range");
+    if (i > 0 && indexlist && indexlist[i] <= indexlist[i - 1])
+      return fail(EPHG_ERR_ARG, "irred_wedge: indexlist must be sorted ascending");
+    pos[p] = i;
+  }
+  // find_irred_wedge (symmetry.f90:303-452): the first point of each orbit, in list order
+  std::vector<int64_t> rep(n);
+  int64_t nir = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p = indexlist ? indexlist[i] - 1 : i;
+    const int v0 = (int)(p % m[0]), v1 = (int)((p / m[0]) % m[1]), v2 = (int)(p / ((int64_t)m[0] * m[1]));
+    int64_t best = p;
+    for (int s = 0; s < nops; ++s) {
+      const int *k = &K[9 * s];
+      const int64_t a = floormod((int64_t)k[0] * v0 + (int64_t)k[3] * v1 + (int64_t)k[6] * v2, m[0]);
+      const int64_t b = floormod((int64_t)k[1] * v0 + (int64_t)k[4] * v1 + (int64_t)k[7] * v2, m[1]);
+      const int64_t c = floormod((int64_t)k[2] * v0 + (int64_t)k[5] * v1 + (int64_t)k[8] * v2, m[2]);
+      const int64_t img = a + m[0] * (b + m[1] * c);
+      if (pos[img] < 0) return fail(EPHG_ERR_ARG, "Severe error: Could not find irreducible wedge.");
+      best = std::min(best, img);
+    }
+    rep[i] = pos[best];
+  }
+  std::vector<int64_t> ibz_of(n, -1);
+  for (int64_t i = 0; i < n; ++i)
+    if (rep[i] == i) {
+      ibz_of[i] = nir;
+      indexlist_irred[nir] = indexlist ? indexlist[i] : i + 1;
+      if (nequiv) nequiv[nir] = 0;
+      ++nir;
+    }
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t r = ibz_of[rep[i]];
+    if (nequiv) nequiv[r]++;
+    if (fbz2ibz) fbz2ibz[i] = r + 1;
+  }
+  *nirred = nir;
+  return EPHG_OK;
+}
+
 // ------------------------------------------------------------- el_wann
 int ephg_el_wann(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
                  double *velocities, double *evecs, const double *scissor) {
@@ -766,6 +862,30 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   launch_zgemm(N, (int)nn, nwsk, P, nwsk, h->Hext, 4 * (int64_t)nn, Hk, nn, st);
   launch_heig(N, nw, Hk, nn, w, V, x.err, st);
   launch_el_post(N, nw, w, V, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, ens, st);
+  // ---- crystal symmetry: every mesh point takes the energies of its orbit's
+  // representative, the irreducible point (electron.f90:363-385, 531-546); the
+  // eigenvectors stay the point's own (:431-437).  The electron side then
+  // starts from the irreducible window points only; the phonon side needs
+  // every window k and keeps them all.
+  const int nsymm = (int)(h->sym_rot.size() / 9);
+  const bool ibz = nsymm > 0 && !ph;
+  int *rep = nullptr;
+  if (nsymm > 0) {
+    std::vector<int> K;
+    const char *why = "";
+    if (ephg::mesh_qrotations(h->lattvecs, nsymm, h->sym_rot.data(), mesh, K, &why))
+      return fail(EPHG_ERR_ARG, "el_rates: %s", why);
+    int *Kd;
+    double *ens_m;
+    if ((rc = wsget((*x.ws), "r_symK", K.size(), &Kd)) || (rc = wsget((*x.ws), "r_rep", (size_t)N, &rep)) ||
+        (rc = wsget((*x.ws), "r_ensm", (size_t)N * nw, &ens_m)))
+      return WSFAILX(rc);
+    CK(cudaMemcpyAsync(Kd, K.data(), K.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_sym_rep(N, mesh, (int)(K.size() / 9), Kd, rep, st);
+    launch_map_ens(N, nw, rep, ens, ens_m, st);
+    ens = ens_m;
+    (*x.launches) += 2;
+  }
   // ---- window (apply_energy_window, electron.f90:597-636) ----
   launch_window_flags(N, nw, ens, req->enref, req->fsthick, flag, st);
   launch_iota(N * nw, iota, st);
@@ -809,22 +929,51 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     launch_glprefac(N, nb, Lq, u, glp, glpf, st);
     (*x.launches) += 1;
   }
-  // ---- initial states (demux_state order, interactions.f90:2169-2191) ----
+  // ---- final states: window bands of the window k' (their ranks, cum) ----
   launch_state_flags(nwv, nw, widx, ens, req->enref, req->fsthick, sflag, nin_k, st);
   CK(cudaMemsetAsync(nin_k + nwv, 0, sizeof(int), st));
   tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
-  cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, sflag, st_code, nst_d, nwv * nw, st);
-  tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
   cub::DeviceScan::ExclusiveSum(cubtmp, tbytes, nin_k, cum, nwv + 1, st);
+  std::vector<int> widx_h(nwv), code_h;
+  CK(cudaMemcpyAsync(widx_h.data(), widx, nwv * sizeof(int), cudaMemcpyDeviceToHost, st));
+  // ---- A-rows: the k of the initial states, the window points or, with
+  // crystal symmetry, the irreducible ones (IBZ blocks, find_irred_wedge with
+  // blocks, electron.f90:553-577), in window order ----
+  int nA = nwv;
+  const int *arow = widx;
+  int *awin = nullptr;
+  std::vector<int> arow_h;
+  if (ibz) {
+    std::vector<int> rep_h(N);
+    CK(cudaMemcpyAsync(rep_h.data(), rep, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<int> awin_h;
+    for (int i = 0; i < nwv; ++i)
+      if (rep_h[widx_h[i]] == widx_h[i]) {
+        awin_h.push_back(i);
+        arow_h.push_back(widx_h[i]);
+      }
+    nA = (int)arow_h.size();
+    int *arow_d, *ninA;
+    if ((rc = wsget((*x.ws), "r_arow", (size_t)nA, &arow_d)) || (rc = wsget((*x.ws), "r_awin", (size_t)nA, &awin)) ||
+        (rc = wsget((*x.ws), "r_ninA", (size_t)nA, &ninA)))
+      return WSFAILX(rc);
+    CK(cudaMemcpyAsync(arow_d, arow_h.data(), (size_t)nA * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(awin, awin_h.data(), (size_t)nA * sizeof(int), cudaMemcpyHostToDevice, st));
+    arow = arow_d;
+    launch_state_flags(nA, nw, arow, ens, req->enref, req->fsthick, sflag, ninA, st);
+  }
+  // ---- initial states (demux_state order, interactions.f90:2169-2191) ----
+  tbytes = std::max(tmp_bytes, std::max(tb2, tb3));
+  cub::DeviceSelect::Flagged(cubtmp, tbytes, iota, sflag, st_code, nst_d, nA * nw, st);
   (*x.launches) += 7;
   CKL();
   int nst = 0, nin = 0;
   CK(cudaMemcpyAsync(&nst, nst_d, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&nin, cum + nwv, sizeof(int), cudaMemcpyDeviceToHost, st));
-  std::vector<int> widx_h(nwv), code_h;
-  CK(cudaMemcpyAsync(widx_h.data(), widx, nwv * sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if ((rc = check_err_view(x))) return rc;
+  if (!ibz) arow_h = widx_h;
   code_h.resize(nst);
   CK(cudaMemcpyAsync(code_h.data(), st_code, nst * sizeof(int), cudaMemcpyDeviceToHost, st));
   // simplices for triangle / tetrahedron deltas
@@ -856,9 +1005,9 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     ed.nvx = nvx;
   }
   CK(cudaStreamSynchronize(st));
-  std::vector<int> first_state(nwv + 1, nst);
+  std::vector<int> first_state(nA + 1, nst);
   for (int j = nst - 1; j >= 0; --j) first_state[code_h[j] / nw] = j;
-  for (int i = nwv - 1; i >= 0; --i)
+  for (int i = nA - 1; i >= 0; --i)
     if (first_state[i] > first_state[i + 1]) first_state[i] = first_state[i + 1];
   CK(cudaEventRecord(ev.e[1], st));
   x.yield();   // serving: hand the GPU to a smaller request before the contractions
@@ -879,6 +1028,8 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   rp.inv_nk = 1.0 / (double)N;
   rp.const_tp = 2.0 * 3.141592653589793 / hbar_eVps;
   ed.widx = widx;
+  ed.sidx = arow;
+  ed.swin = awin;
   ed.st_code = st_code;
   ed.cum = cum;
   ed.ens = ens;
@@ -919,23 +1070,23 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   if ((rc = wsget((*x.ws), "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAILX(rc);
   if (!split) {
     double2 *Pk, *gk, *B, *Pq, *Cb;
-    const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nwv, ((int64_t)1 << 31) / (Nn * 16)));
+    const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nA, ((int64_t)1 << 31) / (Nn * 16)));
     const int64_t sc = std::max<int64_t>(1, std::min<int64_t>({(int64_t)nst, (int64_t)32768,
                                                               ((int64_t)1 << 31) / ((int64_t)nwv * ncol * 16)}));
     if ((rc = wsget((*x.ws), "a_Pk", (size_t)kc * nwsk, &Pk)) || (rc = wsget((*x.ws), "a_gk", (size_t)kc * Nn, &gk)) ||
         (rc = wsget((*x.ws), "a_B", (size_t)nwsq * ldb, &B)) || (rc = wsget((*x.ws), "b_Pq", (size_t)nwv * nwsq, &Pq)) ||
         (rc = wsget((*x.ws), "b_C", (size_t)nwv * ncol * sc, &Cb)))
       return WSFAILX(rc);
-    for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
-      int n = (int)std::min<int64_t>(kc, nwv - i0);
-      launch_phase_mesh(n, widx + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
+    for (int64_t i0 = 0; i0 < nA; i0 += kc) {   // stage A over the A-rows
+      int n = (int)std::min<int64_t>(kc, nA - i0);
+      launch_phase_mesh(n, arow + i0, mesh, L, nwsk, h->Rk, h->degk, 0, roots, Pk, nwsk, st);
       (*x.ta).begin(st);
       launch_zgemm(n, (int)Nn, nwsk, Pk, nwsk, h->G64, Nn, gk, Nn, st);
       (*x.ta).end(st);
       // the rotation writes B columns of states [j0, j1) (grid.y <= 32768 per launch)
       for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
         int je = std::min(j1, j0 + 32768);
-        launch_rotate_states_fp64(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, V, gk, Nn, mesh, L,
+        launch_rotate_states_fp64(j0, je, (int)i0, st_code, nw, nb, nwsq, arow, V, gk, Nn, mesh, L,
                                   roots, h->Rq, h->degq, B + (int64_t)j0 * ncol, ldb, st);
         (*x.launches) += 1;
       }
@@ -955,7 +1106,7 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     }
   } else {
     rc = tc::split_rates_stage(h->split, *x.ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
-                               mesh, L, roots, widx, st_code, first_state, h->Rk, h->degk, h->kposk,
+                               mesh, L, roots, widx, arow, nA, st_code, first_state, h->Rk, h->degk, h->kposk,
                                h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk_max, &nblk,
                                ev.e[2], x.launches, x.ta, x.tb, &h->split_mu, x.chunk_us, x.yield);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
@@ -968,8 +1119,8 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   if (rates) CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (ph) CK(cudaMemcpyAsync(ph->rates_phe, phr, (size_t)N * nb * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (indexlist)
-    for (int i = 0; i < nwv; ++i) indexlist[i] = (int64_t)widx_h[i] + 1;
+  if (indexlist)   // the rows of the rates: the A-rows
+    for (int i = 0; i < nA; ++i) indexlist[i] = (int64_t)arow_h[i] + 1;
   if (lists) {
     if (g2) CK(cudaMemcpyAsync(g2, g2d, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (g2 && xplus) CK(cudaMemcpyAsync(xplus, xpd, vcap * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -984,7 +1135,7 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);
     cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
     cudaEventElapsedTime(&t03, ev.e[0], ev.e[3]);
-    stats->nwv = nwv;
+    stats->nwv = nA;
     stats->nstates_inwindow = nin;
     stats->nstates = nst;
     stats->vertices = vtot;
@@ -994,7 +1145,7 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     stats->ms_stage_a = t12;
     stats->ms_stage_bc = t23;
     stats->ms_total = t03;
-    stats->stage_a_gflop = 8.0 * (double)nwv * nwsk * (double)Nn * 1e-9;
+    stats->stage_a_gflop = 8.0 * (double)nA * nwsk * (double)Nn * 1e-9;
     stats->stage_b_gflop = 8.0 * (double)nwv * nwsq * (double)ncol * nst * 1e-9;
     stats->ms_gemm_a = (*x.ta).total_ms();
     stats->ms_gemm_b = (*x.tb).total_ms();

@@ -44,6 +44,8 @@ struct ephg_handle {
   ephg::PolarDev polar;
   double *polar_G = nullptr, *polar_Gcell = nullptr, *polar_born = nullptr, *polar_tau = nullptr;
   double2 *polar_Da = nullptr;
+  // crystal symmetry (ephg_set_symmetry): real-space rotations (3,3,n), crystal coordinates
+  std::vector<int64_t> sym_rot;
 };
 
 namespace ephg {

@@ -896,7 +896,8 @@ __device__ void pair_epilogue(int ip, int j, GV Gv, const RateParams &rp, const 
   const int nw = rp.nw, nb = rp.nb;
   const int code = d.st_code[j];
   const int i = code / nw, m = code % nw;
-  const int p = d.widx[i], pp = d.widx[ip];
+  const int p = d.sidx[i], pp = d.widx[ip];
+  const int iw = d.swin ? d.swin[i] : i;   // the state's k in the window (simplices)
   const double E = d.ens[(size_t)p * nw + m];
   int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
   int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
@@ -940,7 +941,7 @@ __device__ void pair_epilogue(int ip, int j, GV Gv, const RateParams &rp, const 
         if (ph) {
           // Y: delta(E' - omega) at the initial electron (k, m), interactions.f90:1862
           const double invboseplus1 = 1.0 / (1.0 + bose);
-          const double dy = delta_eval(eps - om, i, m, E, rp, d);
+          const double dy = delta_eval(eps - om, iw, m, E, rp, d);
           y = rp.const_tp * (g2 * (fermi1 * (1.0 - fp) * invboseplus1) * dy);
           if (d.phr && y != 0.0) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * y);
         }

@@ -119,8 +119,10 @@ void launch_rotate_states_fp64(int j0, int j1, int i0, const int *st_code, int n
                                const int *Rq, const double *degq, double2 *B, int64_t ldb,
                                cudaStream_t st);
 struct EpiData {
-  const int *widx;      // window -> mesh index
-  const int *st_code;   // state -> i*nw + m
+  const int *widx;      // window (k' row) -> mesh index
+  const int *st_code;   // state -> i*nw + m, i the state's k row (an A-row)
+  const int *sidx;      // A-row (the k of initial states) -> mesh index
+  const int *swin;      // A-row -> window index (simplices); null: the identity
   const int *cum;       // window k' -> first (k',n) final-state rank
   const double *ens;    // [p][b] eV
   const double2 *U;     // [p][b][c]

@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
   if (ip < nwv) {
     const int code = d.st_code[j];
     const int i = code / nw, m = code % nw;
-    const int p = d.widx[i], pp = d.widx[ip];
+    const int p = d.sidx[i], pp = d.widx[ip];
     const double E = d.ens[(size_t)p * nw + m];
     const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
     const double inv_sig = 1.0 / rp.sigma;
@@ -835,7 +835,7 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
     if (live) {
       const int code = d.st_code[j];
       const int i = code / nw, m = code % nw;
-      const int p = d.widx[i];
+      const int p = d.sidx[i];
       const double E = d.ens[(size_t)p * nw + m];
       const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
       const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
@@ -1782,7 +1782,7 @@ static int epi_tables(Workspace &ws, cudaStream_t st, const double2 *U, const Ra
 // state operand, stage B as chunked GEMMs + a separate epilogue.
 static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk,
                                int nwsq, int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L,
-                               const double2 *roots, const int *widx, const int *st_code,
+                               const double2 *roots, const int *widx, const int *arow, int nA, const int *st_code,
                                const std::vector<int> &first_state, const int *Rk, const double *degk,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
@@ -1808,8 +1808,8 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   }
   }
   const int ncol = nw * nb;
-  // stage A in k chunks of kc rows (multiple of BM)
-  const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nwv, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
+  // stage A over the A-rows in chunks of kc rows (multiple of BM)
+  const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nA, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
   const int64_t Np2 = rup((int64_t)nst * ncol, BN);
   float *PA, *CAr, *CAi, *B2;
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
@@ -1822,22 +1822,22 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
       if (Np2 > used)
         TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
   }
-  // first state of each window k, and the Rp cell at each contraction position
+  // first state of each A-row, and the Rp cell at each contraction position
   int *fs_d, *kinvB;
-  if ((rc = wsget(ws, "tc_fs", (size_t)nwv + 1, &fs_d)) || (rc = wsget(ws, "tc_kinv", (size_t)KpB, &kinvB)))
+  if ((rc = wsget(ws, "tc_fs", (size_t)nA + 1, &fs_d)) || (rc = wsget(ws, "tc_kinv", (size_t)KpB, &kinvB)))
     return tfail(6, ws.msg.c_str());
-  TCK(cudaMemcpyAsync(fs_d, first_state.data(), (size_t)(nwv + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  TCK(cudaMemcpyAsync(fs_d, first_state.data(), (size_t)(nA + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
   TCK(cudaMemsetAsync(kinvB, 0xFF, (size_t)KpB * sizeof(int), st));
   k_kinv<<<(nwsq + 255) / 256, 256, 0, st>>>(nwsq, kposB, kinvB);
   TCK(cudaGetLastError());
   *launches += 1;
-  for (int64_t i0 = 0; i0 < nwv; i0 += kc) {
+  for (int64_t i0 = 0; i0 < nA; i0 += kc) {
     if (i0 > 0) yield();
-    const int n = (int)std::min<int64_t>(kc, nwv - i0);
+    const int n = (int)std::min<int64_t>(kc, nA - i0);
     const int Mp = (int)rup(n, BM);
     TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
     int64_t ne = (int64_t)n * nwsk;
-    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(n, widx + i0, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(n, arow + i0, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
                                                                  degk, kposA, roots, PA, Mp, KpA);
     TCK(cudaGetLastError());
     tA->begin(st);
@@ -1852,7 +1852,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
         std::call_once(attr_once, [] {
           cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         });
-        k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, widx, U, CAr, CAi, NpA, mesh[0], mesh[1],
+        k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, arow, U, CAr, CAi, NpA, mesh[0], mesh[1],
                                       mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
         TCK(cudaGetLastError());
         (*launches)++;
@@ -1860,7 +1860,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
         for (int j0 = first_state[i0], j1 = first_state[i0 + n]; j0 < j1; j0 += 32768) {
           int je = std::min(j1, j0 + 32768);
           dim3 grid(std::max(1, std::min(64, (ncol * nwsq + 255) / 256)), je - j0);
-          k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, widx, U, CAr, CAi, NpA,
+          k_rotate_planes<<<grid, 256, 0, st>>>(j0, je, (int)i0, st_code, nw, nb, nwsq, arow, U, CAr, CAi, NpA,
                                                mesh[0], mesh[1], mesh[2], L, roots, Rq, degq, kposB, B2, Np2, KpB, 0);
           TCK(cudaGetLastError());
           (*launches)++;
@@ -1932,7 +1932,8 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
 // operand) and fused stage B (contraction over Rp + rate epilogue).
 static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk,
                                int nwsq, int64_t Nn, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
-                               const int *widx, const int *st_code, const int *Rk, const double *degk,
+                               const int *widx, const int *arow, int nA, const int *st_code,
+                               const std::vector<int> &first_state, const int *Rk, const double *degk,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
                                cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
@@ -1941,7 +1942,9 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   const int ncol = 48;
   const int KpA = (int)rup(nwsk, 16), KpB = (int)rup(nwsq, 16);
   const int N = rp.N;
-  const int Mp = (int)rup(nwv, 2 * BM);             // window rows (k and k' alike), whole tile pairs
+  const int Mp = (int)rup(nwv, 2 * BM);             // window k' rows, whole tile pairs
+  const bool own_a = arow != widx;                  // A-rows other than the window (irreducible wedge)
+  const int MpA = own_a ? (int)rup(nA, 2 * BM) : Mp;   // stage-A k rows
   const int64_t NA = (int64_t)8 * KpB * ncol;       // stage-A columns (m', kp, n', s')
   // contraction position -> Rp cell
   int *kinvB;
@@ -1984,7 +1987,7 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
     return tfail(6, ws.msg.c_str());
   k_fused_rows<<<(Mp + 127) / 128, 128, 0, st>>>(nwv, Mp, widx, ed_in.ens, et.Uf, ed_in.cum, rp.enref, rp.fsthick,
                                                  mesh[0], mesh[1], trow, tU4, tens);
-  k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, widx, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
+  k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, arow, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
                                                     mesh[1], tst);
   k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, et.cx, et.bs, et.w, et.v, trec);
   TCK(cudaGetLastError());
@@ -1997,10 +2000,30 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
     *launches += 1;
   }
   const FusedTabs tabs{trow, tst, tU4, tens, trec, tglb, Mp, N};
+  // stage A's row tables: the window rows, or the A-rows with their first states
+  FusedTabs tabsA = tabs;
+  if (own_a) {
+    int4 *trowA;
+    float4 *tU4A;
+    double *tensA;
+    int *fsA;
+    if ((rc = wsget(ws, "tc_frowA", (size_t)MpA, &trowA)) || (rc = wsget(ws, "tc_fU4A", (size_t)32 * MpA, &tU4A)) ||
+        (rc = wsget(ws, "tc_fensA", (size_t)8 * MpA, &tensA)) || (rc = wsget(ws, "tc_fsA", (size_t)nA + 1, &fsA)))
+      return tfail(6, ws.msg.c_str());
+    TCK(cudaMemcpyAsync(fsA, first_state.data(), (size_t)(nA + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_fused_rows<<<(MpA + 127) / 128, 128, 0, st>>>(nA, MpA, arow, ed_in.ens, et.Uf, fsA, rp.enref, rp.fsthick,
+                                                    mesh[0], mesh[1], trowA, tU4A, tensA);
+    TCK(cudaGetLastError());
+    *launches += 1;
+    tabsA.row = trowA;
+    tabsA.U4 = tU4A;
+    tabsA.ensw = tensA;
+    tabsA.MpB = MpA;
+  }
   // state operand: whole 8-state groups (8 x 48 = 384 rows), six planes; padding rows zero
   const int64_t Np2 = rup(nst, 8) * ncol;
   float *PA, *PB, *B2;
-  if ((rc = wsget(ws, "tc_PAf", (size_t)4 * Mp * KpA, &PA)) || (rc = wsget(ws, "tc_PB", (size_t)4 * Mp * KpB, &PB)) ||
+  if ((rc = wsget(ws, "tc_PAf", (size_t)4 * MpA * KpA, &PA)) || (rc = wsget(ws, "tc_PB", (size_t)4 * Mp * KpB, &PB)) ||
       (rc = wsget(ws, "tc_B2", (size_t)6 * Np2 * KpB, &B2)))
     return tfail(6, ws.msg.c_str());
   {
@@ -2009,20 +2032,20 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
       if (Np2 > used)
         TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
   }
-  // ---- stage A
-  TCK(cudaMemsetAsync(PA, 0, (size_t)4 * Mp * KpA * sizeof(float), st));
+  // ---- stage A over the A-rows
+  TCK(cudaMemsetAsync(PA, 0, (size_t)4 * MpA * KpA * sizeof(float), st));
   {
-    const int64_t ne = (int64_t)nwv * nwsk;
-    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, widx, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
-                                                                 degk, kposA, roots, PA, Mp, KpA);
+    const int64_t ne = (int64_t)nA * nwsk;
+    k_phase_planes<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nA, arow, mesh[0], mesh[1], mesh[2], L, nwsk, Rk,
+                                                                 degk, kposA, roots, PA, MpA, KpA);
     TCK(cudaGetLastError());
     (*launches)++;
   }
   float2 *phk;
-  if ((rc = wsget(ws, "tc_phk", (size_t)Mp * KpB, &phk))) return tfail(6, ws.msg.c_str());
+  if ((rc = wsget(ws, "tc_phk", (size_t)MpA * KpB, &phk))) return tfail(6, ws.msg.c_str());
   {
-    const int64_t ne = (int64_t)Mp * KpB;
-    k_phase_k_table<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nwv, Mp, KpB, widx, kinvB, mesh[0], mesh[1], mesh[2],
+    const int64_t ne = (int64_t)MpA * KpB;
+    k_phase_k_table<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(nA, MpA, KpB, arow, kinvB, mesh[0], mesh[1], mesh[2],
                                                                   L, Rq, degq, roots, phk);
     TCK(cudaGetLastError());
     (*launches)++;
@@ -2034,7 +2057,7 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   ga.phk = phk;
   ga.err = err;
   tA->begin(st);
-  if ((rc = stageA_fused86(PA, Mp, s.GA6, NA, KpA, tabs, ga, st, chunk_us > 0 ? std::max(1, chunk_us / 25) : 0,
+  if ((rc = stageA_fused86(PA, MpA, s.GA6, NA, KpA, tabsA, ga, st, chunk_us > 0 ? std::max(1, chunk_us / 25) : 0,
                            yield)))
     return rc;
   yield();
@@ -2063,7 +2086,8 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
 
 int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64, int nwsk, int nwsq,
                       int64_t Nn, int nw, int nb, int nwv, int nst, const int mesh[3], int L, const double2 *roots,
-                      const int *widx, const int *st_code, const std::vector<int> &first_state, const int *Rk,
+                      const int *widx, const int *arow, int nA, const int *st_code,
+                      const std::vector<int> &first_state, const int *Rk,
                       const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
                       const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
                       int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
@@ -2081,12 +2105,13 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   if ((rc = wsget(ws, "tc_err", 1, &err))) return tfail(6, ws.msg.c_str());
   TCK(cudaMemsetAsync(err, 0, sizeof(int), st));
   if (fast86) {
-    if ((rc = split_rates_fused86(s, ws, st, G64, nwsk, nwsq, Nn, nwv, nst, mesh, L, roots, widx, st_code, Rk, degk,
-                                  kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err, ev_stage_a, launches, tA,
-                                  tB, build_mu, chunk_us, yield)))
+    if ((rc = split_rates_fused86(s, ws, st, G64, nwsk, nwsq, Nn, nwv, nst, mesh, L, roots, widx, arow, nA, st_code,
+                                  first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err,
+                                  ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield)))
       return rc;
-  } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, st_code,
-                                       first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err,
+  } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, arow,
+                                       nA, st_code, first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in,
+                                       partial, nblk, err,
                                        ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield))) {
     return rc;
   }

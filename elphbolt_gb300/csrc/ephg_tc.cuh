@@ -25,6 +25,10 @@ void free_split(SplitOperands &s);
 const char *last_error();
 
 // Stage A + B + C of the rate pipeline in the split form: fills the rate
+// partials.  widx (nwv) lists the window k' rows of stage B; arow (nA) the
+// k-points of the initial states (the A-rows of stage A: the window points, or
+// their irreducible wedge), st_code the states as A-row * nw + band and
+// first_state (nA + 1) the first state of each A-row.  Fills the rate
 // partials [state][k'-block] like the FP64 path, using up to nblk_max k'
 // blocks (*nblk_used returns the count).  kposA / kposB give the contraction
 // position of each Re / Rp cell (cells ordered far to near).  Records
@@ -37,7 +41,8 @@ const char *last_error();
 int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const double2 *G64,
                       int nwsk, int nwsq, int64_t Nn, int nw, int nb, int nwv, int nst,
                       const int mesh[3], int L, const double2 *roots, const int *widx,
-                      const int *st_code, const std::vector<int> &first_state, const int *Rk,
+                      const int *arow, int nA, const int *st_code, const std::vector<int> &first_state,
+                      const int *Rk,
                       const double *degk, const int *kposA, const int *Rq, const double *degq,
                       const int *kposB, const double2 *U, const RateParams &rp, const EpiData &ed,
                       double *partial, int nblk_max, int *nblk_used, cudaEvent_t ev_stage_a,

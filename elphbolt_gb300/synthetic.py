@@ -335,6 +335,89 @@ def make_wannier(crys: Crystal, nw: int, supercell=(6, 6, 6), seed: int = 202601
     return wd
 
 
+def make_wannier_symmetric(crys: Crystal, n_orb: int = 4, supercell=(4, 4, 4), seed: int = 20260201,
+                           t_ev: float = 2.0, decay_ang: float = 1.2, shells: float = 1.75,
+                           k_nn: float = 10.0, k_2nd: float = 2.0, nvalence: int | None = None) -> WannierData:
+    """Wannier data of a symmetric tight-binding model: the space group of
+    ``crys`` is a symmetry of H(k), D(q) and g(k,q), as for real EPW data.
+
+    n_orb s-like Wannier functions per atom (nw = n_orb * natoms).  Hopping
+    between orbital a of atom i (cell 0) and b of atom j (cell R) is
+    t = c_ab(types) exp(-d/decay) for bond length 0 < d <= ``shells`` times the
+    shortest distance, with c symmetric under (i,a) <-> (j,b); on-site blocks
+    are random symmetric matrices per atom type.  Springs are central, one
+    constant per shell (``k_nn``, ``k_2nd`` eV/A^2).  The e-ph coupling is the
+    bond-stretching derivative of the hopping, g = dt/du = t'(d) e_d for atom j
+    in cell R and -t'(d) e_d for atom i in cell 0 (Ry/bohr).  Every bond lies
+    inside the Wigner-Seitz cell of the supercell (degeneracy 1), so the
+    interpolation reproduces the model exactly.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cells, degs = wigner_seitz(crys.lattvecs, supercell)
+    nat = crys.numatoms
+    nw, nb = n_orb * nat, 3 * nat
+    L = crys.lattvecs * ANG_PER_NM
+    tau = L @ crys.basis
+    _, types = np.unique(np.asarray(crys.masses), return_inverse=True)
+    ntype = int(types.max()) + 1
+    # bond shells
+    dmin = np.inf
+    for i in range(nat):
+        for j in range(nat):
+            for R in cells:
+                v = tau[:, j] + L @ R - tau[:, i]
+                dv = float(np.linalg.norm(v))
+                if dv > 1e-9:
+                    dmin = min(dmin, dv)
+    cut = shells * dmin
+    # hopping prefactors c[ti][tj][a][b] with c[tj][ti] = c[ti][tj]^T; on-site blocks per type
+    c = np.zeros((ntype, ntype, n_orb, n_orb))
+    for ti in range(ntype):
+        for tj in range(ti, ntype):
+            m = rng.uniform(-1.0, 1.0, (n_orb, n_orb)) * t_ev
+            if ti == tj:
+                m = 0.5 * (m + m.T)
+            c[ti, tj], c[tj, ti] = m, m.T
+    eps = []
+    for t in range(ntype):
+        m = rng.normal(0.0, 1.5, (n_orb, n_orb))
+        eps.append(0.5 * (m + m.T))
+    nws = cells.shape[0]
+    H = np.zeros((nws, nw, nw), dtype=np.complex128, order="F")
+    g = np.zeros((nw, nw, nws, nb, nws), dtype=np.complex128, order="F")
+    index = {tuple(int(x) for x in R): r for r, R in enumerate(cells)}
+    r0 = index[(0, 0, 0)]
+    lam = decay_ang / BOHR_ANG            # bohr
+    for r, R in enumerate(cells):
+        for i in range(nat):
+            for j in range(nat):
+                v = tau[:, j] + L @ R - tau[:, i]
+                d = float(np.linalg.norm(v))
+                blk_h = np.zeros((n_orb, n_orb))
+                if d < 1e-9:
+                    blk_h = eps[types[i]]
+                elif d <= cut * (1 + 1e-9):
+                    if degs[r] != 1:
+                        raise ValueError("a bond reaches a Wigner-Seitz boundary cell: enlarge the supercell")
+                    t = c[types[i], types[j]] * math.exp(-d / decay_ang)          # eV
+                    blk_h = t
+                    e = v / d
+                    tp = -t / C.Ryd2eV / lam                                        # Ry/bohr, d t / d d
+                    for x in range(3):
+                        # atom j in cell R moves: d -> d + u.e ; atom i in cell 0 moves: d -> d - u.e
+                        g[n_orb * i:n_orb * (i + 1), n_orb * j:n_orb * (j + 1), r, 3 * j + x, r] += tp * e[x]
+                        g[n_orb * i:n_orb * (i + 1), n_orb * j:n_orb * (j + 1), r, 3 * i + x, r0] -= tp * e[x]
+                H[r, n_orb * i:n_orb * (i + 1), n_orb * j:n_orb * (j + 1)] = blk_h / C.Ryd2eV
+    D = _springs(crys, cells, supercell, rng, k_nn, k_nn, shell2=(shells, k_2nd, k_2nd))
+    wd = WannierData(crystal=crys, numwannbands=nw, numbranches=nb,
+                     coarse_qmesh=np.asarray(supercell, dtype=np.int64),
+                     rcells_k=cells.copy(), rcells_q=cells.copy(), rcells_g=cells.copy(),
+                     elwsdeg=degs.copy(), phwsdeg=degs.copy(), gwsdeg=degs.copy(),
+                     Hwann=np.asfortranarray(H), Dphwann=np.asfortranarray(D), gwann=np.asfortranarray(g))
+    wd.midgap = _midgap(wd, nvalence if nvalence is not None else nw // 2)
+    return wd
+
+
 def _midgap(wd: WannierData, nval: int, mesh=(6, 6, 6)) -> float:
     """(VBM + CBM)/2 of the split after ``nval`` bands on a coarse mesh (eV).
 

@@ -84,6 +84,17 @@ class Wannier:
         if getattr(c, "polar", False):
             self.set_polar(c.epsilon, c.born)
 
+    def set_symmetry(self, rotations):
+        """The crystal's real-space rotations (nops,3,3) (``ephg_set_symmetry``);
+        None or an empty list: the identity only.  Rate requests then start
+        from the irreducible window points (see include/ephg.h)."""
+        from .symmetry import rotations_fortran
+        if rotations is None or len(rotations) == 0:
+            check(self._L.ephg_set_symmetry(self._h, 0, None))
+            return
+        R = rotations_fortran(rotations)
+        check(self._L.ephg_set_symmetry(self._h, R.shape[2], _p(R, c_i64p)))
+
     def set_polar(self, epsilon, born):
         """crys%polar, epsilon (3,3), born (3,3,numatoms) (``ephg_set_polar``);
         epsilon None switches the long-range terms off."""

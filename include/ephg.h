@@ -117,6 +117,42 @@ int ephg_device_count(void);
  * times the electron overlap (:998-1006).  epsilon NULL: non-polar again. */
 int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born);
 
+/* Crystal symmetry (symmetry.f90).
+ *
+ * ephg_crystal_symmetry: the space-group operations of a crystal, what
+ * spg_get_dataset gives calculate_symmetries (symmetry.f90:66-110) with the
+ * tolerance symprec (nm): x' = W x + t in crystal coordinates, rotations
+ * (3,3,nops) column-major integer W, translations (3,nops); lattvecs (3,3)
+ * columns a1 a2 a3 (nm), basis (3,natoms) crystal coordinates, atomtypes
+ * (natoms).  The identity comes first; the other operations in a fixed order
+ * of this library (spglib's order may differ).  maxops: room in the outputs.
+ *
+ * ephg_set_symmetry: the nsymm real-space rotations (3,3,nsymm) of the crystal
+ * (rotations_orig; NULL / 0: the identity only).  Every rate request then
+ * forms, per its mesh, the reciprocal rotations with time reversal, without
+ * those incompatible with the mesh or repeated (symmetry.f90:134-212), and
+ * - gives every mesh point the electron energies of its irreducible point
+ *   (electron.f90:363-385, 531-546; the eigenvectors stay the point's own);
+ * - ephg_el_rates takes initial states on the irreducible window points only
+ *   (IBZ blocks, electron.f90:553-577; interactions.f90:2169-2191): rates and
+ *   indexlist have stats.nwv rows, one per irreducible window point, in
+ *   indexlist_irred order -- rta_rates_eph(nwv_irred, nw);
+ * - ephg_ph_rates keeps every window k (the phonon side sums over them) and
+ *   returns every q of the mesh.
+ *
+ * ephg_irred_wedge: find_irred_wedge (symmetry.f90:303-452) with the nsymm
+ * real-space rotations of a lattice (as for ephg_set_symmetry; no device is
+ * needed) on a mesh, over its nk points of indexlist (1-based muxed, sorted;
+ * NULL: the whole mesh): nirred irreducible points indexlist_irred, their
+ * nequiv images and fbz2ibz (nk, nullable) the 1-based irreducible point of
+ * every input point (create_fbz2ibz_map, :480-503).  Outputs sized nk. */
+int ephg_crystal_symmetry(const double *lattvecs, int64_t natoms, const double *basis, const int64_t *atomtypes,
+                          double symprec, int64_t maxops, int64_t *nops, int64_t *rotations, double *translations);
+int ephg_set_symmetry(ephg_handle *h, int64_t nsymm, const int64_t *rotations);
+int ephg_irred_wedge(const double *lattvecs, int64_t nsymm, const int64_t *rotations, const int64_t mesh[3],
+                     int64_t nk, const int64_t *indexlist, int64_t *nirred, int64_t *indexlist_irred, int64_t *nequiv,
+                     int64_t *fbz2ibz);
+
 /* el_wann (wannier.f90:430-524): kvecs (nk,3) crystal coords -> energies
  * (nk,nw) eV; optional velocities (nk,nw,3) km/s, evecs (nk,nw,nw) with
  * evecs(k,b,:) the eigenvector of band b, scissor (nw) eV.  NULL = absent. */

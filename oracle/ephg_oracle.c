@@ -892,6 +892,151 @@ double or_delta_tetra(double e, int64_t ik, int64_t ib, const int64_t mesh[3], i
   return d / (double)numtetra;
 }
 
+/* ======================= symmetry ======================= */
+
+/* find_star + find_equiv_map: symmetry.f90:215-289.  equiv (nsym, n): the
+ * 1-based muxed image of point i under rotation s, or -1 off the mesh. */
+void or_find_equiv_map(int64_t nsym, const double *qrot, const int64_t mesh[3], int64_t n,
+                       const int64_t *indexlist, int64_t *equiv) {
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t v[3];
+    or_demux_vector(indexlist ? indexlist[i] : i + 1, v, mesh, 0);
+    for (int64_t s = 0; s < nsym; ++s) {
+      const double *q = qrot + 9 * s;
+      double vec[3];
+      int64_t iv[3];
+      double nrm = 0.0;
+      for (int r = 0; r < 3; ++r) {
+        vec[r] = (double)mesh[r] * (q[r] * ((double)v[0] / mesh[0]) + q[r + 3] * ((double)v[1] / mesh[1]) +
+                                    q[r + 6] * ((double)v[2] / mesh[2]));
+        iv[r] = (int64_t)llround(vec[r]);
+        nrm += (vec[r] - iv[r]) * (vec[r] - iv[r]);
+      }
+      if (sqrt(nrm) >= 1e-2) {
+        equiv[s + nsym * i] = -1;
+      } else {
+        for (int r = 0; r < 3; ++r) iv[r] = ((iv[r] % mesh[r]) + mesh[r]) % mesh[r];
+        equiv[s + nsym * i] = or_mux_vector(iv, mesh, 0);
+      }
+    }
+  }
+}
+
+/* calculate_symmetries after spg_get_dataset (symmetry.f90:134-212): the
+ * reciprocal rotations M^-1 R^T M transposed (M = A^T A) of the nsymm
+ * real-space rotations rot (3,3,nsymm, crystal coordinates), time reversal
+ * appended as the negatives, then the rotations that send a mesh point off the
+ * mesh or repeat an earlier valid rotation dropped.  qrot (3,3,2 nsymm)
+ * receives the kept ones; returns their number. */
+int64_t or_symmetry_qrotations(const double lattvecs[9], int64_t nsymm, const int64_t *rot, const int64_t mesh[3],
+                               double *qrot) {
+  const double *A = lattvecs;
+  double M[9], Mi[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M[i + 3 * j] = A[3 * i] * A[3 * j] + A[3 * i + 1] * A[3 * j + 1] + A[3 * i + 2] * A[3 * j + 2];
+  const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
+                     M[6] * (M[1] * M[5] - M[4] * M[2]);
+  Mi[0] = (M[4] * M[8] - M[7] * M[5]) / det;
+  Mi[3] = -(M[3] * M[8] - M[6] * M[5]) / det;
+  Mi[6] = (M[3] * M[7] - M[6] * M[4]) / det;
+  Mi[1] = -(M[1] * M[8] - M[7] * M[2]) / det;
+  Mi[4] = (M[0] * M[8] - M[6] * M[2]) / det;
+  Mi[7] = -(M[0] * M[7] - M[6] * M[1]) / det;
+  Mi[2] = (M[1] * M[5] - M[4] * M[2]) / det;
+  Mi[5] = -(M[0] * M[5] - M[3] * M[2]) / det;
+  Mi[8] = (M[0] * M[4] - M[3] * M[1]) / det;
+  const int64_t n2 = 2 * nsymm;
+  double *q = (double *)calloc(9 * n2 + 1, sizeof(double));
+  int64_t *r = (int64_t *)calloc(9 * n2 + 1, sizeof(int64_t));
+  for (int64_t s = 0; s < nsymm; ++s) {
+    double t2[9], t3[9];   /* t2 = M^-1 R^T, qrot = transpose(t2 M) */
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc += Mi[i + 3 * k] * (double)rot[9 * s + j + 3 * k];
+        t2[i + 3 * j] = acc;
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc += t2[i + 3 * k] * M[k + 3 * j];
+        t3[i + 3 * j] = acc;
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        q[9 * s + i + 3 * j] = t3[j + 3 * i];
+        q[9 * (s + nsymm) + i + 3 * j] = -t3[j + 3 * i];
+      }
+    for (int k = 0; k < 9; ++k) {
+      r[9 * s + k] = rot[9 * s + k];
+      r[9 * (s + nsymm) + k] = -rot[9 * s + k];
+    }
+  }
+  const int64_t N = mesh[0] * mesh[1] * mesh[2];
+  int64_t *eq = (int64_t *)malloc(sizeof(int64_t) * n2 * N);
+  or_find_equiv_map(n2, q, mesh, N, NULL, eq);
+  int *valid = (int *)malloc(sizeof(int) * n2);
+  for (int64_t s = 0; s < n2; ++s) {
+    valid[s] = 1;
+    for (int64_t i = 0; i < N && valid[s]; ++i)
+      if (eq[s + n2 * i] == -1) valid[s] = 0;
+  }
+  for (int64_t ii = 1; ii < n2; ++ii)
+    for (int64_t i = 0; i < ii; ++i) {
+      if (!valid[i]) continue;
+      int same = 1;
+      for (int k = 0; k < 9; ++k) same &= r[9 * ii + k] == r[9 * i + k];
+      if (same) { valid[ii] = 0; break; }
+    }
+  int64_t kk = 0;
+  for (int64_t s = 0; s < n2; ++s)
+    if (valid[s]) {
+      for (int k = 0; k < 9; ++k) qrot[9 * kk + k] = q[9 * s + k];
+      kk++;
+    }
+  free(q); free(r); free(eq); free(valid);
+  return kk;
+}
+
+/* find_irred_wedge: symmetry.f90:303-452 (serial form of its running list).
+ * Over the mesh (indexlist NULL) or the n sorted points of indexlist (blocks):
+ * indexlist_irred (nirr), nequiv (nirr), ibz2fbz (nsym, n, 2) nullable.
+ * Returns 0, or 1 ("Could not find irreducible wedge.", :417). */
+int or_find_irred_wedge(const int64_t mesh[3], int64_t nsym, const double *qrot, int64_t n, const int64_t *indexlist,
+                        int64_t *nirr, int64_t *indexlist_irred, int64_t *nequiv, int64_t *ibz2fbz) {
+  const int64_t N = mesh[0] * mesh[1] * mesh[2];
+  int64_t *eq = (int64_t *)malloc(sizeof(int64_t) * (nsym * n > 0 ? nsym * n : 1));
+  or_find_equiv_map(nsym, qrot, mesh, n, indexlist, eq);
+  char *running = (char *)calloc(N + 1, 1);   /* membership of the running list, by muxed index */
+  int64_t *imagelist = (int64_t *)malloc(sizeof(int64_t) * (nsym > 0 ? nsym : 1));
+  int64_t nir = 0, counter = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t imux = indexlist ? indexlist[i] : i + 1;
+    if (running[imux]) continue;
+    const int64_t ir = nir++;
+    indexlist_irred[ir] = imux;
+    int64_t ne = 0;
+    for (int64_t s = 0; s < nsym; ++s) {
+      const int64_t image = eq[s + nsym * i];
+      int seen = 0;
+      for (int64_t l = 0; l < ne; ++l) seen |= imagelist[l] == image;
+      if (seen) continue;
+      imagelist[ne] = image;
+      if (image >= 1 && image <= N) running[image] = 1;
+      if (ibz2fbz) {
+        ibz2fbz[ne + nsym * (ir + n * 0)] = s + 1;
+        ibz2fbz[ne + nsym * (ir + n * 1)] = image;
+      }
+      ne++;
+    }
+    nequiv[ir] = ne;
+    counter += ne;
+  }
+  *nirr = nir;
+  free(eq); free(running); free(imagelist);
+  return counter == n ? 0 : 1;
+}
+
 /* ======================= driver ======================= */
 
 typedef struct {
@@ -928,11 +1073,24 @@ struct or_rates_ctx {
   int64_t *simplex, *scount, *smap;
   double *se;
   delta_ctx dc;
+  int64_t nirr;       /* with symmetry: irreducible window points (IBZ blocks) */
+  int64_t *irr_pos;   /* (nwv) their row in the IBZ list, -1 for the others; NULL without symmetry */
 };
 
 /* Set-up of the ibzk driver: FBZ energies, window, window eigenvectors,
  * phonons on the q mesh, simplices (electron.f90:321-595, phonon.f90:159-230). */
 or_rates_ctx *or_rates_setup(const or_wannier *w, const or_request *req, int nthreads) {
+  return or_rates_setup_sym(w, req, 0, NULL, nthreads);
+}
+
+/* With nsym > 0 reciprocal rotations qrot (or_symmetry_qrotations): the
+ * electron set-up of calculate_electrons (electron.f90:346-577) -- FBZ energies
+ * from the IBZ of the full mesh mapped onto its images, the window on them,
+ * FBZ blocks eigenvectors computed directly, the IBZ of the window blocks and
+ * its energies mapped again -- so that or_rates_run takes initial states on
+ * the irreducible window points only. */
+or_rates_ctx *or_rates_setup_sym(const or_wannier *w, const or_request *req, int64_t nsym, const double *qrot,
+                                 int nthreads) {
   const int64_t nw = w->nw, nb = w->nb;
   const int64_t *mesh = req->mesh;
   const int64_t N = mesh[0] * mesh[1] * mesh[2];
@@ -952,6 +1110,21 @@ or_rates_ctx *or_rates_setup(const or_wannier *w, const or_request *req, int nth
   }
   double *ens_full = (double *)malloc(sizeof(double) * N * nw);
   or_el_wann(w, N, kfull, ens_full, NULL, NULL, NULL);
+  if (nsym > 0) {   /* IBZ of the full mesh, its energies mapped onto the FBZ (:351-385) */
+    int64_t nir = 0, *irr = (int64_t *)malloc(sizeof(int64_t) * N), *neq = (int64_t *)malloc(sizeof(int64_t) * N);
+    int64_t *map = (int64_t *)malloc(sizeof(int64_t) * nsym * N * 2);
+    if (or_find_irred_wedge(mesh, nsym, qrot, N, NULL, &nir, irr, neq, map)) cx->status = 3;
+    double *kir = (double *)malloc(sizeof(double) * nir * 3), *eir = (double *)malloc(sizeof(double) * nir * nw);
+    for (int64_t i = 0; i < nir; ++i)
+      for (int d = 0; d < 3; ++d) kir[i + nir * d] = kfull[(irr[i] - 1) + N * d];
+    or_el_wann(w, nir, kir, eir, NULL, NULL, NULL);
+    for (int64_t i = 0; i < nir; ++i)
+      for (int64_t l = 0; l < neq[i]; ++l) {
+        const int64_t il = map[l + nsym * (i + N * 1)];
+        for (int64_t b = 0; b < nw; ++b) ens_full[(il - 1) + N * b] = eir[i + nir * b];
+      }
+    free(irr); free(neq); free(map); free(kir); free(eir);
+  }
   /* 2. window: apply_energy_window (electron.f90:597-636), sorted index list */
   int64_t nwv = 0;
   for (int64_t ik = 0; ik < N; ++ik) {
@@ -970,6 +1143,33 @@ or_rates_ctx *or_rates_setup(const or_wannier *w, const or_request *req, int nth
   double *ens = (double *)malloc(sizeof(double) * nwv * nw);
   double *evecs = (double *)malloc(sizeof(double) * 2 * nwv * nw * nw);
   or_el_wann(w, nwv, kw, ens, evecs, NULL, NULL);
+  if (nsym > 0) {
+    /* FBZ blocks energies: the mapped ones (fbz_blocks_quantities, :424); then the
+     * IBZ of the blocks (:450-454), its energies computed and mapped onto the
+     * blocks (:513-529) */
+    for (int64_t i = 0; i < nwv; ++i)
+      for (int64_t b = 0; b < nw; ++b) ens[i + nwv * b] = ens_full[(indexlist[i] - 1) + N * b];
+    int64_t nir = 0, *irr = (int64_t *)malloc(sizeof(int64_t) * nwv), *neq = (int64_t *)malloc(sizeof(int64_t) * nwv);
+    int64_t *map = (int64_t *)malloc(sizeof(int64_t) * nsym * nwv * 2);
+    if (or_find_irred_wedge(mesh, nsym, qrot, nwv, indexlist, &nir, irr, neq, map)) cx->status = 3;
+    double *kir = (double *)malloc(sizeof(double) * (nir > 0 ? nir : 1) * 3);
+    double *eir = (double *)malloc(sizeof(double) * (nir > 0 ? nir : 1) * nw);
+    for (int64_t i = 0; i < nir; ++i)
+      for (int d = 0; d < 3; ++d) kir[i + nir * d] = kfull[(irr[i] - 1) + N * d];
+    or_el_wann(w, nir, kir, eir, NULL, NULL, NULL);
+    for (int64_t i = 0; i < nir; ++i)
+      for (int64_t l = 0; l < neq[i]; ++l) {
+        const int64_t il = map[l + nsym * (i + nwv * 1)];
+        const int64_t aux = or_binsearch(indexlist, nwv, il);
+        if (aux > 0)
+          for (int64_t b = 0; b < nw; ++b) ens[(aux - 1) + nwv * b] = eir[i + nir * b];
+      }
+    cx->nirr = nir;
+    cx->irr_pos = (int64_t *)malloc(sizeof(int64_t) * nwv);
+    for (int64_t i = 0; i < nwv; ++i) cx->irr_pos[i] = -1;
+    for (int64_t i = 0; i < nir; ++i) cx->irr_pos[or_binsearch(indexlist, nwv, irr[i]) - 1] = i;
+    free(irr); free(neq); free(map); free(kir); free(eir);
+  }
   int64_t nin = 0;
   for (int64_t i = 0; i < nwv; ++i)
     for (int64_t b = 0; b < nw; ++b) if (fabs(ens[i + nwv * b] - req->enref) <= req->fsthick) nin++;
@@ -1042,7 +1242,7 @@ void or_rates_free(or_rates_ctx *cx) {
   if (!cx) return;
   free(cx->indexlist); free(cx->kfull); free(cx->ens_full); free(cx->kw); free(cx->ens);
   free(cx->evecs); free(cx->phe); free(cx->phv); free(cx->simplex); free(cx->scount);
-  free(cx->smap); free(cx->se);
+  free(cx->smap); free(cx->se); free(cx->irr_pos);
   free(cx);
 }
 
@@ -1062,13 +1262,17 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
   const double *kw = cx->kw, *ens = cx->ens, *evecs = cx->evecs, *phe = cx->phe, *phv = cx->phv;
   const delta_ctx dc = cx->dc;
   for (int i = 0; i < 8; ++i) info[i] = 0;
-  info[0] = nwv;
+  info[0] = cx->irr_pos ? cx->nirr : nwv;   /* rows of the rates: the IBZ blocks with symmetry */
   info[1] = nin;
   info[5] = cx->status;
   info[6] = cx->us_setup;
-  for (int64_t i = 0; i < nwv; ++i) indexlist[i] = cx->indexlist[i];
+  for (int64_t i = 0; i < nwv; ++i) {
+    if (!cx->irr_pos) indexlist[i] = cx->indexlist[i];
+    else if (cx->irr_pos[i] >= 0) indexlist[cx->irr_pos[i]] = cx->indexlist[i];
+  }
   if (cx->status == 2) return 2;
-  /* 6. in-window initial states in istate order, optionally truncated */
+  /* 6. in-window initial states in istate order, optionally truncated; with
+   *    symmetry those of the irreducible window points (interactions.f90:2169) */
   int64_t nst_all = nwv * nw;
   int64_t *rank = (int64_t *)malloc(sizeof(int64_t) * nst_all);
   int64_t nsel = 0;
@@ -1076,6 +1280,7 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
     int64_t m, ik;
     or_demux_state(istate, nw, &m, &ik);
     rank[istate - 1] = -1;
+    if (cx->irr_pos && cx->irr_pos[ik - 1] < 0) continue;
     if (fabs(ens[(ik - 1) + nwv * (m - 1)] - req->enref) > req->fsthick) continue;
     int64_t k = nsel++;
     if (k < state_begin || (nstates >= 0 && k >= state_begin + nstates)) continue;
@@ -1144,7 +1349,7 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
           int64_t qi[3], qmux;
           double qf[3], qc[3];
           double prim[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-          or_vector_addsub(indexlist[ikp - 1], indexlist[ik - 1], -1, mesh, prim, qi, &qmux, qf, qc);
+          or_vector_addsub(cx->indexlist[ikp - 1], cx->indexlist[ik - 1], -1, mesh, prim, qi, &qmux, qf, qc);
           int64_t iq = qmux;   /* change_grid to the same mesh keeps the index */
           double qv[3] = {qf[0], qf[1], qf[2]};
           if (!literal) {
@@ -1221,7 +1426,7 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
       double acc = 0.0;
       for (int64_t i = 0; i < per_state; ++i) acc += xp[i];
       for (int64_t i = 0; i < per_state; ++i) acc += xm[i];
-      rates[(ik - 1) + N * (m - 1)] = acc;
+      rates[(cx->irr_pos ? cx->irr_pos[ik - 1] : ik - 1) + N * (m - 1)] = acc;
       int64_t off = r * per_state;
       for (int64_t i = 0; i < per_state; ++i)
         if (off + i < cap) {

@@ -18,6 +18,7 @@
  *   ibzq 'g' + 'Y'        src/interactions.f90:1673-1930, 1932-2093
  *   ph-e RTA rates        src/interactions.f90:2723-2828
  *   triangles / tetra     src/delta.f90:61-225,494-646,648-881
+ *   symmetry / IBZ        src/symmetry.f90:134-289,303-452, src/electron.f90:346-577
  *   index helpers         src/misc.f90:588-610,738-763,906-1019, src/vector.f90:38-120
  *   window                src/electron.f90:597-636
  * plus a Gaussian delta of fixed width with the reference's Gaussian
@@ -156,6 +157,21 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
                  int literal, double *rates, int64_t *indexlist, int64_t *info,
                  double *g2, double *xp, double *xm, int64_t cap);
 void or_rates_free(or_rates_ctx *cx);
+
+/* ---- symmetry (symmetry.f90) ----
+ * qrot / rotations: (3,3,n) column-major; indices 1-based muxed. */
+void or_find_equiv_map(int64_t nsym, const double *qrot, const int64_t mesh[3], int64_t n,
+                       const int64_t *indexlist, int64_t *equiv);
+int64_t or_symmetry_qrotations(const double lattvecs[9], int64_t nsymm, const int64_t *rot, const int64_t mesh[3],
+                               double *qrot);
+int or_find_irred_wedge(const int64_t mesh[3], int64_t nsym, const double *qrot, int64_t n, const int64_t *indexlist,
+                        int64_t *nirr, int64_t *indexlist_irred, int64_t *nequiv, int64_t *ibz2fbz);
+/* The rate driver's set-up with nsym > 0 reciprocal rotations (from
+ * or_symmetry_qrotations): or_rates_run then takes the initial states on the
+ * irreducible window points only, and info[0] / indexlist / the rate rows are
+ * those points (IBZ blocks, electron.f90:346-577).  status 3: no wedge. */
+or_rates_ctx *or_rates_setup_sym(const or_wannier *w, const or_request *req, int64_t nsym, const double *qrot,
+                                 int nthreads);
 
 /* ---- phonon side: ibzq 'g' + 'Y' + the ph-e RTA rates ----
  * calculate_eph_interaction_ibzq (interactions.f90:1673-1930), calculate_Y_OTF

@@ -38,9 +38,39 @@ class OrRequest(ct.Structure):
                 ("sigma", ct.c_double)]
 
 
+_REF_ROOT = "/root/reference"
+_SPGLIB = os.path.join(_HERE, "_ref", "libspglib_ref.so")
+
+
 def build():
-    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    """Compile the oracle with its Makefile (gcc, OpenMP), and the reference's
+    own spglib into oracle/_ref/ where the reference tree is present."""
     subprocess.check_call(["make", "-s", "-C", _HERE])
+    if os.path.isdir(os.path.join(_REF_ROOT, "thirdparty", "spglib", "src")) and not os.path.exists(_SPGLIB):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "ref", "REFROOT=" + _REF_ROOT])
+
+
+def spglib_symmetry(lattvecs, basis, types, symprec=1e-5):
+    """The reference's spglib (oracle/_ref, compiled from its vendored sources):
+    spg_get_symmetry on the crystal, (rotations (n,3,3), translations (n,3)) with
+    x' = W x + t; None where the reference tree was not there to compile it."""
+    if not os.path.exists(_SPGLIB):
+        return None
+    # lazy binding: the magnetic-space-group functions of spglib.c refer to a
+    # database file the vendored copy does not carry; they are never called
+    L = ct.CDLL(_SPGLIB, mode=os.RTLD_LAZY)
+    L.spg_get_symmetry.restype = ct.c_int
+    nat = np.asarray(basis).shape[1]
+    maxn = 192
+    rot = np.zeros((maxn, 3, 3), dtype=np.intc)
+    tr = np.zeros((maxn, 3))
+    lat = np.ascontiguousarray(lattvecs, dtype=np.float64)        # lattice[i][j]: row i = i-th component
+    pos = np.ascontiguousarray(np.asarray(basis, dtype=np.float64).T)
+    typ = np.ascontiguousarray(types, dtype=np.intc)
+    n = L.spg_get_symmetry(rot.ctypes.data_as(ct.c_void_p), tr.ctypes.data_as(ct.c_void_p), maxn,
+                           lat.ctypes.data_as(ct.c_void_p), pos.ctypes.data_as(ct.c_void_p),
+                           typ.ctypes.data_as(ct.c_void_p), nat, ct.c_double(symprec))
+    return rot[:n].astype(np.int64), tr[:n].copy()
 
 
 def lib():
@@ -222,6 +252,42 @@ class Wannier:
         return out
 
 
+    def el_rates_sym(self, req, rotations, nthreads=1, literal=False, vertices=False, cap=None):
+        """The rate driver with crystal symmetry (or_rates_setup_sym): rows are
+        the irreducible window points (IBZ blocks)."""
+        L = lib()
+        L.or_rates_setup_sym.restype = ct.c_void_p
+        L.or_rates_setup_sym.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, c_dp, ct.c_int]
+        L.or_rates_run.argtypes = [ct.c_void_p, ct.c_int64, ct.c_int64, ct.c_int, ct.c_int, c_dp, c_i64p,
+                                   c_i64p, c_dp, c_dp, c_dp, ct.c_int64]
+        L.or_rates_free.argtypes = [ct.c_void_p]
+        q = symmetry_qrotations(self.lattvecs, rotations, req.mesh)
+        r = _request(req)
+        N = int(np.prod(req.mesh))
+        rates = np.zeros((N, self.nw), order="F")
+        idx = np.zeros(N, dtype=np.int64)
+        info = np.zeros(8, dtype=np.int64)
+        c = 0
+        g2 = xp = xm = None
+        if vertices:
+            c = int(cap) if cap is not None else N * self.nw * N * self.nw * self.nb
+            g2, xp, xm = (np.zeros(c) for _ in range(3))
+        ctx = L.or_rates_setup_sym(ct.byref(self.s), ct.byref(r), q.shape[2], _p(q), int(nthreads))
+        try:
+            st = L.or_rates_run(ctx, 0, -1, int(nthreads), 1 if literal else 0, _p(rates), _p(idx, c_i64p),
+                                _p(info, c_i64p), _p(g2) if g2 is not None else None,
+                                _p(xp) if xp is not None else None, _p(xm) if xm is not None else None, c)
+        finally:
+            L.or_rates_free(ctx)
+        n = int(info[0])
+        out = dict(status=int(st), nwv=n, nstates_inwindow=int(info[1]), nstates=int(info[2]),
+                   vertices=int(info[3]), pairs=int(info[4]), indexlist=idx[:n].copy(),
+                   rates=np.asfortranarray(rates[:n]), nsym=q.shape[2])
+        if vertices:
+            nv = min(int(info[3]), c)
+            out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
+        return out
+
     def ph_rates(self, req, spindeg=2, nthreads=1, vertices=False, cap=None):
         """ibzq 'g' + 'Y' and the ph-e RTA rates (or_ph_rates); rates_phe (N, nb)."""
         L = lib()
@@ -246,6 +312,36 @@ class Wannier:
             nv = min(int(info[3]), c)
             out.update(g2=g2[:nv], y=y[:nv])
         return out
+
+
+def symmetry_qrotations(lattvecs, rotations, mesh):
+    """or_symmetry_qrotations: the reciprocal rotations (3,3,n) kept for the mesh."""
+    L = lib()
+    L.or_symmetry_qrotations.restype = ct.c_int64
+    L.or_symmetry_qrotations.argtypes = [c_dp, ct.c_int64, c_i64p, c_i64p, c_dp]
+    A = _f64(lattvecs)
+    R = np.asfortranarray(np.transpose(np.asarray(rotations, dtype=np.int64), (1, 2, 0)))
+    m = np.ascontiguousarray(mesh, dtype=np.int64)
+    q = np.zeros((3, 3, 2 * R.shape[2] + 1), order="F")
+    n = L.or_symmetry_qrotations(_p(A), R.shape[2], _p(R, c_i64p), _p(m, c_i64p), _p(q))
+    return np.asfortranarray(q[:, :, :n])
+
+
+def irred_wedge(lattvecs, rotations, mesh, indexlist=None):
+    """or_find_irred_wedge with the rotations kept for the mesh:
+    (status, indexlist_irred, nequiv)."""
+    L = lib()
+    L.or_find_irred_wedge.argtypes = [c_i64p, ct.c_int64, c_dp, ct.c_int64, c_i64p, c_i64p, c_i64p, c_i64p, c_i64p]
+    q = symmetry_qrotations(lattvecs, rotations, mesh)
+    m = np.ascontiguousarray(mesh, dtype=np.int64)
+    n = int(np.prod(m)) if indexlist is None else len(indexlist)
+    idx = None if indexlist is None else np.ascontiguousarray(indexlist, dtype=np.int64)
+    irr = np.zeros(n, dtype=np.int64)
+    neq = np.zeros(n, dtype=np.int64)
+    nir = ct.c_int64()
+    st = L.or_find_irred_wedge(_p(m, c_i64p), q.shape[2], _p(q), n, _p(idx, c_i64p) if idx is not None else None,
+                               ct.byref(nir), _p(irr, c_i64p), _p(neq, c_i64p), None)
+    return st, irr[:nir.value].copy(), neq[:nir.value].copy()
 
 
 def _request(req):
