@@ -1,11 +1,15 @@
 """Run synthetic RTA-rate requests and print their statistics as JSON lines.
 
     python -m elphbolt_gb300.run_rates --mesh 12 --precision split --repeat 2
+    python -m elphbolt_gb300.run_rates --mesh 12 --side ph --crystal sic
 
 The crystal is the Si-like synthetic one (fcc, 2 atoms, nw = 8, 6^3 WS
-supercell); the window is +-0.5 eV about mid-gap + 0.6 eV, Gaussian delta
-10 meV, 300 K.  Useful for quick checks and for profiling a smaller case of
-the same kernels as the benchmark.
+supercell), or with --crystal sic the polar zincblende SiC-like one (same
+sizes, Born charges and dielectric tensor on); the window is +-0.5 eV about
+mid-gap + 0.6 eV, Gaussian delta 10 meV, 300 K.  --side el runs
+ephg_el_rates (electron RTA rates), --side ph runs ephg_ph_rates with the
+electron rates (both sides in one sweep).  Useful for quick checks and for
+profiling a smaller case of the same kernels as the benchmark.
 """
 from __future__ import annotations
 
@@ -21,16 +25,24 @@ def main(argv=None):
     ap.add_argument("--delta", choices=["gaussian", "triangle", "tetra"], default="gaussian")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--nw", type=int, default=8)
+    ap.add_argument("--side", choices=["el", "ph"], default="el")
+    ap.add_argument("--crystal", choices=["si", "sic"], default="si")
     a = ap.parse_args(argv)
     from . import _lib, build, synthetic as S
     from .wannier import Wannier
     build.build()
-    wd = S.si_like(nw=a.nw)
+    if a.crystal == "sic":
+        wd = S.make_wannier(S.make_crystal_sic_like(), a.nw, supercell=(6, 6, 6), seed=20260105)
+    else:
+        wd = S.si_like(nw=a.nw)
     req = S.si_like_request(wd, (a.mesh,) * 3, delta_kind={"gaussian": 0, "triangle": 1, "tetra": 2}[a.delta])
     W = Wannier(wd)
     prec = _lib.PREC_SPLIT_TF32 if a.precision == "split" else _lib.PREC_FP64
     for i in range(a.repeat):
-        out = W.el_rates(req, precision=prec)
+        if a.side == "ph":
+            out = W.ph_rates(req, precision=prec, electrons=True)
+        else:
+            out = W.el_rates(req, precision=prec)
         st = out["stats"]
         st["vertices_per_s"] = st["vertices"] / (st["ms_total"] * 1e-3)
         st["repeat"] = i
