@@ -284,6 +284,65 @@ def symmetry_side(steps):
             "what": "ephg_set_symmetry + ephg_el_rates: initial states on the irreducible window points"}
 
 
+def batched_side(steps):
+    """The batched form (ephg_el_rates_batch): 64 requests on 8 random crystals
+    (nw 8-24, nb 6-18, WS sets of 93-279 vectors; meshes 8^3-16^3, windows
+    0.2-1.0 eV), split form, 8 requests at a time with grouped GEMM launches.
+    Against: the same 64 requests one at a time (split), the same batch without
+    grouping, and the FP64 drop-in one at a time on one request per crystal
+    (the one of median vertex count), which also gives the split form's error."""
+    import numpy as np
+    from elphbolt_gb300 import _lib, synthetic as S
+    from elphbolt_gb300.wannier import Wannier, el_rates_batch
+    t0 = time.time()
+    wds, reqs = S.batch_workload()
+    t_gen = time.time() - t0
+    Ws = [Wannier(wd) for wd in wds]
+    crys, rq = [Ws[c] for c, _ in reqs], [r for _, r in reqs]
+    try:
+        el_rates_batch(crys, rq, nslots=8)   # warm-up: operand planes, workspaces
+        runs = [el_rates_batch(crys, rq, nslots=8) for _ in range(max(3, min(steps, 5)))]
+        ungrouped = [el_rates_batch(crys, rq, nslots=8, grouped=False) for _ in range(2)]
+        t1 = time.time()
+        alone = [W.el_rates(r, precision=_lib.PREC_SPLIT_TF32) for W, r in zip(crys, rq)]
+        t_alone = time.time() - t1
+        outs = runs[-1][0]
+        pick = []
+        for c in range(len(wds)):
+            mine = sorted((o["vertices"], i) for i, (cc, _) in enumerate(reqs) if cc == c for o in [outs[i]])
+            pick.append(mine[len(mine) // 2][1])
+        fp64_s, fp64_v, errs = 0.0, 0, []
+        for i in pick:
+            t2 = time.time()
+            f = crys[i].el_rates(rq[i], precision=_lib.PREC_FP64)
+            fp64_s += time.time() - t2
+            fp64_v += f["vertices"]
+            m = f["rates"] > 0
+            errs.append(float(np.max(np.abs(outs[i]["rates"][m] - f["rates"][m]) / f["rates"][m])))
+    finally:
+        for W in Ws:
+            W.deallocate_wannier()
+    bs = [r[1] for r in runs]
+    wall = float(np.median([b["wall_ms"] for b in bs]))
+    verts = bs[-1]["vertices"]
+    same = all(np.array_equal(a["rates"], o["rates"]) for a, o in zip(alone, outs))
+    gv = verts / (wall * 1e-3)
+    return {"workload": "64 requests on 8 random crystals (nw 8/16/24, nb 6/12/18, WS 93-279), meshes 8^3-16^3, "
+                        "windows 0.2-1.0 eV, Gaussian 10 meV, 300 K",
+            "crystals": [[wd.numwannbands, wd.numbranches, int(wd.rcells_k.shape[0])] for wd in wds],
+            "vertices_per_batch": verts, "ms_per_batch": wall, "value": gv, "unit": UNIT,
+            "group": {k: bs[-1][k] for k in ("group_launches", "group_problems", "group_tiles", "max_group")},
+            "ungrouped_ms_per_batch": float(np.median([b[1]["wall_ms"] for b in ungrouped])),
+            "one_at_a_time_split_ms": t_alone * 1e3,
+            "one_at_a_time_split_value": verts / t_alone,
+            "fp64_dropin_one_at_a_time": {"value": fp64_v / fp64_s, "unit": UNIT, "requests": len(pick),
+                                          "vertices": fp64_v, "seconds": fp64_s},
+            "speedup_vs_fp64_dropin": gv / (fp64_v / fp64_s),
+            "rates_max_rel_vs_fp64": max(errs), "results_equal_alone": same,
+            "peak_workspace_bytes": bs[-1]["peak_workspace_bytes"], "generation_s": t_gen,
+            "what": "ephg_el_rates_batch, 8 slots, grouped tcgen05 GEMM launches; host wall time per batch"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -433,6 +492,11 @@ def run_ours(args, ws, rank, local):
             line["symmetry"] = symmetry_side(args.steps)
         except Exception as e:   # the main line is still printed
             line["symmetry"] = {"error": repr(e)}
+    if not args.no_batched:
+        try:
+            line["batched"] = batched_side(args.steps)
+        except Exception as e:   # the main line is still printed
+            line["batched"] = {"error": repr(e)}
     if serving is not None:
         line["serving"] = serving
     print(json.dumps(line), flush=True)
@@ -505,6 +569,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop (p50 / p99 latency) measurement")
     ap.add_argument("--no-polar", action="store_true", help="skip the polar-crystal measurement")
     ap.add_argument("--no-symmetry", action="store_true", help="skip the crystal-symmetry measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1 and args.impl == "ours":

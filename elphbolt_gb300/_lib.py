@@ -34,7 +34,7 @@ EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count"
            "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates",
            "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
            "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates", "ephg_set_polar",
-           "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge"]
+           "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge", "ephg_el_rates_batch"]
 
 TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
 
@@ -84,6 +84,20 @@ class ServerStats(ct.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BatchOpts(ct.Structure):
+    _fields_ = [("nslots", ct.c_int64), ("hbm_budget_bytes", ct.c_int64), ("grouped", ct.c_int64)]
+
+
+class BatchStats(ct.Structure):
+    _fields_ = [("requests", ct.c_int64), ("failed", ct.c_int64), ("vertices", ct.c_int64),
+                ("wall_ms", ct.c_double), ("vertices_per_s", ct.c_double), ("group_launches", ct.c_int64),
+                ("group_problems", ct.c_int64), ("group_tiles", ct.c_int64), ("max_group", ct.c_int64),
+                ("retried_alone", ct.c_int64), ("peak_workspace_bytes", ct.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -119,6 +133,9 @@ def load(path: str = LIB_PATH):
     L.ephg_irred_wedge.argtypes = [c_dp, ct.c_int64, c_i64p, c_i64p, ct.c_int64, c_i64p, c_i64p, c_i64p, c_i64p,
                                    c_i64p]
     L.ephg_el_wann_noalloc.argtypes = [vp, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    L.ephg_el_rates_batch.argtypes = [ct.c_int64, ct.POINTER(vp), ct.POINTER(RateRequest), ct.POINTER(c_dp),
+                                      ct.POINTER(c_i64p), ct.POINTER(RateStats), ct.POINTER(ct.c_int),
+                                      ct.POINTER(BatchOpts), ct.POINTER(BatchStats)]
     L.ephg_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_int64, ct.c_int, ct.POINTER(vp)]
     L.ephg_server_destroy.argtypes = [vp]
     L.ephg_submit.argtypes = [vp, ct.c_int, ct.POINTER(RateRequest), c_i64p]

@@ -19,7 +19,8 @@ LIB = os.path.join(HERE, "libephg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["ephg_api.cu", "ephg_kernels.cu", "ephg_tc.cu", "ephg_noalloc.cu", "ephg_serve.cu", "ephg_polar.cu", "ephg_sym.cu"]
+SOURCES = ["ephg_api.cu", "ephg_kernels.cu", "ephg_tc.cu", "ephg_noalloc.cu", "ephg_serve.cu", "ephg_polar.cu", "ephg_sym.cu",
+           "ephg_batch.cu"]
 
 
 def nvcc() -> str:

@@ -1108,7 +1108,8 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
     rc = tc::split_rates_stage(h->split, *x.ws, st, h->G64, h->nwsk, nwsq, Nn, nw, nb, nwv, nst,
                                mesh, L, roots, widx, arow, nA, st_code, first_state, h->Rk, h->degk, h->kposk,
                                h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk_max, &nblk,
-                               ev.e[2], x.launches, x.ta, x.tb, &h->split_mu, x.chunk_us, x.yield);
+                               ev.e[2], x.launches, x.ta, x.tb, &h->split_mu, x.chunk_us, x.yield, &x.bm,
+                               x.chunk_bytes);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
   }
   CKL();

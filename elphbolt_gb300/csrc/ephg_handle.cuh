@@ -62,6 +62,8 @@ struct ExecView {
   int64_t *launches;
   int chunk_us = 0;   // > 0: persistent kernels run as launches of about this length (serving)
   Yield yield;        // called between chunks and stages (serving); no-op by default
+  tc::BatchMember bm;                        // batched form: the member of a grouped-launch batcher
+  int64_t chunk_bytes = (int64_t)1 << 31;    // per-chunk GEMM output bound of the generic split path
 };
 // The phonon side of a rate request (ephg_ph_rates): the ph-e rates (N, nb) and
 // the optional per-vertex Y list, formed in the same sweep as the electron side.

@@ -29,6 +29,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <mutex>
 #include <cmath>
 #include <cstdint>
@@ -222,8 +223,70 @@ struct GemmArgs {
   int *err;
 };
 
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
-    k_cgemm_3xtf32(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, GemmArgs g) {
+// One output tile as the three roles see it: operand maps, first A / B row of
+// plane 0, K blocks, and the tile's first output element.
+struct TileJob {
+  const CUtensorMap *tA, *tB;
+  int arow, brow, nkb;
+  int Astride, Bstride;
+  float *Cr, *Ci;
+  int64_t ldc;
+};
+
+__device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, const CUtensorMap *tB, const GemmArgs &g, int t) {
+  const int mt = t % g.mtiles, nt = t / g.mtiles;
+  TileJob j;
+  j.tA = tA;
+  j.tB = tB;
+  j.arow = (int)(g.Aoff + (int64_t)mt * BM);
+  j.brow = (int)(g.Boff + (int64_t)nt * BN);
+  j.nkb = g.nkb;
+  j.Astride = (int)g.Astride;
+  j.Bstride = (int)g.Bstride;
+  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * BN;
+  j.Cr = g.Cr + off;
+  j.Ci = g.Ci + off;
+  j.ldc = g.ldc;
+  return j;
+}
+
+// A single GEMM: its maps are kernel parameters.
+struct OneGemm {
+  const CUtensorMap *tA, *tB;
+  const GemmArgs *g;
+  static constexpr bool kGlobalMaps = false;
+  __device__ __forceinline__ TileJob operator()(int t) const { return tile_job(tA, tB, *g, t); }
+};
+
+// A group of GEMMs of different requests, shapes and operands in one launch:
+// problem p owns tiles [tile0, tile0 + mtiles * ntiles) of the launch's tile
+// space; its maps sit in global memory beside its shape.
+struct GroupProblem {   // 64-byte aligned: CUtensorMap is
+  CUtensorMap tA, tB;
+  GemmArgs g;
+  int tile0;
+};
+
+struct GroupGemm {
+  const GroupProblem *tab;
+  int np;
+  static constexpr bool kGlobalMaps = true;
+  __device__ __forceinline__ TileJob operator()(int t) const {
+    int lo = 0, hi = np - 1;   // last problem with tile0 <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&tab[mid].tile0) <= t) lo = mid; else hi = mid - 1;
+    }
+    const GroupProblem *q = tab + lo;
+    return tile_job(&q->tA, &q->tB, q->g, t - q->tile0);
+  }
+};
+
+// Warp-specialised 3xTF32 complex GEMM over the tiles [t0, t1) of a tile
+// space, strided by the grid: warp 0 lane 0 issues TMA loads, warp 1 lane 0
+// the MMAs, warps 2..5 drain TMEM.  Every wait is bounded (err).
+template <class Jobs>
+__device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -262,24 +325,31 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int t = g.t0 + blockIdx.x; t < g.t1 && ok; t += gridDim.x) {
-        const int mt = t % g.mtiles, nt = t / g.mtiles;
-        for (int kb = 0; kb < g.nkb; ++kb) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
+      const CUtensorMap *seen = nullptr;
+      for (int t = t0 + blockIdx.x; t < t1 && ok; t += gridDim.x) {
+        const TileJob j = jobs(t);
+        if (Jobs::kGlobalMaps && j.tA != seen) {
+          // maps in global memory, written before the launch: order the tensor-map
+          // proxy's reads of them after those writes
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(j.tA) : "memory");
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(j.tB) : "memory");
+          seen = j.tA;
+        }
+        for (int kb = 0; kb < j.nkb; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, err)) { ok = false; break; }
           uint8_t *sb = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], STAGE_BYTES);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
-            tma_load_2d_hint(sb + p * PLANE_BYTES, &tA, &full[stage], kb * BK, (int)(p * g.Astride + g.Aoff + mt * BM),
-                             keep);
+            tma_load_2d_hint(sb + p * PLANE_BYTES, j.tA, &full[stage], kb * BK, p * j.Astride + j.arow, keep);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
-            tma_load_2d(sb + (4 + p) * PLANE_BYTES, &tB, &full[stage], kb * BK, (int)(p * g.Bstride + g.Boff + nt * BN));
+            tma_load_2d(sb + (4 + p) * PLANE_BYTES, j.tB, &full[stage], kb * BK, p * j.Bstride + j.brow);
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       }
       // drain: wait until every issued stage has landed before the CTA can exit
-      for (int s = 0; s < STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, g.err), stage = (stage + 1) % STAGES,
+      for (int s = 0; s < STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, err), stage = (stage + 1) % STAGES,
                                          phase ^= (stage == 0);
     }
   } else if (warp == 1) {
@@ -290,11 +360,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int it = 0;
       bool ok = true;
       const uint32_t mr = tmem, mi = tmem + BN, cr = tmem + 2 * BN, ci = tmem + 3 * BN;
-      for (int t = g.t0 + blockIdx.x; t < g.t1 && ok; t += gridDim.x, ++it) {
-        if (!mbar_wait(&tempty[0], (it & 1) ^ 1, g.err)) { ok = false; break; }
+      for (int t = t0 + blockIdx.x; t < t1 && ok; t += gridDim.x, ++it) {
+        const int nkb = jobs(t).nkb;
+        if (!mbar_wait(&tempty[0], (it & 1) ^ 1, err)) { ok = false; break; }
         tc_fence_after();
-        for (int kb = 0; kb < g.nkb; ++kb) {
-          if (!mbar_wait(&full[stage], phase, g.err)) { ok = false; break; }
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&full[stage], phase, err)) { ok = false; break; }
           tc_fence_after();
           uint8_t *sb = smem + stage * STAGE_BYTES;
 #pragma unroll
@@ -317,7 +388,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             // main: Re = Ar Br - Ai Bi, Im = Ar Bi + Ai Br (hi parts).  The last K
             // block holds the nearest cells, the largest terms: they go to the
             // short correction chain instead of the long main chain.
-            const bool nearblk = (kb == g.nkb - 1) && g.nkb > 1;
+            const bool nearblk = (kb == nkb - 1) && nkb > 1;
             const uint32_t dr = nearblk ? cr : mr, di = nearblk ? ci : mi;
             const uint32_t am = nearblk ? 1u : acc;
             umma(dr, Ahr, Bhr, IDP, am);
@@ -335,13 +406,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     int it = 0;
-    for (int t = g.t0 + blockIdx.x; t < g.t1; t += gridDim.x, ++it) {
-      const int mt = t % g.mtiles, nt = t / g.mtiles;
-      if (!mbar_wait(&tfull[0], it & 1, g.err)) break;
+    for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x, ++it) {
+      const TileJob j = jobs(t);
+      if (!mbar_wait(&tfull[0], it & 1, err)) break;
       tc_fence_after();
       const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
-      float *cr = g.Cr + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
-      float *ci = g.Ci + (int64_t)(mt * BM + row) * g.ldc + (int64_t)nt * BN;
+      float *cr = j.Cr + (int64_t)row * j.ldc;
+      float *ci = j.Ci + (int64_t)row * j.ldc;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 16) {
         float vr[16], vi[16], wr[16], wi[16];
@@ -370,6 +441,17 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+}
+
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    k_cgemm_3xtf32(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, GemmArgs g) {
+  cgemm_body(OneGemm{&tA, &tB, &g}, g.t0, g.t1, g.err);
+}
+
+// The grouped form: the GEMMs of many rate requests in one persistent launch.
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    k_cgemm_group(const GroupProblem *tab, int np, int t0, int t1, int *err) {
+  cgemm_body(GroupGemm{tab, np}, t0, t1, err);
 }
 
 // -------------------------------------------------------- tensor maps
@@ -411,13 +493,183 @@ static int num_sms() {
   return n > 0 ? n : 1;
 }
 
+// ------------------------------------------------------ grouped launches
+// The GEMMs of rate requests running concurrently (one host thread and stream
+// each) are gathered into rounds: a member that reaches a GEMM submits it and
+// blocks; when every active member has submitted, the last one launches the
+// round's problems as one k_cgemm_group launch on the batcher's stream (after
+// each member's stream reached its submit), and each member's stream waits for
+// that launch before its next kernel.  Members are active only inside the
+// split form's generic contraction stages; anywhere else they do not hold a
+// round back.
+class GemmBatcher {
+ public:
+  explicit GemmBatcher(int n) : act_(n, 0), rc_(n, 0), ready_(n, nullptr) {
+    cudaStreamCreateWithFlags(&gst_, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&done_, cudaEventDisableTiming);
+    for (auto &e : ready_) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    for (int r = 0; r < kRing; ++r) cudaEventCreateWithFlags(&slot_ev_[r], cudaEventDisableTiming);
+    cudaMallocHost((void **)&htab_, sizeof(GroupProblem) * (size_t)kRing * n);
+    cudaMalloc((void **)&dtab_, sizeof(GroupProblem) * (size_t)kRing * n);
+    cudaMalloc((void **)&derr_, sizeof(int));
+    cudaMemset(derr_, 0, sizeof(int));
+    cap_ = n;
+    ok_ = htab_ && dtab_ && derr_ && gst_;
+  }
+  ~GemmBatcher() {
+    if (gst_) cudaStreamSynchronize(gst_);
+    if (htab_) cudaFreeHost(htab_);
+    if (dtab_) cudaFree(dtab_);
+    if (derr_) cudaFree(derr_);
+    for (auto &e : ready_) cudaEventDestroy(e);
+    for (int r = 0; r < kRing; ++r) cudaEventDestroy(slot_ev_[r]);
+    cudaEventDestroy(done_);
+    if (gst_) cudaStreamDestroy(gst_);
+  }
+  bool ok() const { return ok_; }
+  void activate(int id) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (!act_[id]) { act_[id] = 1; ++active_; }
+  }
+  void deactivate(int id) {
+    std::unique_lock<std::mutex> lk(mu_);
+    if (!act_[id]) return;
+    act_[id] = 0;
+    --active_;
+    if (!pend_.empty() && (int)pend_.size() == active_) launch_locked();
+  }
+  int submit(int id, const GroupProblem &p, cudaStream_t st) {
+    if (cudaEventRecord(ready_[id], st) != cudaSuccess) return tfail(2, "batch: event record failed");
+    std::unique_lock<std::mutex> lk(mu_);
+    if (!act_[id]) { act_[id] = 1; ++active_; }
+    pend_.push_back({id, st, p});
+    const uint64_t my = round_;
+    if ((int)pend_.size() == active_) launch_locked();
+    else cv_.wait(lk, [&] { return round_ != my; });
+    return rc_[id];
+  }
+  // device word of the grouped launches' bounded waits (read after the members finished)
+  int device_error() {
+    int w = 0;
+    cudaStreamSynchronize(gst_);
+    cudaMemcpy(&w, derr_, sizeof(int), cudaMemcpyDeviceToHost);
+    return w;
+  }
+  void stats(int64_t *launches, int64_t *problems, int64_t *tiles, int64_t *max_group) const {
+    *launches = launches_;
+    *problems = problems_;
+    *tiles = tiles_;
+    *max_group = max_group_;
+  }
+
+ private:
+  static constexpr int kRing = 8;
+  struct Pend {
+    int id;
+    cudaStream_t st;
+    GroupProblem p;
+  };
+  void launch_locked() {
+    // heaviest tiles (most K blocks) first: the strided tile order then ends on light tiles
+    std::stable_sort(pend_.begin(), pend_.end(), [](const Pend &a, const Pend &b) { return a.p.g.nkb > b.p.g.nkb; });
+    const int np = (int)pend_.size();
+    const int slot = (int)(round_ % kRing);
+    GroupProblem *h = htab_ + (size_t)slot * cap_, *d = dtab_ + (size_t)slot * cap_;
+    cudaEventSynchronize(slot_ev_[slot]);   // the copy that last read this staging slot has run
+    int64_t T = 0;
+    for (int i = 0; i < np; ++i) {
+      h[i] = pend_[i].p;
+      h[i].tile0 = (int)T;
+      T += (int64_t)h[i].g.mtiles * h[i].g.ntiles;
+    }
+    int rc = 0;
+    if (T > INT32_MAX) rc = tfail(1, "batch: too many tiles in one round");
+    for (int i = 0; i < np && !rc; ++i)
+      if (cudaStreamWaitEvent(gst_, ready_[pend_[i].id], 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
+    if (!rc && cudaMemcpyAsync(d, h, sizeof(GroupProblem) * np, cudaMemcpyHostToDevice, gst_) != cudaSuccess)
+      rc = tfail(2, "batch: problem table upload failed");
+    if (!rc) {
+      cudaEventRecord(slot_ev_[slot], gst_);
+      const int grid = (int)std::min<int64_t>(T, num_sms());
+      k_cgemm_group<<<grid, GEMM_THREADS, SMEM_BYTES, gst_>>>(d, np, 0, (int)T, derr_);
+      if (cudaGetLastError() != cudaSuccess) rc = tfail(2, "batch: grouped GEMM launch failed");
+    }
+    if (!rc && cudaEventRecord(done_, gst_) != cudaSuccess) rc = tfail(2, "batch: event record failed");
+    for (auto &q : pend_) {
+      if (!rc && cudaStreamWaitEvent(q.st, done_, 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
+      rc_[q.id] = rc;
+    }
+    ++launches_;
+    problems_ += np;
+    tiles_ += T;
+    max_group_ = std::max<int64_t>(max_group_, np);
+    pend_.clear();
+    ++round_;
+    cv_.notify_all();
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::vector<char> act_;
+  std::vector<int> rc_;
+  std::vector<cudaEvent_t> ready_;
+  std::vector<Pend> pend_;
+  int active_ = 0, cap_ = 0;
+  uint64_t round_ = 0;
+  cudaStream_t gst_ = nullptr;
+  cudaEvent_t done_ = nullptr, slot_ev_[kRing] = {};
+  GroupProblem *htab_ = nullptr, *dtab_ = nullptr;
+  int *derr_ = nullptr;
+  bool ok_ = false;
+  int64_t launches_ = 0, problems_ = 0, tiles_ = 0, max_group_ = 0;
+};
+
+GemmBatcher *batcher_create(int nmembers) {
+  if (nmembers <= 0) return nullptr;
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(k_cgemm_group, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
+  GemmBatcher *b = new GemmBatcher(nmembers);
+  if (!b->ok()) {
+    delete b;
+    return nullptr;
+  }
+  return b;
+}
+void batcher_destroy(GemmBatcher *b) { delete b; }
+void batcher_activate(const BatchMember &m) { if (m.gb) m.gb->activate(m.id); }
+void batcher_deactivate(const BatchMember &m) { if (m.gb) m.gb->deactivate(m.id); }
+int batcher_device_error(GemmBatcher *b) { return b ? b->device_error() : 0; }
+void batcher_stats(const GemmBatcher *b, int64_t *launches, int64_t *problems, int64_t *tiles, int64_t *max_group) {
+  b->stats(launches, problems, tiles, max_group);
+}
+
 // C[Mp][ldc] (re, im planes) = A x B^T.  A: planes of Astride rows, rows
 // [Aoff, Aoff + Mp) of each; B: planes of Bstride rows, rows [Boff, Boff + Np).
+// With a batch member the GEMM joins its batcher's next grouped launch.
 static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const float *Bp, int64_t Bstride,
                  int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st,
-                 int chunk_us = 0, const Yield &yield = Yield()) {
+                 int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr) {
   if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
   if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
+  if (bm && bm->gb) {
+    GroupProblem p;
+    memset(&p, 0, sizeof p);
+    int rc;
+    if ((rc = make_map(&p.tA, Ap, Kp, 4 * Astride)) || (rc = make_map(&p.tB, Bp, Kp, 4 * Bstride))) return rc;
+    p.g.mtiles = Mp / BM;
+    p.g.ntiles = Np / BN;
+    p.g.nkb = Kp / BK;
+    p.g.Astride = Astride;
+    p.g.Bstride = Bstride;
+    p.g.Aoff = Aoff;
+    p.g.Boff = Boff;
+    p.g.Cr = Cr;
+    p.g.Ci = Ci;
+    p.g.ldc = ldc;
+    p.g.err = err;
+    return bm->gb->submit(bm->id, p, st);
+  }
   CUtensorMap ta, tb;
   int rc;
   if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 4 * Bstride))) return rc;
@@ -578,30 +830,45 @@ __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int 
     const int64_t col = (int64_t)(j - jbase) * ncol + c;
     put4(Bp, Np2 * Kp2, col * Kp2 + kpos[rp], cmul(ph, acc));
   }
+  // the K padding [nws, Kp2) of the state's rows: zero (the workspace holds
+  // whatever an earlier request left there, and 0 x NaN is NaN)
+  const int npad = Kp2 - nws;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ncol * npad; e += gridDim.x * blockDim.x) {
+    const int64_t col = (int64_t)(j - jbase) * ncol + e / npad;
+    put4(Bp, Np2 * Kp2, col * Kp2 + nws + e % npad, make_double2(0.0, 0.0));
+  }
 }
 
 // Stage-A rotation, one block per window k: the block loads g(k,Rp) for KT
-// contraction positions at a time (coalesced rows of nw*nw*nb values), rotates
-// over the initial band for every in-window state of k, applies the k-half of
-// the Rp phase and writes KT consecutive K positions of each operand row, so
-// that both the reads and the split-plane writes are whole sectors.
-// kinv[kp] = Rp cell at contraction position kp (-1 for padding).
+// contraction positions at a time (coalesced rows of nw*nw values per mode),
+// rotates over the initial band for every in-window state of k, applies the
+// k-half of the Rp phase and writes KT consecutive K positions of each operand
+// row, so that both the reads and the split-plane writes are whole sectors.
+// Modes are taken sch at a time so that the staged g fits shared memory for
+// any nb.  kinv[kp] = Rp cell at contraction position kp (-1 for padding).
 constexpr int ROT_KT = 8;
+constexpr int ROT_SMEM = 160 * 1024;
 
-__global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state, int nw, int nb, const int *st_code,
-                                                  const int *widx, const double2 *U, const float *gr, const float *gi,
-                                                  int64_t ldg, int m1, int m2, int m3, int L, const double2 *roots,
-                                                  const int *Rq, const double *degq, const int *kinv, int Kp2,
-                                                  float *Bp, int64_t Np2) {
+// shared memory of k_rotate_k for sch modes per pass and nsk <= nw states per row
+static size_t rotate_k_smem(int nw, int sch) {
+  return ((sizeof(float2) * ROT_KT * nw * nw * sch + 15) & ~(size_t)15) + sizeof(float2) * (nw * nw + ROT_KT);
+}
+
+__global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state, int nw, int nb, int sch,
+                                                  const int *st_code, const int *widx, const double2 *U,
+                                                  const float *gr, const float *gi, int64_t ldg, int m1, int m2,
+                                                  int m3, int L, const double2 *roots, const int *Rq,
+                                                  const double *degq, const int *kinv, int Kp2, float *Bp,
+                                                  int64_t Np2) {
   extern __shared__ unsigned char rsm[];
   const int i = i0 + blockIdx.x;
   const int j0 = first_state[i], j1 = first_state[i + 1];
   const int nsk = j1 - j0;
   if (nsk <= 0) return;
   const int p = widx[i];
-  const int per = nw * nw * nb, ncol = nw * nb;
-  float2 *sg = (float2 *)rsm;                                   // [ROT_KT][per]
-  float2 *sU = (float2 *)(rsm + ((sizeof(float2) * ROT_KT * per + 15) & ~(size_t)15));  // [nsk][nw]
+  const int per = nw * nw * nb, ncol = nw * nb, nn = nw * nw;
+  float2 *sg = (float2 *)rsm;                                   // [ROT_KT][nw * nw * sch]
+  float2 *sU = (float2 *)(rsm + ((sizeof(float2) * ROT_KT * nn * sch + 15) & ~(size_t)15));  // [nsk][nw]
   float2 *sph = sU + nsk * nw;                                  // [ROT_KT]
   for (int t = threadIdx.x; t < nsk * nw; t += blockDim.x) {
     int js = t / nw, mp = t % nw;
@@ -611,35 +878,38 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
   }
   const int64_t grow = (int64_t)(i - i0) * ldg;
   const int64_t plane = Np2 * Kp2;
-  for (int kp0 = 0; kp0 < Kp2; kp0 += ROT_KT) {
-    __syncthreads();
-    for (int t = threadIdx.x; t < ROT_KT * per; t += blockDim.x) {
-      int kk = t / per, e = t % per;
-      int rp = kinv[kp0 + kk];
-      sg[t] = rp >= 0 ? make_float2(gr[grow + (int64_t)rp * per + e], gi[grow + (int64_t)rp * per + e])
-                      : make_float2(0.f, 0.f);
-    }
-    if (threadIdx.x < ROT_KT) {
-      int rp = kinv[kp0 + threadIdx.x];
-      float2 ph = make_float2(0.f, 0.f);
-      if (rp >= 0) {
-        double2 r = roots[phase_idx(p, m1, m2, m3, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
-        ph = make_float2((float)(r.x / degq[rp]), (float)(-r.y / degq[rp]));
+  for (int s0 = 0; s0 < nb; s0 += sch) {
+    const int ns = min(sch, nb - s0), pc = nn * ns, nc = nw * ns;
+    for (int kp0 = 0; kp0 < Kp2; kp0 += ROT_KT) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < ROT_KT * pc; t += blockDim.x) {
+        int kk = t / pc, e = t % pc;
+        int rp = kinv[kp0 + kk];
+        const int64_t off = grow + (int64_t)rp * per + nn * s0 + e;
+        sg[t] = rp >= 0 ? make_float2(gr[off], gi[off]) : make_float2(0.f, 0.f);
       }
-      sph[threadIdx.x] = ph;
-    }
-    __syncthreads();
-    for (int o = threadIdx.x; o < nsk * ncol * ROT_KT; o += blockDim.x) {
-      const int kk = o % ROT_KT, c = (o / ROT_KT) % ncol, js = o / (ROT_KT * ncol);
-      const int np = c % nw, s = c / nw;
-      float2 acc = make_float2(0.f, 0.f);
-      const float2 *g = sg + kk * per + np + nw * nw * s;
-      const float2 *u = sU + js * nw;
-      for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
-      const float2 ph = sph[kk];
-      const int64_t col = (int64_t)(j0 + js) * ncol + c;
-      put4(Bp, plane, col * Kp2 + kp0 + kk,
-           make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
+      if (threadIdx.x < ROT_KT) {
+        int rp = kinv[kp0 + threadIdx.x];
+        float2 ph = make_float2(0.f, 0.f);
+        if (rp >= 0) {
+          double2 r = roots[phase_idx(p, m1, m2, m3, L, Rq[3 * rp], Rq[3 * rp + 1], Rq[3 * rp + 2])];
+          ph = make_float2((float)(r.x / degq[rp]), (float)(-r.y / degq[rp]));
+        }
+        sph[threadIdx.x] = ph;
+      }
+      __syncthreads();
+      for (int o = threadIdx.x; o < nsk * nc * ROT_KT; o += blockDim.x) {
+        const int kk = o % ROT_KT, c = (o / ROT_KT) % nc, js = o / (ROT_KT * nc);
+        const int np = c % nw, s = c / nw;
+        float2 acc = make_float2(0.f, 0.f);
+        const float2 *g = sg + kk * pc + np + nn * s;
+        const float2 *u = sU + js * nw;
+        for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
+        const float2 ph = sph[kk];
+        const int64_t col = (int64_t)(j0 + js) * ncol + np + nw * (s0 + s);
+        put4(Bp, plane, col * Kp2 + kp0 + kk,
+             make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
+      }
     }
   }
 }
@@ -1787,7 +2057,8 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
                                cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
-                               std::mutex *build_mu, int chunk_us, const Yield &yield) {
+                               std::mutex *build_mu, int chunk_us, const Yield &yield, const BatchMember *bm,
+                               int64_t chunk_bytes) {
   int rc;
   const int KpA = (int)rup(nwsk, BK), KpB = (int)rup(nwsq, BK);
   const int64_t NpA = rup(Nn, BN);
@@ -1808,8 +2079,14 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   }
   }
   const int ncol = nw * nb;
+  // batched: this request takes part in the grouped launches from here to the end of stage B
+  struct ActiveScope {
+    const BatchMember *m;
+    explicit ActiveScope(const BatchMember *m_) : m(m_) { if (m) batcher_activate(*m); }
+    ~ActiveScope() { if (m) batcher_deactivate(*m); }
+  } active_scope(bm && bm->gb ? bm : nullptr);
   // stage A over the A-rows in chunks of kc rows (multiple of BM)
-  const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nA, BM), ((int64_t)1 << 31) / (NpA * 8) / BM * BM));
+  const int64_t kc = std::max<int64_t>(BM, std::min<int64_t>(rup(nA, BM), chunk_bytes / (NpA * 8) / BM * BM));
   const int64_t Np2 = rup((int64_t)nst * ncol, BN);
   float *PA, *CAr, *CAi, *B2;
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
@@ -1841,19 +2118,22 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                                                  degk, kposA, roots, PA, Mp, KpA);
     TCK(cudaGetLastError());
     tA->begin(st);
-    if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st, chunk_us, yield))) return rc;
+    if ((rc = cgemm(PA, Mp, 0, Mp, s.G, NpA, 0, (int)NpA, KpA, CAr, CAi, NpA, err, st, chunk_us, yield, bm)))
+      return rc;
     tA->end(st);
     {
-      const int per = nw * nw * nb;
-      const size_t sm = ((sizeof(float2) * ROT_KT * per + 15) & ~(size_t)15) + sizeof(float2) * (nw * nw + ROT_KT);
-      if (sm <= 160 * 1024) {
+      // modes per pass: all of them when the staged g fits, else as many as fit
+      int sch = nb;
+      while (sch > 1 && rotate_k_smem(nw, sch) > (size_t)ROT_SMEM) --sch;
+      const size_t sm = rotate_k_smem(nw, sch);
+      if (sm <= (size_t)ROT_SMEM) {
         // once per process: changing a kernel attribute can wait for the device's queued work
         static std::once_flag attr_once;
         std::call_once(attr_once, [] {
-          cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+          cudaFuncSetAttribute(k_rotate_k, cudaFuncAttributeMaxDynamicSharedMemorySize, ROT_SMEM);
         });
-        k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, st_code, arow, U, CAr, CAi, NpA, mesh[0], mesh[1],
-                                      mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
+        k_rotate_k<<<n, 256, sm, st>>>((int)i0, fs_d, nw, nb, sch, st_code, arow, U, CAr, CAi, NpA, mesh[0],
+                                      mesh[1], mesh[2], L, roots, Rq, degq, kinvB, KpB, B2, Np2);
         TCK(cudaGetLastError());
         (*launches)++;
       } else {   // large nw*nw*nb: one thread per output element
@@ -1873,8 +2153,8 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   // stage B: A planes = e^{2 pi i k'.Rp} for the window k'
   const int MpB = (int)rup(nwv, BM);
   float *PB, *CBr, *CBi;
-  // states per chunk: a multiple of 8 (8 * 48 = 3 * 128 columns) bounded by ~2 GB of output
-  int64_t sc = ((int64_t)1 << 31) / ((int64_t)MpB * ncol * 8);
+  // states per chunk: a multiple of 8 (8 * 48 = 3 * 128 columns) bounded by chunk_bytes of output
+  int64_t sc = chunk_bytes / ((int64_t)MpB * ncol * 8);
   sc = std::max<int64_t>(8, sc / 8 * 8);
   sc = std::min<int64_t>(sc, rup(nst, 8));
   sc = std::min<int64_t>(sc, 32768);
@@ -1899,7 +2179,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
     if (j0 > 0) yield();
-    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st, chunk_us, yield)))
+    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st, chunk_us, yield, bm)))
       return rc;
     tB->end(st);
     const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
@@ -2091,7 +2371,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const double *degk, const int *kposA, const int *Rq, const double *degq, const int *kposB,
                       const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
                       int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
-                      std::mutex *build_mu, int chunk_us, const Yield &yield) {
+                      std::mutex *build_mu, int chunk_us, const Yield &yield, const BatchMember *bm,
+                      int64_t chunk_bytes) {
   // The fused path packs mesh coordinates in 10 bits each.
   const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
                        mesh[2] <= 1024);
@@ -2112,7 +2393,8 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, arow,
                                        nA, st_code, first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in,
                                        partial, nblk, err,
-                                       ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield))) {
+                                       ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield, bm,
+                                       std::max<int64_t>(chunk_bytes, (int64_t)1 << 24)))) {
     return rc;
   }
   int herr = 0;

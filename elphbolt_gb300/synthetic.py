@@ -139,6 +139,10 @@ def wigner_seitz(lattvecs: np.ndarray, supercell, tol: float = 1e-8):
     return cells, degs
 
 
+_WRAP_SHIFTS = np.array([(i, j, k) for k in range(-3, 4) for j in range(-3, 4) for i in range(-3, 4)],
+                        dtype=np.int64)
+
+
 def ws_wrapping_vectors(lvec: np.ndarray, vl: np.ndarray, eps: float = 1e-6):
     """Shortest lattice wraps of a vector given in lattice coordinates.
 
@@ -148,23 +152,18 @@ def ws_wrapping_vectors(lvec: np.ndarray, vl: np.ndarray, eps: float = 1e-6):
     """
     iv0 = np.trunc(vl).astype(np.int64)
     wl = vl - iv0
-    n = 0
+    # all 343 shifts at once (i fastest, then j, then k), then the reference's
+    # running minimum over them in the same order
+    wc = lvec @ (wl[:, None] + _WRAP_SHIFTS.T)
+    norms = np.sqrt(np.einsum("ij,ij->j", wc, wc)).tolist()
     d = np.finfo(np.float64).max
-    shifts = []
-    for k in range(-3, 4):
-        for j in range(-3, 4):
-            for i in range(-3, 4):
-                wc = lvec @ (wl + np.array([i, j, k]))
-                nrm = math.sqrt(float(wc @ wc))
-                shifts.append((i, j, k, nrm))
-                if abs(nrm - d) < eps:
-                    n += 1
-                elif nrm < d:
-                    n = 1
-                    d = nrm
-    out = [np.array([i, j, k], dtype=np.int64) - iv0
-           for (i, j, k, nrm) in shifts if abs(nrm - d) < eps]
-    return np.array(out, dtype=np.int64)
+    for nrm in norms:
+        if abs(nrm - d) < eps:
+            continue
+        if nrm < d:
+            d = nrm
+    keep = np.abs(np.asarray(norms) - d) < eps
+    return (_WRAP_SHIFTS[keep] - iv0).astype(np.int64)
 
 
 def _springs(crys: Crystal, rcells_q: np.ndarray, coarse_qmesh, rng,
@@ -468,3 +467,32 @@ def si_like_request(wd: WannierData, mesh=(12, 12, 12), T: float = 300.0,
     mu = wd.midgap + shift
     return RateRequest(mesh=tuple(int(x) for x in mesh), enref=mu, fsthick=window,
                        chempot=mu, T=T, delta_kind=delta_kind, sigma=sigma)
+
+
+# The batched workload: many requests of uneven size on random crystals.
+# (nw, natoms, WS supercell) of each crystal; nb = 3 natoms.
+BATCH_CRYSTALS = [(8, 2, (6, 6, 6)), (8, 4, (5, 5, 5)), (16, 2, (5, 5, 5)), (16, 4, (5, 5, 5)),
+                  (8, 6, (5, 5, 5)), (24, 2, (5, 5, 5)), (16, 6, (4, 4, 4)), (24, 4, (4, 4, 4))]
+
+
+def batch_workload(n_requests: int = 64, mesh_range=(8, 16), window_range=(0.2, 1.0), seed: int = 20260102,
+                   crystals=None):
+    """Random crystals (``make_crystal_multi``: fcc cell, masses U[12, 60] amu)
+    with nw in {8, 16, 24}, nb in {6, 12, 18} and WS sets of 93-279 vectors,
+    and ``n_requests`` requests drawn over them: crystal i % len(crystals), a
+    cubic mesh uniform in ``mesh_range``, a full window width uniform in
+    ``window_range`` eV about mid-gap + 0.6 eV, 300 K, Gaussian delta 10 meV.
+    Returns (list of WannierData, list of (crystal index, RateRequest))."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = crystals if crystals is not None else BATCH_CRYSTALS
+    wds = []
+    for c, (nw, nat, sc) in enumerate(specs):
+        crys = make_crystal_multi(nat, rng)
+        wds.append(make_wannier(crys, nw, supercell=sc, seed=seed + 1 + c))
+    reqs = []
+    for i in range(n_requests):
+        c = i % len(wds)
+        m = int(rng.integers(mesh_range[0], mesh_range[1] + 1))
+        width = float(rng.uniform(*window_range))
+        reqs.append((c, si_like_request(wds[c], (m, m, m), window=0.5 * width)))
+    return wds, reqs

@@ -274,3 +274,46 @@ class Wannier:
             self.deallocate_wannier()
         except Exception:
             pass
+
+
+def _rate_request(req, precision):
+    r = _lib.RateRequest()
+    for i in range(3):
+        r.mesh[i] = int(req.mesh[i])
+    r.enref, r.fsthick, r.chempot, r.T = req.enref, req.fsthick, req.chempot, req.T
+    r.delta_kind, r.sigma, r.precision = int(req.delta_kind), float(req.sigma), int(precision)
+    return r
+
+
+def el_rates_batch(crystals, reqs, precision=_lib.PREC_SPLIT_TF32, nslots=8, grouped=True, budget=0,
+                   raise_on_error=True):
+    """The batched form (``ephg_el_rates_batch``): request i against crystal
+    ``crystals[i]`` (a ``Wannier``; repeats allowed), all solved in one call.
+    Returns (outputs, batch stats, status codes); output i is laid out as
+    ``Wannier.el_rates``'s (None where the request failed)."""
+    n = len(reqs)
+    if len(crystals) != n or n == 0:
+        raise ValueError("one crystal per request")
+    L = _lib.load()
+    R = (_lib.RateRequest * n)(*[_rate_request(q, precision) for q in reqs])
+    H = (ct.c_void_p * n)(*[c._h for c in crystals])
+    rates = [np.zeros((int(np.prod(q.mesh)), c.numwannbands), order="F") for q, c in zip(reqs, crystals)]
+    idx = [np.zeros(int(np.prod(q.mesh)), dtype=np.int64) for q in reqs]
+    RP = (c_dp * n)(*[_p(a) for a in rates])
+    IP = (c_i64p * n)(*[_p(a, c_i64p) for a in idx])
+    st = (_lib.RateStats * n)()
+    status = (ct.c_int * n)()
+    opts = _lib.BatchOpts(int(nslots), int(budget), 1 if grouped else 0)
+    bs = _lib.BatchStats()
+    rc = L.ephg_el_rates_batch(n, H, R, RP, IP, st, status, ct.byref(opts), ct.byref(bs))
+    if rc != _lib.EPHG_OK and raise_on_error:
+        check(rc)
+    outs = []
+    for i in range(n):
+        if status[i] != _lib.EPHG_OK:
+            outs.append(None)
+            continue
+        nwv = int(st[i].nwv)
+        outs.append(dict(nwv=nwv, indexlist=idx[i][:nwv].copy(), rates=np.asfortranarray(rates[i][:nwv]),
+                         stats=st[i].as_dict(), nstates=int(st[i].nstates), vertices=int(st[i].vertices)))
+    return outs, bs.as_dict(), list(status)

@@ -265,6 +265,44 @@ int ephg_wait(ephg_server *s, int64_t ticket, double *rates, int64_t *indexlist,
               double *latency_ms);
 int ephg_server_stats_get(ephg_server *s, ephg_server_stats *out);
 
+/* ---- Batched form ----
+ * No counterpart in the reference (one crystal, one request per run).  n rate
+ * requests, request i against crystal handle crystals[i] (any number of
+ * distinct handles, repeats allowed), solved together: up to nslots requests
+ * run at once, one host thread and stream each, largest estimated work first.
+ * With grouped != 0 the split form's generic contractions (every shape but
+ * the nw = 8, nb = 6 Gaussian one, which runs its own fused kernels) meet in
+ * rounds: when every request inside a contraction stage has reached its next
+ * GEMM, those GEMMs (different crystals, shapes and operands) run as ONE
+ * persistent tcgen05 launch over all their tiles.  The requests' workspaces
+ * share hbm_budget_bytes (0: 80% of the device memory free at the call); a
+ * request that does not fit runs again alone after the others, with the
+ * whole budget.  Outputs per request as for ephg_el_rates (rates[i] (N_i,nw_i),
+ * indexlists[i] (N_i), stats + 0..n-1 nullable), status[i] its return code;
+ * every result equals the same request run alone.  Returns EPHG_OK when every
+ * request succeeded, else the first failing request's code. */
+typedef struct {
+  int64_t nslots;             /* requests running at once, 1..64; 0 = 8 */
+  int64_t hbm_budget_bytes;   /* workspace budget of the batch; 0 = 80% of the free device memory */
+  int64_t grouped;            /* 1: grouped GEMM launches across the running requests; 0: each its own */
+} ephg_batch_opts;
+
+typedef struct {
+  int64_t requests, failed, vertices;
+  double wall_ms;             /* host wall time of the call */
+  double vertices_per_s;      /* vertices / wall_ms */
+  int64_t group_launches;     /* grouped GEMM launches */
+  int64_t group_problems;     /* GEMMs they ran */
+  int64_t group_tiles;        /* 128 x 128 output tiles they ran */
+  int64_t max_group;          /* most GEMMs in one launch */
+  int64_t retried_alone;      /* requests re-run alone after their workspace did not fit */
+  int64_t peak_workspace_bytes;
+} ephg_batch_stats;
+
+int ephg_el_rates_batch(int64_t n, ephg_handle *const *crystals, const ephg_rate_request *reqs,
+                        double *const *rates, int64_t *const *indexlists, ephg_rate_stats *stats, int *status,
+                        const ephg_batch_opts *opts, ephg_batch_stats *bstats);
+
 /* el_wann without any device allocation.  No counterpart in the reference:
  * it serves callers that cannot allocate device memory where they need the
  * electrons -- a host code handing over buffers it already owns on the device
