@@ -847,7 +847,9 @@ __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int 
 // Modes are taken sch at a time so that the staged g fits shared memory for
 // any nb.  kinv[kp] = Rp cell at contraction position kp (-1 for padding).
 constexpr int ROT_KT = 8;
+static_assert(ROT_KT == 8, "k_rotate_k writes 8 K positions as two float4 per plane");
 constexpr int ROT_SMEM = 160 * 1024;
+constexpr int ROT_SMEM_TARGET = 72 * 1024;
 
 // shared memory of k_rotate_k for sch modes per pass and nsk <= nw states per row
 static size_t rotate_k_smem(int nw, int sch) {
@@ -882,11 +884,34 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
     const int ns = min(sch, nb - s0), pc = nn * ns, nc = nw * ns;
     for (int kp0 = 0; kp0 < Kp2; kp0 += ROT_KT) {
       __syncthreads();
-      for (int t = threadIdx.x; t < ROT_KT * pc; t += blockDim.x) {
-        int kk = t / pc, e = t % pc;
-        int rp = kinv[kp0 + kk];
-        const int64_t off = grow + (int64_t)rp * per + nn * s0 + e;
-        sg[t] = rp >= 0 ? make_float2(gr[off], gi[off]) : make_float2(0.f, 0.f);
+      // 16-byte loads (4 consecutive values; every row offset is a multiple of 4),
+      // four of them in flight per thread before the shared stores
+      const int pc4 = pc >> 2, tot = ROT_KT * pc4;
+      for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * blockDim.x) {
+        float4 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          a[u] = b[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (t < tot) {
+            const int kk = t / pc4, e = 4 * (t - kk * pc4);
+            const int rp = kinv[kp0 + kk];
+            if (rp >= 0) {
+              const int64_t off = grow + (int64_t)rp * per + nn * s0 + e;
+              a[u] = __ldg((const float4 *)(gr + off));
+              b[u] = __ldg((const float4 *)(gi + off));
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          if (t < tot) {
+            float4 *dst = (float4 *)(sg + 4 * t);
+            dst[0] = make_float4(a[u].x, b[u].x, a[u].y, b[u].y);
+            dst[1] = make_float4(a[u].z, b[u].z, a[u].w, b[u].w);
+          }
+        }
       }
       if (threadIdx.x < ROT_KT) {
         int rp = kinv[kp0 + threadIdx.x];
@@ -898,17 +923,41 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
         sph[threadIdx.x] = ph;
       }
       __syncthreads();
-      for (int o = threadIdx.x; o < nsk * nc * ROT_KT; o += blockDim.x) {
-        const int kk = o % ROT_KT, c = (o / ROT_KT) % nc, js = o / (ROT_KT * nc);
+      // a thread forms the ROT_KT positions of one operand row: lanes walk
+      // consecutive bands n' (conflict-free shared reads) and each writes whole
+      // 32-byte sectors of the four planes
+      for (int o = threadIdx.x; o < nsk * nc; o += blockDim.x) {
+        const int c = o % nc, js = o / nc;
         const int np = c % nw, s = c / nw;
-        float2 acc = make_float2(0.f, 0.f);
-        const float2 *g = sg + kk * pc + np + nn * s;
+        float2 acc[ROT_KT];
+#pragma unroll
+        for (int kk = 0; kk < ROT_KT; ++kk) acc[kk] = make_float2(0.f, 0.f);
+        const float2 *g = sg + np + nn * s;
         const float2 *u = sU + js * nw;
-        for (int mp = 0; mp < nw; ++mp) cfmaf(acc, u[mp], g[nw * mp]);
-        const float2 ph = sph[kk];
+        for (int mp = 0; mp < nw; ++mp) {
+          const float2 um = u[mp];
+#pragma unroll
+          for (int kk = 0; kk < ROT_KT; ++kk) cfmaf(acc[kk], um, g[kk * pc + nw * mp]);
+        }
+        float pl[4][ROT_KT];
+#pragma unroll
+        for (int kk = 0; kk < ROT_KT; ++kk) {
+          const float2 ph = sph[kk];
+          float hr, lr, hi, li;
+          split2((double)(ph.x * acc[kk].x - ph.y * acc[kk].y), hr, lr);
+          split2((double)(ph.x * acc[kk].y + ph.y * acc[kk].x), hi, li);
+          pl[0][kk] = hr;
+          pl[1][kk] = hi;
+          pl[2][kk] = lr;
+          pl[3][kk] = li;
+        }
         const int64_t col = (int64_t)(j0 + js) * ncol + np + nw * (s0 + s);
-        put4(Bp, plane, col * Kp2 + kp0 + kk,
-             make_double2((double)(ph.x * acc.x - ph.y * acc.y), (double)(ph.x * acc.y + ph.y * acc.x)));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float4 *dst = (float4 *)(Bp + q * plane + col * Kp2 + kp0);
+          dst[0] = make_float4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+          dst[1] = make_float4(pl[q][4], pl[q][5], pl[q][6], pl[q][7]);
+        }
       }
     }
   }
@@ -1094,11 +1143,41 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
   for (int j = jb0; j < jb1; ++j) {
     __syncthreads();
     const int64_t cbase = (int64_t)(j - j0) * ncol;
-    for (int t = threadIdx.x; t < EPI_ROWS * ncol; t += EPI_ROWS) {
-      const int r = t / ncol, c = t % ncol;
-      const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + c;    // rows < Mp exist in the chunk
-      sr[r * ld + c] = Cr[o];
-      si[r * ld + c] = Ci[o];
+    if ((ncol & 3) == 0) {
+      // 16-byte streaming loads, four rows' worth in flight per thread before
+      // the shared stores (rows < Mp exist in the chunk; ldc and the state's
+      // column offset are multiples of 4)
+      const int nc4 = ncol >> 2, tot = EPI_ROWS * nc4;
+      for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * EPI_ROWS) {
+        float4 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * EPI_ROWS;
+          if (t < tot) {
+            const int r = t / nc4, c4 = t - r * nc4;
+            const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + 4 * c4;
+            a[u] = __ldcs((const float4 *)(Cr + o));
+            b[u] = __ldcs((const float4 *)(Ci + o));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * EPI_ROWS;
+          if (t < tot) {
+            const int r = t / nc4, c = 4 * (t - r * nc4);
+            float *dr = sr + r * ld + c, *di = si + r * ld + c;
+            dr[0] = a[u].x, dr[1] = a[u].y, dr[2] = a[u].z, dr[3] = a[u].w;
+            di[0] = b[u].x, di[1] = b[u].y, di[2] = b[u].z, di[3] = b[u].w;
+          }
+        }
+      }
+    } else {
+      for (int t = threadIdx.x; t < EPI_ROWS * ncol; t += EPI_ROWS) {
+        const int r = t / ncol, c = t % ncol;
+        const int64_t o = (int64_t)(ip0 + r) * ldc + cbase + c;    // rows < Mp exist in the chunk
+        sr[r * ld + c] = Cr[o];
+        si[r * ld + c] = Ci[o];
+      }
     }
     __syncthreads();
     double v = 0.0;
@@ -1186,6 +1265,118 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
       for (int w = 0; w < EPI_ROWS / 32; ++w) sacc += wsum[w];
       partial[(size_t)j * nblk + blockIdx.x] = sacc;
     }
+  }
+}
+
+// Generic-shape split epilogue without shared-memory staging: one thread per
+// (k' row, state), EPI_ROWS consecutive rows of one state per block.  A thread
+// reads its row's nw x nb complex Rp sums as 16-byte loads straight from the
+// GEMM output (the two 16-byte halves of a sector meet in L1), so that shared
+// memory does not cap the resident warps.  NW bands fixed at compile time (the
+// band and mode arrays then live in registers), nb <= EPR_NB.
+constexpr int EPR_NB = 18;
+
+template <int NW>
+__global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, const float *Cr, const float *Ci,
+                                                            int64_t ldc, RateParams rp, EpiData d, QTab qt,
+                                                            double *partial, int nblk) {
+  static_assert(NW % 4 == 0, "16-byte row loads");
+  __shared__ double wsum[EPI_ROWS / 32];
+  const int ip = blockIdx.x * EPI_ROWS + threadIdx.x;
+  const int j = j0 + blockIdx.y;
+  const int nb = rp.nb, ncol = NW * nb;
+  double v = 0.0;
+  if (ip < nwv) {
+    const int code = d.st_code[j];
+    const int i = code / NW, m = code % NW;
+    const int p = d.sidx[i], pp = d.widx[ip];
+    const double E = d.ens[(size_t)p * NW + m];
+    const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+    const double inv_sig = 1.0 / rp.sigma;
+    const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
+    const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
+    const int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
+    const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
+                        rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
+    const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    const float *rr = Cr + base, *ri = Ci + base;
+    const bool ph = d.phr || d.yv;
+    const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
+    float acc = 0.0f;
+    int rank_n = 0;
+    for (int n = 0; n < NW; ++n) {
+      const double eps = d.ens[(size_t)pp * NW + n];
+      if (fabs(eps - rp.enref) > rp.fsthick) continue;
+      const float2 *Ukp = d.Uf + ((size_t)pp * NW + n) * NW;
+      float2 uk[NW];
+#pragma unroll
+      for (int c = 0; c < NW; ++c) uk[c] = Ukp[c];
+      float2 unm = make_float2(0.f, 0.f);   // <U_k'[n]|U_k[m]>, polar crystals
+      if (d.glpf) {
+        const float2 *Uk = d.Uf + ((size_t)p * NW + m) * NW;
+#pragma unroll
+        for (int c = 0; c < NW; ++c) cfmaf_cj(unm, uk[c], Uk[c]);
+      }
+      float2 h[EPR_NB];
+#pragma unroll
+      for (int s = 0; s < EPR_NB; ++s) {
+        if (s >= nb) break;
+        float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < NW; c += 4) {
+          const float4 xr = __ldg((const float4 *)(rr + c + NW * s));
+          const float4 xi = __ldg((const float4 *)(ri + c + NW * s));
+          cfmaf_cj(a, uk[c], make_float2(xr.x, xi.x));
+          cfmaf_cj(a, uk[c + 1], make_float2(xr.y, xi.y));
+          cfmaf_cj(a, uk[c + 2], make_float2(xr.z, xi.z));
+          cfmaf_cj(a, uk[c + 3], make_float2(xr.w, xi.w));
+        }
+        h[s] = a;
+      }
+      const float dn = (float)((E - eps) * inv_sig);
+#pragma unroll
+      for (int s = 0; s < EPR_NB; ++s) {
+        if (s >= nb) break;
+        const int qs = q * nb + s;
+        const float2 *u = d.uf + (size_t)qs * nb;
+        float2 g = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int sp = 0; sp < EPR_NB; ++sp)
+          if (sp < nb) cfmaf(g, u[sp], h[sp]);
+        if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
+        const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
+        const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
+        const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
+        const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
+        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
+        const float xp = g2c * (qt.bose[qs] + fp) * dp;
+        const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+        acc += xp + xm;
+        const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
+        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+        if (d.g2) {
+          int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
+          if (off < d.cap) {
+            const double om = d.om[qs];
+            d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
+            d.xp[off] = xp;
+            d.xm[off] = xm;
+            if (d.yv) d.yv[off] = y;
+          }
+        }
+      }
+      rank_n++;
+    }
+    v = (double)acc;
+  }
+  // fixed-order block reduction: warp shuffle tree, then the warp sums in order
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int w = 0; w < EPI_ROWS / 32; ++w) sacc += wsum[w];
+    partial[(size_t)j * nblk + blockIdx.x] = sacc;
   }
 }
 
@@ -2122,11 +2313,12 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
       return rc;
     tA->end(st);
     {
-      // modes per pass: all of them when the staged g fits, else as many as fit
+      // modes per pass: as many as keep the staged g within ROT_SMEM_TARGET (three
+      // blocks per SM), at least one (up to ROT_SMEM)
       int sch = nb;
-      while (sch > 1 && rotate_k_smem(nw, sch) > (size_t)ROT_SMEM) --sch;
+      while (sch > 1 && rotate_k_smem(nw, sch) > (size_t)ROT_SMEM_TARGET) --sch;
       const size_t sm = rotate_k_smem(nw, sch);
-      if (sm <= (size_t)ROT_SMEM) {
+      if (sm <= (size_t)ROT_SMEM && (nw % 2) == 0) {   // 16-byte staging: nw * nw a multiple of 4
         // once per process: changing a kernel attribute can wait for the device's queued work
         static std::once_flag attr_once;
         std::call_once(attr_once, [] {
@@ -2183,7 +2375,19 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
       return rc;
     tB->end(st);
     const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
-    if (rp.delta_kind == 0 && esm > 200 * 1024) {
+    const bool rows_kernel = rp.delta_kind == 0 && nb <= EPR_NB && (nw == 8 || nw == 16 || nw == 24 || nw == 32);
+    if (rows_kernel) {
+      dim3 grid(nblk, ns);
+      if (nw == 8)
+        k_epilogue_rows<8><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      else if (nw == 16)
+        k_epilogue_rows<16><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      else if (nw == 24)
+        k_epilogue_rows<24><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      else
+        k_epilogue_rows<32><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      TCK(cudaGetLastError());
+    } else if (rp.delta_kind == 0 && esm > 200 * 1024) {
       dim3 grid(nblk, ns);
       k_epilogue_split<<<grid, 128, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
       TCK(cudaGetLastError());
