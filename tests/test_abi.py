@@ -57,3 +57,19 @@ def test_null_arguments(lib):
     assert lib.ephg_el_wann(None, 1, None, None, None, None, None) == _lib.EPHG_ERR_ARG
     assert lib.ephg_el_rates(None, None, None, None, None, None, None, None, 0) == _lib.EPHG_ERR_ARG
     assert lib.ephg_destroy(None) == _lib.EPHG_OK
+
+
+def test_batch_refuses_bad_arguments(lib):
+    """ephg_el_rates_batch checks its arguments before touching a device."""
+    n = 2
+    H = (ct.c_void_p * n)(None, None)
+    R = (_lib.RateRequest * n)()
+    RP = (_lib.c_dp * n)()
+    IP = (_lib.c_i64p * n)()
+    st = (ct.c_int * n)()
+    assert lib.ephg_el_rates_batch(0, H, R, RP, IP, None, st, None, None) == _lib.EPHG_ERR_ARG
+    assert lib.ephg_el_rates_batch(n, None, R, RP, IP, None, st, None, None) == _lib.EPHG_ERR_ARG
+    assert lib.ephg_el_rates_batch(n, H, R, RP, IP, None, None, None, None) == _lib.EPHG_ERR_ARG
+    # null crystal handles
+    assert lib.ephg_el_rates_batch(n, H, R, RP, IP, None, st, None, None) == _lib.EPHG_ERR_ARG
+    assert b"null crystal" in lib.ephg_last_error()
