@@ -20,12 +20,16 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <mutex>
+#include <random>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "../../include/ephg.h"
+#include "../../include/ephg_debug.h"
+#include "ephg_gate.cuh"
 #include "ephg_handle.cuh"
 
 namespace {
@@ -225,5 +229,90 @@ extern "C" int ephg_el_rates_batch(int64_t n, ephg_handle *const *crystals, cons
   if (first_bad >= 0)
     return api_fail(status[first_bad], "el_rates_batch: request %lld: %s", (long long)first_bad,
                     msg[first_bad].c_str());
+  return EPHG_OK;
+}
+
+// The round logic of the grouped launches (ephg::RoundGate) under host
+// threads only: members alternate active stretches of 1-4 submissions, with
+// random pauses, and inactive stretches; some become active by submitting.
+// The launch callback checks that each member's items arrive once each, in
+// order; each submit checks that its item was launched before it returned.
+extern "C" int ephg_debug_batcher_selftest(int nmembers, int iters, uint64_t seed, int64_t *rounds,
+                                           int64_t *max_group) {
+  using ephg::api_fail;
+  if (nmembers < 1 || nmembers > 64 || iters < 1) return api_fail(EPHG_ERR_ARG, "batcher_selftest: bad arguments");
+  struct Item {
+    int64_t seq;
+  };
+  struct Shared {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<int64_t> launched;   // last sequence number launched, per member
+    int64_t items = 0, max_group = 0, finished = 0;
+    std::string why;
+  };
+  auto *sh = new Shared;   // leaked on a deadlock: the blocked threads still refer to it
+  sh->launched.assign(nmembers, -1);
+  auto *gate = new ephg::RoundGate<Item>(nmembers, [sh](std::vector<std::pair<int, Item>> &r) {
+    std::lock_guard<std::mutex> lk(sh->mu);
+    std::vector<char> seen(sh->launched.size(), 0);
+    for (auto &it : r) {
+      if (seen[it.first]) sh->why = "a member has two items in one round";
+      seen[it.first] = 1;
+      if (it.second.seq != sh->launched[it.first] + 1) sh->why = "a member's items launched out of order or lost";
+      sh->launched[it.first] = it.second.seq;
+    }
+    sh->items += (int64_t)r.size();
+    sh->max_group = std::max<int64_t>(sh->max_group, (int64_t)r.size());
+    return 0;
+  });
+  std::vector<std::thread> th;
+  std::vector<int64_t> submitted(nmembers, 0);
+  for (int w = 0; w < nmembers; ++w)
+    th.emplace_back([=, &submitted] {
+      std::mt19937_64 rng(seed * 1000003ull + (uint64_t)w);
+      int64_t seq = 0;
+      for (int it = 0; it < iters; ++it) {
+        if (rng() & 1) gate->activate(w);
+        const int k = 1 + (int)(rng() % 4);
+        for (int j = 0; j < k; ++j) {
+          std::this_thread::sleep_for(std::chrono::microseconds(rng() % 200));
+          const int rc = gate->submit(w, Item{seq});
+          std::lock_guard<std::mutex> lk(sh->mu);
+          if (rc != 0) sh->why = "submit returned an error";
+          if (sh->launched[w] < seq) sh->why = "submit returned before its round was launched";
+          ++seq;
+        }
+        gate->deactivate(w);
+        std::this_thread::sleep_for(std::chrono::microseconds(rng() % 300));
+      }
+      submitted[w] = seq;
+      std::lock_guard<std::mutex> lk(sh->mu);
+      ++sh->finished;
+      sh->cv.notify_all();
+    });
+  bool done;
+  {
+    std::unique_lock<std::mutex> lk(sh->mu);
+    done = sh->cv.wait_for(lk, std::chrono::seconds(60), [&] { return sh->finished == nmembers; });
+  }
+  if (!done) {   // a deadlock: the members stay blocked; report it and leave them be
+    for (auto &t : th) t.detach();
+    return api_fail(EPHG_ERR_TIMEOUT, "batcher_selftest: members still blocked after 60 s");
+  }
+  for (auto &t : th) t.join();
+  int64_t total = 0;
+  for (int64_t x : submitted) total += x;
+  const uint64_t nr = gate->rounds();
+  std::string why = sh->why;
+  const int64_t items = sh->items, mg = sh->max_group;
+  delete gate;
+  delete sh;
+  if (rounds) *rounds = (int64_t)nr;
+  if (max_group) *max_group = mg;
+  if (!why.empty()) return api_fail(EPHG_ERR_INDEX, "batcher_selftest: %s", why.c_str());
+  if (items != total)
+    return api_fail(EPHG_ERR_INDEX, "batcher_selftest: %lld items launched of %lld submitted", (long long)items,
+                    (long long)total);
   return EPHG_OK;
 }

@@ -36,6 +36,7 @@
 #include <cstring>
 #include <string>
 
+#include "ephg_gate.cuh"
 #include "ephg_tc.cuh"
 
 namespace ephg {
@@ -504,7 +505,8 @@ static int num_sms() {
 // round back.
 class GemmBatcher {
  public:
-  explicit GemmBatcher(int n) : act_(n, 0), rc_(n, 0), ready_(n, nullptr) {
+  explicit GemmBatcher(int n)
+      : ready_(n, nullptr), gate_(n, [this](std::vector<std::pair<int, Pend>> &r) { return launch_round(r); }) {
     cudaStreamCreateWithFlags(&gst_, cudaStreamNonBlocking);
     cudaEventCreateWithFlags(&done_, cudaEventDisableTiming);
     for (auto &e : ready_) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -527,26 +529,11 @@ class GemmBatcher {
     if (gst_) cudaStreamDestroy(gst_);
   }
   bool ok() const { return ok_; }
-  void activate(int id) {
-    std::lock_guard<std::mutex> lk(mu_);
-    if (!act_[id]) { act_[id] = 1; ++active_; }
-  }
-  void deactivate(int id) {
-    std::unique_lock<std::mutex> lk(mu_);
-    if (!act_[id]) return;
-    act_[id] = 0;
-    --active_;
-    if (!pend_.empty() && (int)pend_.size() == active_) launch_locked();
-  }
+  void activate(int id) { gate_.activate(id); }
+  void deactivate(int id) { gate_.deactivate(id); }
   int submit(int id, const GroupProblem &p, cudaStream_t st) {
     if (cudaEventRecord(ready_[id], st) != cudaSuccess) return tfail(2, "batch: event record failed");
-    std::unique_lock<std::mutex> lk(mu_);
-    if (!act_[id]) { act_[id] = 1; ++active_; }
-    pend_.push_back({id, st, p});
-    const uint64_t my = round_;
-    if ((int)pend_.size() == active_) launch_locked();
-    else cv_.wait(lk, [&] { return round_ != my; });
-    return rc_[id];
+    return gate_.submit(id, Pend{st, p});
   }
   // device word of the grouped launches' bounded waits (read after the members finished)
   int device_error() {
@@ -565,27 +552,32 @@ class GemmBatcher {
  private:
   static constexpr int kRing = 8;
   struct Pend {
-    int id;
     cudaStream_t st;
     GroupProblem p;
   };
-  void launch_locked() {
+  // one round (under the gate's lock): table upload, the grouped launch, and the
+  // members' streams made to wait for it
+  int launch_round(std::vector<std::pair<int, Pend>> &pend) {
     // heaviest tiles (most K blocks) first: the strided tile order then ends on light tiles
-    std::stable_sort(pend_.begin(), pend_.end(), [](const Pend &a, const Pend &b) { return a.p.g.nkb > b.p.g.nkb; });
-    const int np = (int)pend_.size();
-    const int slot = (int)(round_ % kRing);
+    std::stable_sort(pend.begin(), pend.end(),
+                     [](const std::pair<int, Pend> &a, const std::pair<int, Pend> &b) {
+                       return a.second.p.g.nkb > b.second.p.g.nkb;
+                     });
+    const int np = (int)pend.size();
+    const int slot = (int)(nround_++ % kRing);
     GroupProblem *h = htab_ + (size_t)slot * cap_, *d = dtab_ + (size_t)slot * cap_;
     cudaEventSynchronize(slot_ev_[slot]);   // the copy that last read this staging slot has run
     int64_t T = 0;
     for (int i = 0; i < np; ++i) {
-      h[i] = pend_[i].p;
+      h[i] = pend[i].second.p;
       h[i].tile0 = (int)T;
       T += (int64_t)h[i].g.mtiles * h[i].g.ntiles;
     }
     int rc = 0;
     if (T > INT32_MAX) rc = tfail(1, "batch: too many tiles in one round");
     for (int i = 0; i < np && !rc; ++i)
-      if (cudaStreamWaitEvent(gst_, ready_[pend_[i].id], 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
+      if (cudaStreamWaitEvent(gst_, ready_[pend[i].first], 0) != cudaSuccess)
+        rc = tfail(2, "batch: stream wait failed");
     if (!rc && cudaMemcpyAsync(d, h, sizeof(GroupProblem) * np, cudaMemcpyHostToDevice, gst_) != cudaSuccess)
       rc = tfail(2, "batch: problem table upload failed");
     if (!rc) {
@@ -595,32 +587,24 @@ class GemmBatcher {
       if (cudaGetLastError() != cudaSuccess) rc = tfail(2, "batch: grouped GEMM launch failed");
     }
     if (!rc && cudaEventRecord(done_, gst_) != cudaSuccess) rc = tfail(2, "batch: event record failed");
-    for (auto &q : pend_) {
-      if (!rc && cudaStreamWaitEvent(q.st, done_, 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
-      rc_[q.id] = rc;
-    }
+    for (auto &q : pend)
+      if (!rc && cudaStreamWaitEvent(q.second.st, done_, 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
     ++launches_;
     problems_ += np;
     tiles_ += T;
     max_group_ = std::max<int64_t>(max_group_, np);
-    pend_.clear();
-    ++round_;
-    cv_.notify_all();
+    return rc;
   }
-  std::mutex mu_;
-  std::condition_variable cv_;
-  std::vector<char> act_;
-  std::vector<int> rc_;
   std::vector<cudaEvent_t> ready_;
-  std::vector<Pend> pend_;
-  int active_ = 0, cap_ = 0;
-  uint64_t round_ = 0;
+  int cap_ = 0;
+  uint64_t nround_ = 0;
   cudaStream_t gst_ = nullptr;
   cudaEvent_t done_ = nullptr, slot_ev_[kRing] = {};
   GroupProblem *htab_ = nullptr, *dtab_ = nullptr;
   int *derr_ = nullptr;
   bool ok_ = false;
   int64_t launches_ = 0, problems_ = 0, tiles_ = 0, max_group_ = 0;
+  RoundGate<Pend> gate_;   // last: its callback uses the members above
 };
 
 GemmBatcher *batcher_create(int nmembers) {

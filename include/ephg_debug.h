@@ -34,6 +34,16 @@ const char *ephg_debug_last_error(void);
 int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t budget, int64_t per_request_bytes,
                                const int64_t *meshes, ephg_server_stats *out, int *max_concurrent, double *lat_ms);
 
+/* The batched form's round logic (the grouped launches' gate) under nmembers
+ * host threads, no GPU: members alternate active stretches of 1-4 submissions
+ * with random pauses (seeded) and inactive stretches, iters times each.
+ * Checks that every submission is launched exactly once, in each member's
+ * order, before its submit returns, and that no member stays blocked (60 s).
+ * Fills *rounds (launches) and *max_group (most items in one launch);
+ * returns EPHG_ERR_INDEX on a broken invariant, EPHG_ERR_TIMEOUT on a
+ * deadlock. */
+int ephg_debug_batcher_selftest(int nmembers, int iters, uint64_t seed, int64_t *rounds, int64_t *max_group);
+
 #ifdef __cplusplus
 }
 #endif
