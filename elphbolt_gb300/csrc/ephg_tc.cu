@@ -36,6 +36,7 @@
 #include <cstring>
 #include <string>
 
+#include "../../include/ephg_debug.h"
 #include "ephg_gate.cuh"
 #include "ephg_tc.cuh"
 
@@ -234,7 +235,8 @@ struct TileJob {
   int64_t ldc;
 };
 
-__device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, const CUtensorMap *tB, const GemmArgs &g, int t) {
+__host__ __device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, const CUtensorMap *tB, const GemmArgs &g,
+                                                     int t) {
   const int mt = t % g.mtiles, nt = t / g.mtiles;
   TileJob j;
   j.tA = tA;
@@ -272,11 +274,16 @@ struct GroupGemm {
   const GroupProblem *tab;
   int np;
   static constexpr bool kGlobalMaps = true;
-  __device__ __forceinline__ TileJob operator()(int t) const {
+  __host__ __device__ __forceinline__ TileJob operator()(int t) const {
     int lo = 0, hi = np - 1;   // last problem with tile0 <= t
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(&tab[mid].tile0) <= t) lo = mid; else hi = mid - 1;
+#ifdef __CUDA_ARCH__
+      const int t0 = __ldg(&tab[mid].tile0);
+#else
+      const int t0 = tab[mid].tile0;
+#endif
+      if (t0 <= t) lo = mid; else hi = mid - 1;
     }
     const GroupProblem *q = tab + lo;
     return tile_job(&q->tA, &q->tB, q->g, t - q->tile0);
@@ -2657,3 +2664,41 @@ extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A
 }
 
 extern "C" const char *ephg_debug_last_error(void) { return ephg::tc::last_error(); }
+
+// The grouped GEMM's tile lookup on the host: np problems of mtiles[i] x
+// ntiles[i] tiles laid out as the batcher lays them out; every tile of the
+// launch is mapped and hits[tile0(i) + mt + mtiles[i] nt] counted.  Returns
+// EPHG_ERR_INDEX if a tile maps outside its problem or its rows disagree.
+extern "C" int ephg_debug_group_tiles(int np, const int *mtiles, const int *ntiles, int *hits) {
+  using namespace ephg::tc;
+  if (np <= 0 || !mtiles || !ntiles || !hits) return 1;
+  std::vector<GroupProblem> tab(np);
+  int64_t T = 0;
+  for (int i = 0; i < np; ++i) {
+    memset(&tab[i], 0, sizeof(GroupProblem));
+    if (mtiles[i] <= 0 || ntiles[i] <= 0) return 1;
+    tab[i].g.mtiles = mtiles[i];
+    tab[i].g.ntiles = ntiles[i];
+    tab[i].g.nkb = 1;
+    tab[i].g.Astride = (int64_t)mtiles[i] * BM;
+    tab[i].g.Bstride = (int64_t)ntiles[i] * BN;
+    tab[i].g.ldc = (int64_t)ntiles[i] * BN;
+    tab[i].tile0 = (int)T;
+    T += (int64_t)mtiles[i] * ntiles[i];
+  }
+  if (T > INT32_MAX) return 1;
+  const GroupGemm jobs{tab.data(), np};
+  for (int t = 0; t < (int)T; ++t) {
+    const TileJob j = jobs(t);
+    const int64_t p = (const uint8_t *)j.tA - (const uint8_t *)&tab[0].tA;
+    if (p < 0 || p % (int64_t)sizeof(GroupProblem)) return EPHG_ERR_INDEX;
+    const int i = (int)(p / (int64_t)sizeof(GroupProblem));
+    if (i >= np || j.tB != &tab[i].tB || j.arow % BM || j.brow % BN) return EPHG_ERR_INDEX;
+    const int mt = j.arow / BM, nt = j.brow / BN;
+    if (mt >= mtiles[i] || nt >= ntiles[i] || t - tab[i].tile0 != mt + mtiles[i] * nt) return EPHG_ERR_INDEX;
+    if ((int64_t)(j.Cr - (float *)nullptr) != (int64_t)mt * BM * tab[i].g.ldc + (int64_t)nt * BN)
+      return EPHG_ERR_INDEX;
+    hits[tab[i].tile0 + mt + mtiles[i] * nt]++;
+  }
+  return EPHG_OK;
+}

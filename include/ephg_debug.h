@@ -44,6 +44,14 @@ int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t 
  * deadlock. */
 int ephg_debug_batcher_selftest(int nmembers, int iters, uint64_t seed, int64_t *rounds, int64_t *max_group);
 
+/* The grouped GEMM's tile -> (problem, row tile, column tile) lookup, run on
+ * the host over np problems of mtiles[i] x ntiles[i] output tiles laid out in
+ * one launch's tile space as the batcher lays them out (problem i from tile
+ * sum_{j<i} mtiles[j] ntiles[j]); counts each tile's hits in hits[] (sized
+ * to the total).  Returns EPHG_ERR_INDEX if a tile maps outside its problem
+ * or its operand rows and output offset disagree. */
+int ephg_debug_group_tiles(int np, const int *mtiles, const int *ntiles, int *hits);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,3 +34,23 @@ def test_gate_rounds(lib, members, iters, seed):
 def test_gate_refuses_bad_arguments(lib):
     assert lib.ephg_debug_batcher_selftest(0, 1, 0, None, None) == _lib.EPHG_ERR_ARG
     assert lib.ephg_debug_batcher_selftest(65, 1, 0, None, None) == _lib.EPHG_ERR_ARG
+
+
+def test_group_tile_lookup(lib):
+    """The grouped GEMM kernel's tile -> (problem, row tile, column tile) lookup,
+    run on the host over random problem sets: every tile of every problem is
+    hit exactly once, and its operand rows and output offset agree."""
+    import numpy as np
+    lib.ephg_debug_group_tiles.argtypes = [ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int),
+                                           ct.POINTER(ct.c_int)]
+    lib.ephg_debug_group_tiles.restype = ct.c_int
+    rng = np.random.default_rng(11)
+    for np_ in (1, 2, 3, 7, 8, 31, 64):
+        m = rng.integers(1, 40, np_).astype(np.int32)
+        n = rng.integers(1, 300, np_).astype(np.int32)
+        hits = np.zeros(int((m.astype(np.int64) * n).sum()), dtype=np.int32)
+        rc = lib.ephg_debug_group_tiles(np_, m.ctypes.data_as(ct.POINTER(ct.c_int)),
+                                        n.ctypes.data_as(ct.POINTER(ct.c_int)),
+                                        hits.ctypes.data_as(ct.POINTER(ct.c_int)))
+        assert rc == _lib.EPHG_OK
+        assert np.all(hits == 1)
