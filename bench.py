@@ -327,10 +327,13 @@ def batched_side(steps):
     verts = bs[-1]["vertices"]
     same = all(np.array_equal(a["rates"], o["rates"]) for a, o in zip(alone, outs))
     gv = verts / (wall * 1e-3)
+    # algorithmic contraction work of the batch (stages A + B, complex MACs x 8)
+    gflop = float(sum(o["stats"]["stage_a_gflop"] + o["stats"]["stage_b_gflop"] for o in outs))
     return {"workload": "64 requests on 8 random crystals (nw 8/16/24, nb 6/12/18, WS 93-279), meshes 8^3-16^3, "
                         "windows 0.2-1.0 eV, Gaussian 10 meV, 300 K",
             "crystals": [[wd.numwannbands, wd.numbranches, int(wd.rcells_k.shape[0])] for wd in wds],
             "vertices_per_batch": verts, "ms_per_batch": wall, "value": gv, "unit": UNIT,
+            "contraction_gflop_per_batch": gflop, "contraction_tflops_over_wall": gflop / wall,
             "group": {k: bs[-1][k] for k in ("group_launches", "group_problems", "group_tiles", "max_group")},
             "ungrouped_ms_per_batch": float(np.median([b[1]["wall_ms"] for b in ungrouped])),
             "one_at_a_time_split_ms": t_alone * 1e3,
