@@ -129,3 +129,27 @@ def test_el_rates_split_vs_fp64_multi_tile():
     rel = np.abs(g["rates"] - d["rates"])[mask] / d["rates"][mask]
     assert rel.max() <= 1e-6, rel.max()
     assert np.all(g["rates"][~mask] == 0)
+
+
+@pytest.mark.parametrize("nw,natoms", [(24, 2), (32, 2), (32, 4)])
+def test_el_rates_wide_bands_vs_oracle(oracle_lib, nw, natoms):
+    """Wide band sets (nw 24 and 32, nb 6 and 12) through the generic split
+    path (stage-A rotation tiled over modes, the per-row epilogue of that nw)
+    and the FP64 form, against the oracle: rates within 1e-6 (split) and 1e-10
+    (FP64) relative."""
+    from elphbolt_gb300.wannier import Wannier
+    rng = np.random.default_rng(100 + nw + natoms)
+    wd = S.make_wannier(S.make_crystal_multi(natoms, rng), nw, supercell=(2, 2, 2), seed=300 + nw + natoms)
+    req = S.si_like_request(wd, (4, 4, 4), window=0.5, shift=0.6)
+    o = oracle_lib.Wannier(wd).el_rates(req, nthreads=4, literal=False)
+    W = Wannier(wd)
+    try:
+        outs = {p: W.el_rates(req, precision=p) for p in (_lib.PREC_SPLIT_TF32, _lib.PREC_FP64)}
+    finally:
+        W.deallocate_wannier()
+    scale = np.abs(o["rates"]).max()
+    for p, tol, floor in ((_lib.PREC_SPLIT_TF32, 1e-6, 1e-8), (_lib.PREC_FP64, 1e-10, 1e-14)):
+        g = outs[p]
+        assert np.array_equal(g["indexlist"], o["indexlist"]) and g["vertices"] == o["vertices"]
+        err = np.abs(g["rates"] - o["rates"])
+        assert np.all(err <= tol * np.abs(o["rates"]) + floor * scale), (p, float(err.max() / scale))
