@@ -16,8 +16,11 @@ rates -> destroy, every host<->device copy inside the timed region).
 ``--impl reference``: the reference algorithm on the host cores (the CPU
 restatement of the reference path, literal per-vertex g2, OpenMP over k').
 
-Multi-GPU: the path runs as independent replicas, one per rank (no
-collective on the data path); value is the whole job's vertices / max time.
+One GPU per call: the library's fused kernels share operand tiles between
+the two CTAs of a cluster by TMA multicast within this GPU's memory, and the
+path runs on one image and one GPU.  Under torchrun with more than one rank
+the GPU arm does no work and rank 0 prints a line saying so; the reference
+arm (host cores only) runs on rank 0.
 """
 from __future__ import annotations
 
@@ -95,19 +98,6 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def replica_value(dist, world, steps, vertices_per_step, local_ms):
-    """Whole-job vertices/s of `world` independent replicas (one per rank, no
-    collective on the data path): every rank runs the same request and the job
-    takes as long as the slowest rank (max over ranks, via the process group)."""
-    t = float(local_ms)
-    if dist is not None and world > 1:
-        import torch
-        x = torch.tensor([t], dtype=torch.float64)
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        t = float(x.item())
-    return world * steps * vertices_per_step / (t * 1e-3), t
-
-
 MESH = (24, 24, 24)
 
 
@@ -118,14 +108,13 @@ def workload():
     return wd, req
 
 
-def config_dict(wd, req, stats=None):
+def config_dict(wd, req):
+    """The workload, identical in both arms (run statistics go to ``stats``)."""
     c = {"workload": "Si-like fcc 2-atom, nwann 8, nmodes 6, %d Re / %d Rp WS cells (6^3), 24^3 k=q mesh, "
                      "window +-0.5 eV at mid-gap+0.6 eV, Gaussian delta 10 meV, T 300 K" % (wd.nwsk, wd.nwsq),
          "mesh": list(req.mesh), "nwann": wd.numwannbands, "nmodes": wd.numbranches,
          "n_ws_re": wd.nwsk, "n_ws_rp": wd.nwsq, "precision": "split-FP32 (3xTF32, FP32 accumulate)",
          "l2_policy": "inputs larger than L2 (g(Re,Rp) TF32 planes 494 MB, stage-B operand planes 2.9 GB)"}
-    if stats:
-        c.update({"window_k": stats["nwv"], "initial_states": stats["nstates"], "vertices_per_step": stats["vertices"]})
     return c
 
 
@@ -164,8 +153,24 @@ def cpu_sample(wd, req, seconds_target=20.0, states=None):
     R.close()
     v = b["vertices"]
     t = b["us_loop"] * 1e-6
+    # the oracle's rates of initial states 0 .. n (zero elsewhere), for the parity check
     return dict(value=v / t, cores=ncores, states=n, vertices=v, seconds=t, setup_s=t_setup,
-                nstates_total=a["nstates_inwindow"])
+                nstates_total=a["nstates_inwindow"], rates=a["rates"] + b["rates"], indexlist=b["indexlist"])
+
+
+def error_vs_oracle(cpu, gpu_idx, forms):
+    """Largest relative error per rate of each GPU form against the oracle, on
+    the initial states the oracle ran (the CPU sample)."""
+    import numpy as np
+    if not np.array_equal(cpu["indexlist"], gpu_idx):
+        return {"error": "window k lists differ"}
+    ref = cpu["rates"]
+    m = ref > 0
+    out = {"states": int(m.sum()), "what": "GPU rates vs the CPU oracle (FP64, literal per-vertex g2) on the "
+                                         "states of the cpu_baseline sample, full k' sums"}
+    for name, r in forms.items():
+        out[name + "_max_rel"] = float(np.max(np.abs(r[m] - ref[m]) / ref[m]))
+    return out
 
 
 def cpu_sample_ph(wd, req, seconds_target=10.0):
@@ -396,19 +401,12 @@ def run_ours(args, ws, rank, local):
 
     dev = 0
     torch.cuda.set_device(dev)
-    group = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        group = dist
     wd, req = workload()
     W = Wannier(wd)
     prec = _lib.PREC_SPLIT_TF32
     for _ in range(args.warmup):
         out = W.el_rates(req, precision=prec)
-    # ---- timed region: value ----
-    if group:
-        group.barrier()
+    # ---- timed region: value (one rank: the barrier is the synchronize) ----
     torch.cuda.synchronize()
     dev_ms, launches, gemm_ms, gemm_n, wall0 = [], 0, 0.0, 0, time.time()
     with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
@@ -421,14 +419,13 @@ def run_ours(args, ws, rank, local):
             gemm_n += st["gemm_b_launches"]
         torch.cuda.synchronize()
         wall = time.time() - wall0
-    if group:
-        group.barrier()
     st = out["stats"]
     vertices = st["vertices"]
-    value, total_ms = replica_value(group, ws, args.steps, vertices, float(sum(dev_ms)))
+    total_ms = float(sum(dev_ms))
+    value = args.steps * vertices / (total_ms * 1e-3)
     split_rates = out["rates"]
-    # ---- e2e: one-shot drop-in through the C ABI from pinned host buffers ----
-    e2e = e2e_measure(wd, req, prec, max(1, min(args.steps, 3)))
+    # ---- e2e: one-shot drop-in through the C ABI from pinned host buffers, same step count ----
+    e2e = e2e_measure(wd, req, prec, args.steps)
     # ---- FP64 plain drop-in on the same request (one step) ----
     f = W.el_rates(req, precision=_lib.PREC_FP64)
     fst = f["stats"]
@@ -436,33 +433,33 @@ def run_ours(args, ws, rank, local):
     ref = f["rates"]
     mask = ref > 0
     rate_err = float(np.max(np.abs(split_rates[mask] - ref[mask]) / ref[mask])) if mask.any() else None
-    ph = phonon_side(W, req, args.steps, float(np.median(dev_ms)), fst["ms_total"]) if rank == 0 else None
+    ph = phonon_side(W, req, args.steps, float(np.median(dev_ms)), fst["ms_total"])
     W.deallocate_wannier()
-    if rank != 0:
-        return 0
     # ---- roofline of the dominant kernel (stage-B 3xTF32 contraction fused with the rate epilogue) ----
     bf16, hbm, src = peaks()
     achieved = st["stage_b_gflop"] / (st["ms_gemm_b"] * 1e-3) / 1e3          # TFLOP/s algorithmic
     peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
     tpg = traffic_per_gflop()
     cpu = cpu_sample(wd, req)
+    parity = error_vs_oracle(cpu, out["indexlist"], {"split": split_rates, "fp64": ref})
     cpu_ph = cpu_sample_ph(wd, req)
     ph["cpu_baseline"] = {"value": cpu_ph["value"], "unit": UNIT, "cores": cpu_ph["cores"], "kind": "port",
                           "sample": "%d q-points x %d branches, %d vertices in %.1f s (gReq per q, literal 'el' "
                                     "g2 per vertex, OpenMP over k within each q)" % (cpu_ph["qpoints"], wd.numbranches,
                                                                        cpu_ph["vertices"], cpu_ph["seconds"])}
     serving = None
-    if not args.no_serving and ws == 1:   # the metric's p99 latency: the serving loop under a Poisson stream
+    if not args.no_serving:   # the metric's p99 latency: the serving loop under a Poisson stream
         try:
             from elphbolt_gb300 import serve_bench
             serving = serve_bench.measure(wds=serve_bench.make_crystals(base=wd))
         except Exception as e:   # the main line is still printed
             serving = {"error": repr(e)}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (3xTF32 contractions) + f64 (eigensolves, sums)",
             "data": "synthetic (seeded, reference units and layouts)",
-            "config": config_dict(wd, req, st),
+            "config": config_dict(wd, req),
+            "stats": {"window_k": st["nwv"], "initial_states": st["nstates"], "vertices_per_step": vertices},
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -478,8 +475,9 @@ def run_ours(args, ws, rank, local):
                                            cpu["states"], cpu["nstates_total"], cpu["vertices"], cpu["seconds"],
                                            cpu["setup_s"])},
             "fp64_dropin": {"value": fp64_value, "unit": UNIT, "ms_per_step": fst["ms_total"],
-                            "split_speedup": value / ws / fp64_value},
+                            "split_speedup": value / fp64_value},
             "error_vs_fp64": {"rates_max_rel": rate_err},
+            "error_vs_oracle": parity,
             "stage_ms": {"setup": st["ms_setup"], "stage_a": st["ms_stage_a"], "stage_bc": st["ms_stage_bc"],
                          "gemm_a": st["ms_gemm_a"], "gemm_b": st["ms_gemm_b"]},
             "wall_s": wall,
@@ -575,11 +573,15 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if ws > 1 and args.impl == "ours":
-        # one GPU per rank: each replica sees only its own device
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if ws > 1 or args.gpus > 1:
+        # one image, one GPU: no work on any rank, one line from rank 0
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "n_gpus": max(ws, args.gpus), "value": None,
+                              "unavailable": "one GPU per call: the path runs on one image and one GPU, and its "
+                                             "fused kernels use TMA multicast within one GPU's memory"}), flush=True)
+        return 0
     return run_ours(args, ws, rank, local)
 
 

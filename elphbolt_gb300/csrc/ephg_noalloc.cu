@@ -13,8 +13,11 @@
 // The array is part of the library image: every GPU that loads the library
 // holds its EPHG_NOALLOC_SCRATCH_BYTES until the process exits.  Host code may
 // not use the array's name as a device address (in host code it names a host
-// stand-in); its device address is obtained once per device with
-// cudaGetSymbolAddress, on the first call made with that device current.
+// stand-in); its device address comes from cudaGetSymbolAddress with the
+// handle's device current.  The first call on a device looks it up (set-up);
+// every later call made while the handle's stream is not capturing looks it up
+// again, so that a primary context re-created after cudaDeviceReset (by this
+// code or another library in the process) never sees a stale address.
 #include <mutex>
 
 #include "ephg_handle.cuh"
@@ -28,11 +31,13 @@ constexpr int MAX_DEVICES = 64;
 void *g_scratch_addr[MAX_DEVICES];   // device address of the array, per device
 std::mutex g_scratch_mu;
 
-// Set-up, once per device, with that device current.
-int scratch_address(int dev, unsigned char **out) {
+// The array's device address on device `dev` (current): looked up on the
+// first call and again on every call with `refresh` set (the stream is not
+// capturing), else the address of the last lookup.
+int scratch_address(int dev, bool refresh, unsigned char **out) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (dev < 0 || dev >= MAX_DEVICES) return ephg::api_fail(EPHG_ERR_CUDA, "el_wann_noalloc: device %d out of range", dev);
-  if (!g_scratch_addr[dev]) {
+  if (!g_scratch_addr[dev] || refresh) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
@@ -73,8 +78,11 @@ extern "C" int ephg_el_wann_noalloc(ephg_handle *h, int64_t nk, const double *kv
   int cur = -1;
   if (cudaGetDevice(&cur) != cudaSuccess || cur != h->device)
     return api_fail(EPHG_ERR_ARG, "el_wann_noalloc: the handle's device (%d) must be current (is %d)", h->device, cur);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->st, &cap) != cudaSuccess)
+    return api_fail(EPHG_ERR_CUDA, "el_wann_noalloc: cudaStreamIsCapturing failed");
   unsigned char *base = nullptr;
-  int rc = scratch_address(h->device, &base);
+  int rc = scratch_address(h->device, cap == cudaStreamCaptureStatusNone, &base);
   if (rc) return rc;
   // Every scratch region is written in full before it is read, so nothing has
   // to be cleared between calls.

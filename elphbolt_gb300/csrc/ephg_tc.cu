@@ -100,17 +100,23 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: gives up after ~2 s, records DERR_TIMEOUT and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+// Bounded wait: gives up after `limit` SM cycles, records DERR_TIMEOUT and
+// returns false.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, int *err, long long limit) {
   if (mbar_try(bar, parity)) return true;
   long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > WAIT_CYCLES) {
+    if (clock64() - t0 > limit) {
       atomicOr(err, DERR_TIMEOUT);
       return false;
     }
   }
   return true;
+}
+
+// The kernels' waits: ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+  return mbar_wait_limit(bar, parity, err, WAIT_CYCLES);
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0,
@@ -301,7 +307,8 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
   uint64_t *empty = full + STAGES;
   uint64_t *tfull = empty + STAGES;
   uint64_t *tempty = tfull + 2;
-  uint32_t *tslot = (uint32_t *)(tempty + 2);
+  uint64_t *drain = tempty + 2;
+  uint32_t *tslot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -313,6 +320,7 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 128);
     }
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -408,6 +416,11 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
         if (ok) umma_commit(&tfull[0]);   // accumulators ready for the epilogue
+      }
+      // a wait gave up: let the MMAs already issued retire before TMEM is freed
+      if (!ok) {
+        umma_commit(drain);
+        mbar_wait(drain, 0, err);
       }
     }
   } else {   // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4
@@ -1599,7 +1612,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   uint64_t *empty = full + F_STAGES;
   uint64_t *tfull = empty + F_STAGES;
   uint64_t *tempty = tfull + 1;
-  uint32_t *tslot = (uint32_t *)(tempty + 1);
+  uint64_t *drain = tempty + 1;
+  uint32_t *tslot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   // CTA pairs (clusters of 2) take m-tiles 2x, 2x + 1 of the same state pair:
@@ -1613,6 +1627,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, F_EPI_THREADS);
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -1696,6 +1711,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           if (++stage == F_STAGES) { stage = 0; phase ^= 1; }
         }
         if (ok) umma_commit(tfull);
+      }
+      // a wait gave up: let the MMAs already issued retire before TMEM is freed
+      if (!ok) {
+        umma_commit(drain);
+        mbar_wait(drain, 0, g.err);
       }
     }
   } else {   // ---- epilogue: warps 2..9
@@ -2005,7 +2025,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   uint64_t *empty = full + A_STAGES;
   uint64_t *tfull = empty + A_STAGES;
   uint64_t *tempty = tfull + 1;
-  uint32_t *tslot = (uint32_t *)(tempty + 1);
+  uint64_t *drain = tempty + 1;
+  uint32_t *tslot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   // CTA pairs (clusters of 2) take m-tiles 2x, 2x + 1 of the same n-tile: each
@@ -2019,6 +2040,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, F_EPI_THREADS);
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -2095,6 +2117,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           if (++stage == A_STAGES) { stage = 0; phase ^= 1; }
         }
         if (ok) umma_commit(tfull);
+      }
+      // a wait gave up: let the MMAs already issued retire before TMEM is freed
+      if (!ok) {
+        umma_commit(drain);
+        mbar_wait(drain, 0, g.err);
       }
     }
   } else {   // ---- epilogue: warps 2..9
@@ -2618,8 +2645,67 @@ __global__ void k_join(int64_t M, int64_t N, const float *Cr, const float *Ci, i
   int64_t r = idx / N, c = idx % N;
   C[idx] = make_double2(Cr[r * ldc + c], Ci[r * ldc + c]);
 }
+
+// The give-up path of the tcgen05 kernels' bounded waits, run on its own: one
+// CTA of 64 threads.  Warp 1 allocates TMEM as the kernels do; warp 0 lane 0
+// waits `limit` cycles on a barrier that no thread arrives on (or, with
+// `arrive`, on one it has arrived on itself, which ends at once).  When the
+// wait gives up it records DERR_TIMEOUT and, as an MMA issuer whose wait gave
+// up, commits to its drain barrier and waits for it (no MMA was issued, so the
+// commit arrives at once); then the CTA frees TMEM and returns.  No TMA load
+// and no MMA is issued.
+__global__ void __launch_bounds__(64) k_wait_probe(long long limit, int arrive, int *err) {
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)),
+                 "r"(32)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (warp == 0 && lane == 0) {
+    if (arrive) mbar_arrive(&bars[0]);
+    if (!mbar_wait_limit(&bars[0], 0, err, limit)) {
+      umma_commit(&bars[1]);
+      mbar_wait_limit(&bars[1], 0, err, WAIT_CYCLES);
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32) : "memory");
+  }
+}
 }  // namespace tc
 }  // namespace ephg
+
+extern "C" int ephg_debug_wait_timeout(int64_t limit_cycles, int64_t arrive, int *device_err) {
+  using namespace ephg;
+  using namespace ephg::tc;
+  if (limit_cycles < 0 || limit_cycles > WAIT_CYCLES) return tfail(1, "debug_wait_timeout: limit out of range");
+  int *err = nullptr;
+  if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return tfail(2, "debug_wait_timeout: cudaMalloc failed");
+  int rc = 0, herr = 0;
+  cudaMemset(err, 0, sizeof(int));
+  k_wait_probe<<<1, 64>>>((long long)limit_cycles, arrive ? 1 : 0, err);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (device_err) *device_err = herr;
+  if (e != cudaSuccess) rc = tfail(2, cudaGetErrorString(e));
+  else if (herr & DERR_TIMEOUT) rc = tfail(7, "debug_wait_timeout: bounded wait gave up");
+  return rc;
+}
 
 extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A, const double *B, double *C) {
   using namespace ephg;

@@ -192,8 +192,23 @@ def _write_stream(path, count, *arrays):
             np.ascontiguousarray(a, dtype=dt).tofile(f)
 
 
-def write_gk2_istate(dirpath, istate, g2):
-    _write_stream(os.path.join(dirpath, "gk2.istate%d" % istate), len(g2), (g2, np.float64))
+def write_gk2_istate(dirpath, istate, g2, g2_istate=None):
+    """gk2.istate<n> as the ibzk 'g' pass writes it (interactions.f90:2337-2348):
+    int64 count, then the whole g2_istate buffer -- not 1:count.  The buffer is
+    allocated once per image with nprocs = nstates_inwindow * numbranches
+    entries and zeroed once (:2146-2148); each state overwrites 1:count, so
+    entries past count keep an earlier state's values.  ``g2_istate``, if given,
+    is that running buffer (updated in place); otherwise the file holds count
+    values.  With q on the k mesh (mesh_ref = 1) every window k' is a final
+    state of every initial state, so count = nprocs and both agree."""
+    g2 = np.asarray(g2, dtype=np.float64)
+    if g2_istate is None:
+        _write_stream(os.path.join(dirpath, "gk2.istate%d" % istate), len(g2), (g2, np.float64))
+        return
+    if len(g2) > len(g2_istate):
+        raise ValueError("count %d exceeds the g2_istate buffer (%d)" % (len(g2), len(g2_istate)))
+    g2_istate[:len(g2)] = g2
+    _write_stream(os.path.join(dirpath, "gk2.istate%d" % istate), len(g2), (g2_istate, np.float64))
 
 
 def write_gq2_istate(dirpath, istate, g2):
@@ -246,6 +261,7 @@ def dump_el_side(wann, req, g2dir, xdir, precision=None):
     ikp, n = np.nonzero(win)                                    # final states (window k', band), in order
     os.makedirs(g2dir, exist_ok=True)
     os.makedirs(xdir, exist_ok=True)
+    g2_istate = np.zeros(nin * nb)                             # nprocs = nstates_inwindow * numbranches
     j = 0
     for ik in range(len(idx)):
         for m in range(nw):
@@ -257,7 +273,7 @@ def dump_el_side(wann, req, g2dir, xdir, precision=None):
             iq = dq[:, 0] + mesh[0] * (dq[:, 1] + mesh[1] * dq[:, 2]) + 1
             ist_el = np.repeat(ikp * nw + n + 1, nb)
             ist_ph = ((np.repeat(iq, nb) - 1) * nb + np.tile(np.arange(1, nb + 1), len(iq)))
-            write_gk2_istate(g2dir, istate, out["g2"][sl])
+            write_gk2_istate(g2dir, istate, out["g2"][sl], g2_istate)
             write_X_istate(xdir, istate, out["xp"][sl], out["xm"][sl], ist_el, ist_ph)
             j += 1
     return out

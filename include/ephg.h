@@ -2,9 +2,9 @@
  * ephg.h - C ABI of the GB300 (sm_103a) e-ph vertex library.
  *
  * Drop-in for elphbolt's Wannier-interpolation procedures and the electron-
- * and phonon-side e-ph rate drivers, callable from Fortran through ISO_C_BINDING (see
- * INTEGRATION.md for the bind(C) interfaces).  Every entry point names the
- * reference procedure it replaces.
+ * and phonon-side e-ph rate drivers, callable from Fortran through ISO_C_BINDING
+ * (the bind(C) interfaces are in include/wannier_gpu.f90).  Every entry point names
+ * the reference procedure it replaces.
  *
  * Conventions
  *  - Arrays are caller-owned, Fortran column-major, with the reference's
@@ -315,10 +315,14 @@ int ephg_el_rates_batch(int64_t n, ephg_handle *const *crystals, const ephg_rate
  * scratch is one fixed array of EPHG_NOALLOC_SCRATCH_BYTES inside the library
  * (every GPU that loads the library holds it until exit); requests that need
  * more are refused with EPHG_ERR_ARG and the largest nk that fits in the
- * message.  The first call on a device resolves the array's address (set-up,
- * once per device), so make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race.  The handle's device must be
- * current; the call returns after the handle's stream has finished. */
+ * message.  The first call on a device resolves the array's address (set-up),
+ * so make it before any stream capture; later calls outside a capture resolve
+ * it again (a re-created context is picked up).  All calls share the array:
+ * calls that overlap on the GPU race.  The handle's device must be current.
+ * The kernels run on the handle's own stream, which does not wait for other
+ * streams: kvecs must be complete before the call (synchronise the stream or
+ * OpenACC queue that wrote it), and the call returns after the handle's stream
+ * has finished, so energies and evecs are complete on return. */
 #define EPHG_NOALLOC_SCRATCH_BYTES (16ull << 20)
 int ephg_el_wann_noalloc(ephg_handle *h, int64_t nk, const double *kvecs, double *energies,
                          double *evecs);

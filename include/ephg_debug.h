@@ -22,6 +22,16 @@ int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A, const dou
 /* message of the last failure of the hook */
 const char *ephg_debug_last_error(void);
 
+/* The give-up path of the tcgen05 kernels' bounded barrier waits, on its own:
+ * one CTA allocates TMEM, waits limit_cycles (0 .. ~4e9 SM cycles) on a
+ * barrier that nothing arrives on (arrive != 0: one it arrived on itself),
+ * records the timeout in its error word, drains its (empty) MMA queue, frees
+ * TMEM and returns; no TMA load or MMA is issued.  *device_err (nullable)
+ * receives the error word.  Returns EPHG_ERR_TIMEOUT when the wait gave up --
+ * what every kernel entry point returns when one of its waits does -- and
+ * EPHG_OK when it did not; the CUDA context stays usable either way. */
+int ephg_debug_wait_timeout(int64_t limit_cycles, int64_t arrive, int *device_err);
+
 /* The serving loop's slots, queue, admission, GPU hand-over and statistics run
  * against a simulated executor (no GPU): two crystals of 1000 resident bytes
  * each; request i for crystal i % 2 with a cubic mesh meshes[i] needs

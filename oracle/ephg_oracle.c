@@ -274,8 +274,10 @@ void or_el_wann(const or_wannier *w, int64_t nk, const double *kvecs, double *en
   free(H); free(dH); free(V); free(ev);
 }
 
-/* ws_wrapping_vectors: wannier.f90:532-582.  Returns the number of wrappers
- * (the second-pass count; see the quirk note in the design doc). */
+/* ws_wrapping_vectors: wannier.f90:532-582.  Returns the number of wrappers.
+ * The reference counts them in a first pass and fills them in a second; with
+ * distances within 2 eps of each other the two counts can differ, and this
+ * restatement returns the second-pass count. */
 int or_ws_wrapping_vectors(const double lvec[9], const double vl[3], double eps,
                            int64_t *wrappers, int maxw) {
   int64_t iv0[3];

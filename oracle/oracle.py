@@ -38,7 +38,8 @@ class OrRequest(ct.Structure):
                 ("sigma", ct.c_double)]
 
 
-_REF_ROOT = "/root/reference"
+# the elphbolt source tree (read only, for its vendored spglib): ELPHBOLT_REFERENCE
+_REF_ROOT = os.environ.get("ELPHBOLT_REFERENCE", "/root/reference")
 _SPGLIB = os.path.join(_HERE, "_ref", "libspglib_ref.so")
 
 

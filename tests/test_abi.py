@@ -73,3 +73,45 @@ def test_batch_refuses_bad_arguments(lib):
     # null crystal handles
     assert lib.ephg_el_rates_batch(n, H, R, RP, IP, None, st, None, None) == _lib.EPHG_ERR_ARG
     assert b"null crystal" in lib.ephg_last_error()
+
+
+def test_debug_header_symbols_exported(lib):
+    txt = open(os.path.join(ROOT, "include", "ephg_debug.h")).read()
+    syms = sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(ephg_debug_\w+)\s*\(", txt, re.M)))
+    assert "ephg_debug_wait_timeout" in syms
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_fortran_binding_covers_the_header():
+    """include/wannier_gpu.f90 has a bind(C) interface for every entry point of
+    include/ephg.h, and its bind(C) types have the C structs' fields in order."""
+    f90 = open(os.path.join(ROOT, "include", "wannier_gpu.f90")).read()
+    bound = set(re.findall(r'bind\(C,\s*name="(ephg_\w+)"\)', f90))
+    assert set(header_symbols()) <= bound, set(header_symbols()) - bound
+    hdr = open(os.path.join(ROOT, "include", "ephg.h")).read()
+
+    def c_fields(name):
+        body = re.search(r"typedef struct \{([^{}]*)\}\s*%s;" % name, hdr).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        out = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            names = decl.split(None, 1)[1] if not decl.startswith("const") else decl.split(None, 2)[2]
+            for n in names.split(","):
+                out.append(re.sub(r"[\s*]|\[.*\]", "", n))
+        return out
+
+    def f_fields(name):
+        body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type" % name, f90, re.S).group(1)
+        out = []
+        for line in body.replace("&\n", " ").splitlines():
+            if "::" in line:
+                out += [re.sub(r"\(.*\)", "", n).strip() for n in line.split("::")[1].split(",")]
+        return out
+
+    for t in ("ephg_wannier_desc", "ephg_rate_request", "ephg_rate_stats", "ephg_batch_opts", "ephg_batch_stats",
+              "ephg_server_stats"):
+        assert c_fields(t) == f_fields(t), t

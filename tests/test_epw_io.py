@@ -103,6 +103,23 @@ def test_stream_files_byte_layout(tmp_path):
     assert list(E.read_istate(str(tmp_path / "Y.istate2"), with_indices=True)[3]) == [3, 2, 1]
 
 
+def test_gk2_istate_writes_the_whole_buffer(tmp_path):
+    """The ibzk 'g' pass writes count and then all of g2_istate(nprocs)
+    (interactions.f90:2343-2348): entries past count keep the values an earlier
+    state left (the buffer is zeroed once, :2146-2148); readers take count."""
+    buf = np.zeros(5)
+    E.write_gk2_istate(str(tmp_path), 1, [1.0, 2.0, 3.0, 4.0], buf)
+    E.write_gk2_istate(str(tmp_path), 2, [9.0, 8.0], buf)
+    raw = (tmp_path / "gk2.istate2").read_bytes()
+    assert len(raw) == 8 + 5 * 8
+    assert np.frombuffer(raw[:8], dtype=np.int64)[0] == 2
+    assert np.array_equal(np.frombuffer(raw[8:], dtype=np.float64), [9.0, 8.0, 3.0, 4.0, 0.0])
+    n, v = E.read_istate(str(tmp_path / "gk2.istate2"))
+    assert n == 2 and list(v) == [9.0, 8.0]
+    with pytest.raises(ValueError):
+        E.write_gk2_istate(str(tmp_path), 3, np.ones(6), buf)
+
+
 @pytest.mark.gpu
 def test_dumped_files_give_the_rates(tmp_path, oracle_lib):
     """The library's vertex lists written as gk2 / X / gq2 / Y files; summed back
@@ -120,6 +137,8 @@ def test_dumped_files_give_the_rates(tmp_path, oracle_lib):
         n, _, ist_el, ist_ph = E.read_istate(str(tmp_path / "X" / os.listdir(tmp_path / "X")[0]), with_indices=True)
         nin = out["stats"]["nstates_inwindow"]
         assert n == nin * wd.numbranches
+        raw = (tmp_path / "g2" / "gk2.istate1").read_bytes()
+        assert len(raw) == 8 + 8 * nin * wd.numbranches      # count, then g2_istate(nprocs)
         assert ist_el.min() >= 1 and ist_el.max() <= out["nwv"] * wd.numwannbands
         assert ist_ph.min() >= 1 and ist_ph.max() <= np.prod(req.mesh) * wd.numbranches
         rph = E.dump_ph_side(W, req, str(tmp_path / "gq2"), str(tmp_path / "Y"))
