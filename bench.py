@@ -126,6 +126,32 @@ def peaks():
     return 1900.0, 6800.0, "fallback"
 
 
+def tf32_cublas_tflops(n=8192, reps=10):
+    """Dense TF32 tensor throughput of this GPU, measured live: cuBLAS SGEMM with
+    TF32 tensor ops (torch.matmul, allow_tf32), n^3, best of `reps` (CUDA events)."""
+    import torch
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(3):
+            torch.matmul(a, b)
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
 def traffic_per_gflop():
     """DRAM bytes per algorithmic GFLOP of the fused stage-B kernel, from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "stageB_fused86_traffic.json")
@@ -289,6 +315,52 @@ def symmetry_side(steps):
             "what": "ephg_set_symmetry + ephg_el_rates: initial states on the irreducible window points"}
 
 
+def large_side():
+    """The large single instance: a 6-atom fcc cell (masses U[12, 60] amu),
+    nw 32, nb 18, 279 Re / 279 Rp Wigner-Seitz cells (g(Re,Rp) 23 GB complex128,
+    resident), a 40^3 k = q mesh, window +-0.1 eV about mid-gap + 0.6 eV,
+    Gaussian 10 meV, 300 K, split form.  One warm-up request (operand planes),
+    one timed; the rates of a sample of initial states against the CPU oracle
+    (FP64, restructured form, full k' sums)."""
+    import numpy as np
+    from elphbolt_gb300 import _lib, synthetic as S
+    from elphbolt_gb300.wannier import Wannier
+    from oracle import oracle as O
+    t0 = time.time()
+    wd = S.large_instance()
+    req = S.si_like_request(wd, (40, 40, 40), window=0.1)
+    t_gen = time.time() - t0
+    t1 = time.time()
+    W = Wannier(wd)
+    t_create = time.time() - t1
+    try:
+        W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+        out = W.el_rates(req, precision=_lib.PREC_SPLIT_TF32)
+    finally:
+        W.deallocate_wannier()
+    st = out["stats"]
+    ncores = os.cpu_count() or 1
+    t2 = time.time()
+    R = O.RatesRun(O.Wannier(wd), req, nthreads=ncores)
+    t_oset = time.time() - t2
+    a = R.run(0, 6, literal=False)
+    R.close()
+    ref = a["rates"]
+    m = ref > 0
+    err = float(np.max(np.abs(out["rates"][m] - ref[m]) / ref[m])) if m.any() else None
+    same = bool(np.array_equal(a["indexlist"], out["indexlist"]))
+    return {"workload": "6-atom fcc, nw 32, nb 18, %d Re / %d Rp WS cells (6^3; g 23 GB c128), 40^3 k=q mesh, "
+                        "window +-0.1 eV at mid-gap+0.6 eV, Gaussian 10 meV, 300 K" % (wd.nwsk, wd.nwsq),
+            "value": st["vertices"] / (st["ms_total"] * 1e-3), "unit": UNIT, "ms_per_step": st["ms_total"],
+            "vertices": st["vertices"], "window_k": st["nwv"], "initial_states": st["nstates"],
+            "stage_ms": {"setup": st["ms_setup"], "stage_a": st["ms_stage_a"], "stage_bc": st["ms_stage_bc"]},
+            "contraction_tflops": (st["stage_a_gflop"] + st["stage_b_gflop"]) / st["ms_total"],
+            "rates_max_rel_vs_oracle": err, "oracle_states": int(m.sum()), "window_lists_equal": same,
+            "oracle_setup_s": t_oset, "generation_s": t_gen, "create_s": t_create,
+            "what": "ephg_el_rates, split form (generic nw / nb path); error vs the CPU oracle on the first "
+                    "initial states (full k' sums)"}
+
+
 def batched_side(steps):
     """The batched form (ephg_el_rates_batch): 64 requests on 8 random crystals
     (nw 8-24, nb 6-18, WS sets of 93-279 vectors; meshes 8^3-16^3, windows
@@ -439,6 +511,11 @@ def run_ours(args, ws, rank, local):
     bf16, hbm, src = peaks()
     achieved = st["stage_b_gflop"] / (st["ms_gemm_b"] * 1e-3) / 1e3          # TFLOP/s algorithmic
     peak = bf16 / 2.0 / 3.0       # TF32 = 1/2 of BF16 dense; three TF32 products per FP32-accurate one
+    try:
+        tf32 = tf32_cublas_tflops()
+    except Exception:
+        tf32 = None
+    clk = clk.summary()
     tpg = traffic_per_gflop()
     cpu = cpu_sample(wd, req)
     parity = error_vs_oracle(cpu, out["indexlist"], {"split": split_rates, "fp64": ref})
@@ -468,7 +545,11 @@ def run_ours(args, ws, rank, local):
                          "kernel": "k_stageB_fused86 (stage B Rp Fourier on tcgen05 + rate epilogue)",
                          "peak_source": "%s bf16 %.1f TFLOP/s / 2 (TF32) / 3 (split), of %s" % (src, bf16, src),
                          "launches_per_step": st["gemm_b_launches"],
-                         "ms_per_launch": st["ms_gemm_b"] / max(1, st["gemm_b_launches"])},
+                         "ms_per_launch": st["ms_gemm_b"] / max(1, st["gemm_b_launches"]),
+                         "mcycles_per_launch": (st["ms_gemm_b"] / max(1, st["gemm_b_launches"]) * clk["sm_mhz"] * 1e-3
+                                                if clk.get("sm_mhz") else None),
+                         "tf32_cublas_tflops_measured": tf32,
+                         "frac_of_measured_tf32_over_3": (achieved / (tf32 / 3.0)) if tf32 else None},
             "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
                              "sample": "%d initial states of %d, %d vertices in %.1f s (literal per-vertex g2, "
                                        "OpenMP over k'); set-up %.1f s excluded" % (
@@ -481,7 +562,7 @@ def run_ours(args, ws, rank, local):
             "stage_ms": {"setup": st["ms_setup"], "stage_a": st["ms_stage_a"], "stage_bc": st["ms_stage_bc"],
                          "gemm_a": st["ms_gemm_a"], "gemm_b": st["ms_gemm_b"]},
             "wall_s": wall,
-            "clocks": clk.summary()}
+            "clocks": clk}
     line["phonon_side"] = ph
     if not args.no_polar:
         try:
@@ -498,6 +579,11 @@ def run_ours(args, ws, rank, local):
             line["batched"] = batched_side(args.steps)
         except Exception as e:   # the main line is still printed
             line["batched"] = {"error": repr(e)}
+    if not args.no_large:
+        try:
+            line["large"] = large_side()
+        except Exception as e:   # the main line is still printed
+            line["large"] = {"error": repr(e)}
     if serving is not None:
         line["serving"] = serving
     print(json.dumps(line), flush=True)
@@ -571,6 +657,7 @@ def main():
     ap.add_argument("--no-polar", action="store_true", help="skip the polar-crystal measurement")
     ap.add_argument("--no-symmetry", action="store_true", help="skip the crystal-symmetry measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-instance (nw 32, nb 18, 40^3) measurement")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

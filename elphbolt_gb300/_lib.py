@@ -34,9 +34,11 @@ EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count"
            "ephg_ph_wann", "ephg_gkRp", "ephg_gReq", "ephg_g2", "ephg_kq_index", "ephg_el_rates",
            "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
            "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates", "ephg_set_polar",
-           "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge", "ephg_el_rates_batch"]
+           "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge", "ephg_el_rates_batch",
+           "ephg_g2_average_degenerate"]
 
 TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
+DEGAVG_REFERENCE, DEGAVG_MEAN = 0, 1
 
 
 class EphgError(RuntimeError):
@@ -127,6 +129,7 @@ def load(path: str = LIB_PATH):
     L.ephg_ph_rates.argtypes = [vp, ct.POINTER(RateRequest), ct.c_int64, c_dp, c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, ct.c_int64]
     L.ephg_set_polar.argtypes = [vp, c_dp, c_dp]
+    L.ephg_g2_average_degenerate.argtypes = [vp, ct.POINTER(RateRequest), ct.c_int64, ct.c_double, ct.c_int64, c_dp]
     L.ephg_crystal_symmetry.argtypes = [c_dp, ct.c_int64, c_dp, c_i64p, ct.c_double, ct.c_int64, c_i64p, c_i64p,
                                         c_dp]
     L.ephg_set_symmetry.argtypes = [vp, ct.c_int64, c_i64p]

@@ -817,8 +817,8 @@ static int check_err_view(const ExecView &x) {
 
 int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
                         int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus,
-                        int64_t cap, const PhOut *ph) {
-  if (!h || !req || (!ph && (!rates || !indexlist)) || (ph && !ph->rates_phe))
+                        int64_t cap, const PhOut *ph, const DegAvgReq *avg) {
+  if (!h || !req || (!ph && !avg && (!rates || !indexlist)) || (ph && !ph->rates_phe) || (avg && (ph || !avg->g2)))
     return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   for (int i = 0; i < 3; ++i)
     if (req->mesh[i] <= 0) return fail(EPHG_ERR_ARG, "el_rates: bad mesh");
@@ -1009,6 +1009,37 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   for (int j = nst - 1; j >= 0; --j) first_state[code_h[j] / nw] = j;
   for (int i = nA - 1; i >= 0; --i)
     if (first_state[i] > first_state[i + 1]) first_state[i] = first_state[i + 1];
+  if (avg) {   // degenerate-subspace averaging of the caller's vertex list, no contraction
+    const int64_t per = (int64_t)nin * nb, vtot = (int64_t)nst * per;
+    if (avg->nv != vtot)
+      return fail(EPHG_ERR_ARG, "g2_average_degenerate: the list has %lld entries, the request's vertex list %lld",
+                  (long long)avg->nv, (long long)vtot);
+    double *g2d;
+    int *fsd;
+    if ((rc = wsget((*x.ws), "r_vg2", (size_t)vtot, &g2d)) || (rc = wsget((*x.ws), "r_fsd", (size_t)nA + 1, &fsd)))
+      return WSFAILX(rc);
+    CK(cudaMemcpyAsync(g2d, avg->g2, (size_t)vtot * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(fsd, first_state.data(), (size_t)(nA + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (launch_degenerate_average(g2d, per, nin, st_code, arow, widx, cum, fsd, ens, om, nst, nA, nwv, nw, nb, mesh,
+                                  req->enref, req->fsthick, avg->thres, avg->mode, st))
+      return fail(EPHG_ERR_ARG, "g2_average_degenerate: nw and nb must be <= 64");
+    (*x.launches) += 3;
+    CKL();
+    CK(cudaMemcpyAsync(avg->g2, g2d, (size_t)vtot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (indexlist)
+      for (int i = 0; i < nA; ++i) indexlist[i] = (int64_t)arow_h[i] + 1;
+    if ((rc = check_err_view(x))) return rc;
+    if (stats) {
+      memset(stats, 0, sizeof *stats);
+      stats->nwv = nA;
+      stats->nstates_inwindow = nin;
+      stats->nstates = nst;
+      stats->vertices = vtot;
+      stats->pairs = (int64_t)nst * nwv;
+    }
+    return EPHG_OK;
+  }
   CK(cudaEventRecord(ev.e[1], st));
   x.yield();   // serving: hand the GPU to a smaller request before the contractions
   // ---- stage A: g(k,Rp) for window k, rotation over m, k-half of the Rp phase ----
@@ -1162,6 +1193,16 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   if (!h) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
   return el_rates_view(h, x, req, rates, indexlist, stats, g2, xplus, xminus, cap);
+}
+
+extern "C" int ephg_g2_average_degenerate(ephg_handle *h, const ephg_rate_request *req, int64_t mode, double thres,
+                                          int64_t nv, double *g2) {
+  if (!h || !req || !g2 || nv < 0) return fail(EPHG_ERR_ARG, "g2_average_degenerate: bad arguments");
+  if (mode != EPHG_DEGAVG_REFERENCE && mode != EPHG_DEGAVG_MEAN)
+    return fail(EPHG_ERR_ARG, "g2_average_degenerate: bad mode");
+  const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
+  const DegAvgReq avg{g2, nv, (int)mode, thres > 0 ? thres : 1.0e-6};
+  return el_rates_view(h, x, req, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr, &avg);
 }
 
 extern "C" int ephg_ph_rates(ephg_handle *h, const ephg_rate_request *req, int64_t spindeg, double *rates_phe,

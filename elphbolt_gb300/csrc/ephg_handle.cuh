@@ -72,11 +72,20 @@ struct PhOut {
   double *y;
   double spindeg;
 };
+// A caller's |g|^2 vertex list to average over degenerate subspaces
+// (ephg_g2_average_degenerate) instead of running the contractions.
+struct DegAvgReq {
+  double *g2;
+  int64_t nv;
+  int mode;
+  double thres;
+};
 // ph == nullptr: the electron side only (ephg_el_rates); otherwise rates and
-// indexlist may be NULL.
+// indexlist may be NULL.  avg != nullptr: the request's set-up only, then the
+// averaging of avg->g2 (rates and indexlist may be NULL).
 int el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus, int64_t cap,
-                  const PhOut *ph = nullptr);
+                  const PhOut *ph = nullptr, const DegAvgReq *avg = nullptr);
 // record a failure message for ephg_last_error() and return code
 int api_fail(int code, const char *fmt, ...);
 // read, clear and translate the handle's device error word

@@ -1046,4 +1046,117 @@ void launch_rate_final(int nst, int nblk, const double *partial, const int *st_c
   k_rate_final<<<(nst + 127) / 128, 128, 0, st>>>(nst, nblk, partial, st_code, nw, N, rates_f);
 }
 
+// ------------------------------------------ degenerate-subspace averaging
+// The gauge fixing of plot_along_path (wannier.f90:1332-1384, the same loops
+// in test/check_interactions_symmetries.f90:330-384) on a |g|^2 vertex list in
+// the electron side's order (state j, final state f = (k', n), branch s),
+// FP64.  Three passes in the reference's order, each over groups of one index
+// with the others fixed: branches s of q = k' - k (phonon energies), initial
+// bands m of each k, final bands n of each k' (electron energies); a member's
+// partners are those with |E - E'| < thres.  Mode 0 restates the reference's
+// loops literally, in place: member a becomes the mean, summed in member
+// order, of its partners' values as they are at that moment (so a later member
+// sees its predecessors' new values); mode 1 takes every mean from the values
+// before the pass.  One thread per group set; groups of a pass are disjoint.
+constexpr int DEG_MAXG = 64;
+
+__device__ void deg_group(int mode, double thres, int c, double *v, int64_t st, const double *e) {
+  double tmp[DEG_MAXG];
+  if (mode == 1)
+    for (int a = 0; a < c; ++a) tmp[a] = v[a * st];
+  for (int a = 0; a < c; ++a) {
+    int cnt = 0;
+    double aux = 0.0;
+    for (int b = 0; b < c; ++b)
+      if (fabs(e[a] - e[b]) < thres) {
+        ++cnt;
+        aux += mode == 0 ? v[b * st] : tmp[b];
+      }
+    v[a * st] = aux / (double)cnt;
+  }
+}
+
+// window bands of mesh point p in band order: their count, bands in `band`
+__device__ __forceinline__ int window_bands(const double *ens, int p, int nw, double enref, double fsthick, int *band,
+                                            double *e) {
+  int c = 0;
+  for (int n = 0; n < nw; ++n) {
+    const double x = ens[(size_t)p * nw + n];
+    if (fabs(x - enref) <= fsthick) {
+      band[c] = n;
+      e[c] = x;
+      ++c;
+    }
+  }
+  return c;
+}
+
+struct DegList {
+  double *g2;
+  const int *st_code, *arow, *widx, *cum, *first_state;
+  const double *ens, *om;
+  int nst, nA, nwv, nw, nb, mesh[3];
+  int64_t per;          // entries per state: nin * nb
+  double enref, fsthick, thres;
+  int mode;
+};
+
+// pass 1: branches, per (state, k' row)
+__global__ void k_deg_branches(DegList L) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)L.nst * L.nwv) return;
+  const int j = (int)(t / L.nwv), b = (int)(t % L.nwv);
+  const int p = L.arow[L.st_code[j] / L.nw], pp = L.widx[b];
+  const int a1 = p % L.mesh[0], a2 = (p / L.mesh[0]) % L.mesh[1], a3 = p / (L.mesh[0] * L.mesh[1]);
+  const int b1 = pp % L.mesh[0], b2 = (pp / L.mesh[0]) % L.mesh[1], b3 = pp / (L.mesh[0] * L.mesh[1]);
+  const int q = (int)(floormod(b1 - a1, L.mesh[0]) +
+                      L.mesh[0] * (floormod(b2 - a2, L.mesh[1]) + L.mesh[1] * floormod(b3 - a3, L.mesh[2])));
+  double e[DEG_MAXG];
+  for (int s = 0; s < L.nb; ++s) e[s] = L.om[(size_t)q * L.nb + s];
+  const int nf = L.cum[b + 1] - L.cum[b];
+  for (int r = 0; r < nf; ++r)
+    deg_group(L.mode, L.thres, L.nb, L.g2 + (int64_t)j * L.per + (int64_t)(L.cum[b] + r) * L.nb, 1, e);
+}
+
+// pass 2: initial bands, per (initial k row, final state); the states of one
+// k row are consecutive, in band order
+__global__ void k_deg_initial(DegList L, int nin) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)L.nA * nin) return;
+  const int a = (int)(t / nin), f = (int)(t % nin);
+  const int j0 = L.first_state[a], c = L.first_state[a + 1] - j0;
+  if (c <= 0) return;
+  const int p = L.arow[a];
+  double e[DEG_MAXG];
+  for (int i = 0; i < c; ++i) e[i] = L.ens[(size_t)p * L.nw + L.st_code[j0 + i] % L.nw];
+  for (int s = 0; s < L.nb; ++s)
+    deg_group(L.mode, L.thres, c, L.g2 + (int64_t)j0 * L.per + (int64_t)f * L.nb + s, L.per, e);
+}
+
+// pass 3: final bands, per (state, k' row)
+__global__ void k_deg_final(DegList L) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)L.nst * L.nwv) return;
+  const int j = (int)(t / L.nwv), b = (int)(t % L.nwv);
+  int band[DEG_MAXG];
+  double e[DEG_MAXG];
+  const int c = window_bands(L.ens, L.widx[b], L.nw, L.enref, L.fsthick, band, e);
+  for (int s = 0; s < L.nb; ++s)
+    deg_group(L.mode, L.thres, c, L.g2 + (int64_t)j * L.per + (int64_t)L.cum[b] * L.nb + s, L.nb, e);
+}
+
+int launch_degenerate_average(double *g2, int64_t per, int nin, const int *st_code, const int *arow, const int *widx,
+                              const int *cum, const int *first_state, const double *ens, const double *om, int nst,
+                              int nA, int nwv, int nw, int nb, const int mesh[3], double enref, double fsthick,
+                              double thres, int mode, cudaStream_t st) {
+  if (nw > DEG_MAXG || nb > DEG_MAXG) return 1;
+  DegList L{g2, st_code, arow, widx, cum, first_state, ens, om, nst, nA, nwv, nw, nb, {mesh[0], mesh[1], mesh[2]},
+            per, enref, fsthick, thres, mode};
+  const int64_t n1 = (int64_t)nst * nwv, n2 = (int64_t)nA * nin;
+  if (n1 > 0) k_deg_branches<<<(unsigned)((n1 + 127) / 128), 128, 0, st>>>(L);
+  if (n2 > 0) k_deg_initial<<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(L, nin);
+  if (n1 > 0) k_deg_final<<<(unsigned)((n1 + 127) / 128), 128, 0, st>>>(L);
+  return 0;
+}
+
 }  // namespace ephg

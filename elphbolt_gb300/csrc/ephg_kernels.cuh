@@ -159,5 +159,10 @@ void launch_epilogue_fp32(int nwv, int j0, int j1, const float *Cr, const float 
 void launch_bose(int N, int nb, const double *om, double T, double *bose, cudaStream_t st);
 void launch_rate_final(int nst, int nblk, const double *partial, const int *st_code, int nw,
                        int N, double *rates_f, cudaStream_t st);
+// degenerate-subspace averaging of a vertex list (3 launches); 1 if nw or nb > 64
+int launch_degenerate_average(double *g2, int64_t per, int nin, const int *st_code, const int *arow, const int *widx,
+                              const int *cum, const int *first_state, const double *ens, const double *om, int nst,
+                              int nA, int nwv, int nw, int nb, const int mesh[3], double enref, double fsthick,
+                              double thres, int mode, cudaStream_t st);
 
 }  // namespace ephg

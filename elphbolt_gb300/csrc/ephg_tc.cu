@@ -976,20 +976,9 @@ __global__ void k_kinv(int n, const int *kpos, int *kinv) {
 struct QTab {
   const float *cx;     // [q][s]: const_tp * g2unitfactor / (2 omega) if omega >= 0.5 meV else 0
   const float *bose;   // [q][s]
-  const float *w;      // [q][s]: omega / sigma
-  const float *v;      // [q][s]: omega / kT
+  const float4 *wv;    // [q][s]: omega / sigma as a double-float, e^(omega / kT) (wv_pack)
 };
 
-__global__ void k_qtab(int n, const double *om, const double *bose, double sigma, double kT, double const_tp,
-                       float *cx, float *bs, float *w, float *v) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double o = om[i];
-  cx[i] = (o >= 0.5e-3) ? (float)(const_tp * 0.5 * g2unitfactor / o) : 0.0f;
-  bs[i] = (float)bose[i];
-  w[i] = (float)(o / sigma);
-  v[i] = (float)(o / kT);
-}
 
 __global__ void k_to_f2(int64_t n, const double2 *a, float2 *b) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1019,6 +1008,97 @@ __device__ __forceinline__ float y_factor(const YOcc &o, float bose) {
   return o.f1 * ib / (1.0f + o.emx * (bose * ib));
 }
 
+// ---- occupation and delta factors of one vertex, split epilogues ----
+// The exponents of the Gaussian and of the Fermi factors reach tens to hundreds
+// in the tails, where an FP32 argument's rounding (6e-8 relative) becomes a
+// relative error of the exponential as large as the argument times 6e-8.  So
+// every argument is carried as a double-float (hi + lo, |lo| <= ulp(hi) / 2,
+// Dekker / Knuth error-free transformations), the exponential is taken of the
+// hi part with the accurate expf and corrected by (1 + lo); the result is
+// then accurate to a few FP32 ulps whatever the argument.
+struct F2 {
+  float hi, lo;
+};
+__host__ __device__ __forceinline__ F2 f2_of(double x) {
+  const float h = (float)x;
+  return F2{h, (float)(x - (double)h)};
+}
+// a + b exactly as hi + lo (Knuth's two-sum)
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return F2{s, e};
+}
+// (a + b) for double-floats, to about 2^-44 relative
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  F2 s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return s;
+}
+// t^2 / 2 for a double-float t (the hi product's rounding error by FMA)
+__device__ __forceinline__ F2 f2_half_sq(F2 t) {
+  const float p = __fmul_rn(t.hi, t.hi);
+  const float e = __fmaf_rn(t.hi, t.hi, -p);
+  return F2{0.5f * p, 0.5f * __fmaf_rn(2.0f * t.hi, t.lo, e)};
+}
+// e^(hi + lo)
+__device__ __forceinline__ float f2_exp(F2 a) { return expf(a.hi) * (1.0f + a.lo); }
+
+// The phonon side's Gaussian factors are formed scaled by 2^64
+// (e^(64 ln 2 - t^2/2)), so that its sums keep the tails down to e^-131 in
+// FP32's range; the electron side's X+- use unscaled ones.
+constexpr float LN2X64_HI = 44.361419677734375f, LN2X64_LO = -1.2189786957605975e-07f;
+constexpr float TWO_M64 = 5.421010862427522e-20f;   // 2^-64, exact
+constexpr double TWO_M64D = 5.421010862427522e-20;
+
+// Per-mode inputs: w = omega / sigma as a double-float and e^(omega / kT)
+// (from FP64, clamped to FP32's range).
+__host__ __device__ __forceinline__ float4 wv_pack(double w, double v) {
+  const F2 a = f2_of(w);
+  return make_float4(a.hi, a.lo, (float)fmin(exp(v), 3.0e38), 0.f);
+}
+
+struct VtxF {
+  float ap, am;   // n + f(E + omega), n + 1 - f(E - omega)
+  float dp;       // delta(E' - E - omega) (= the phonon side's delta(E' - omega - E)), x 2^64 if SHIFT
+  float dm;       // delta(E' - E + omega), x 2^64 if SHIFT
+};
+// dn = (E - E') / sigma (double-float); ex = e^x, emx = e^-x with x = (E -
+// mu) / kT (FP64 exponentials, clamped to FP32's range); wv (wv_pack) of the
+// mode; bose = n(omega); dnorm = 1 / (sigma sqrt(2 pi) N_k).  The Fermi
+// factors need no exponential here: f(E + omega) = 1 / (1 + e^x e^v), and
+// 1 + n - f(E - omega) = n + 1 / (1 + e^-x e^v), which has no cancellation
+// when f(E - omega) is close to 1.
+template <bool SHIFT>
+__device__ __forceinline__ VtxF vtx_factors(F2 dn, float ex, float emx, float4 wv, float bose, float dnorm) {
+  VtxF r;
+  const F2 w{wv.x, wv.y};
+  const F2 tp = f2_add(dn, w), tm = f2_add(dn, F2{-w.hi, -w.lo});
+  const F2 ap = f2_half_sq(tp), am = f2_half_sq(tm);
+  if (SHIFT) {
+    const F2 sh{LN2X64_HI, LN2X64_LO};
+    r.dp = dnorm * f2_exp(f2_add(sh, F2{-ap.hi, -ap.lo}));
+    r.dm = dnorm * f2_exp(f2_add(sh, F2{-am.hi, -am.lo}));
+  } else {
+    r.dp = dnorm * f2_exp(F2{-ap.hi, -ap.lo});
+    r.dm = dnorm * f2_exp(F2{-am.hi, -am.lo});
+  }
+  r.ap = bose + __frcp_rn(1.0f + ex * wv.z);
+  r.am = bose + __frcp_rn(1.0f + emx * wv.z);
+  return r;
+}
+
+__global__ void k_qtab(int n, const double *om, const double *bose, double sigma, double kT, double const_tp,
+                       float *cx, float *bs, float4 *wv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double o = om[i];
+  cx[i] = (o >= 0.5e-3) ? (float)(const_tp * 0.5 * g2unitfactor / o) : 0.0f;
+  bs[i] = (float)bose[i];
+  wv[i] = wv_pack(o / sigma, o / kT);
+}
+
 // One thread per (k', initial state): G(n',s') from the FP32 GEMM output, the
 // U_k' and phonon rotations in FP32, the Gaussian delta and occupations from
 // FP64 energy differences scaled to O(1) before rounding, X+- and the pair sum.
@@ -1034,7 +1114,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
     const int i = code / nw, m = code % nw;
     const int p = d.sidx[i], pp = d.widx[ip];
     const double E = d.ens[(size_t)p * nw + m];
-    const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+    const float ex = (float)fmin(exp((E - rp.chempot) / (kB * rp.T)), 3.0e38);
     const double inv_sig = 1.0 / rp.sigma;
     const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
     int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
@@ -1043,7 +1123,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
                         rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
     const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
     const bool ph = d.phr || d.yv;
-    const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
+    const YOcc yo = y_occ(E, rp.chempot, kB * rp.T);   // also e^-x of the Fermi factors
     float acc = 0.0f;
     int rank_n = 0;
     for (int n = 0; n < nw; ++n) {
@@ -1064,7 +1144,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
         const float2 *Uk = d.Uf + ((size_t)p * nw + m) * nw;
         for (int c = 0; c < nw; ++c) cfmaf_cj(unm, Ukp[c], Uk[c]);
       }
-      const float dn = (float)((E - eps) * inv_sig);
+      const F2 dn = f2_of((E - eps) * inv_sig);
       for (int s = 0; s < nb; ++s) {
         const int qs = q * nb + s;
         const float2 *u = d.uf + (size_t)qs * nb;
@@ -1072,16 +1152,13 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
         for (int sp = 0; sp < nb; ++sp) cfmaf(g, u[sp], h[sp]);
         if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
         const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
-        const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
-        const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
-        const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
-        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-        const float xp = g2c * (qt.bose[qs] + fp) * dp;
-        const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+        const VtxF f = vtx_factors<true>(dn, ex, yo.emx, qt.wv[qs], qt.bose[qs], dnorm);
+        const float xp = g2c * f.ap * (f.dp * TWO_M64);
+        const float xm = g2c * f.am * (f.dm * TWO_M64);
         acc += xp + xm;
-        // Y: the Gaussian is even, so delta(E' - omega - E) is dp
-        const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
-        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+        // Y, scaled by 2^64: the Gaussian is even, so delta(E' - omega - E) is dp
+        const float y = ph ? g2c * f.dp * y_factor(yo, qt.bose[qs]) : 0.f;
+        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * TWO_M64D * (double)y);
         if (d.g2) {
           int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
           if (off < d.cap) {
@@ -1089,7 +1166,7 @@ __global__ void __launch_bounds__(128) k_epilogue_split(int nwv, int j0, const f
             d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
             d.xp[off] = xp;
             d.xm[off] = xm;
-            if (d.yv) d.yv[off] = y;
+            if (d.yv) d.yv[off] = TWO_M64D * (double)y;
           }
         }
       }
@@ -1190,13 +1267,13 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
       const int i = code / nw, m = code % nw;
       const int p = d.sidx[i];
       const double E = d.ens[(size_t)p * nw + m];
-      const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+      const float ex = (float)fmin(exp((E - rp.chempot) / (kB * rp.T)), 3.0e38);
       const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
       const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
                           rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
       const float *gr = sr + row * ld, *gi = si + row * ld;
       const bool ph = d.phr || d.yv;
-      const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
+      const YOcc yo = y_occ(E, rp.chempot, kB * rp.T);   // also e^-x of the Fermi factors
       float acc = 0.0f;
       int rank_n = 0;
       for (int n = 0; n < nw; ++n) {
@@ -1224,7 +1301,7 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
             if (np < nw) cfmaf_cj(a, uk[np], make_float2(gr[np + nw * s], gi[np + nw * s]));
           h[s] = a;
         }
-        const float dn = (float)((E - eps) * inv_sig);
+        const F2 dn = f2_of((E - eps) * inv_sig);
 #pragma unroll
         for (int s = 0; s < AB; ++s) {
           if (s >= nb) break;
@@ -1236,15 +1313,13 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
             if (sp < nb) cfmaf(g, u[sp], h[sp]);
           if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
           const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
-          const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
-          const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
-          const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
-          const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-          const float xp = g2c * (qt.bose[qs] + fp) * dp;
-          const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+          const VtxF f = vtx_factors<true>(dn, ex, yo.emx, qt.wv[qs], qt.bose[qs], dnorm);
+          const float xp = g2c * f.ap * (f.dp * TWO_M64);
+          const float xm = g2c * f.am * (f.dm * TWO_M64);
           acc += xp + xm;
-          const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
-          if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+          // Y, scaled by 2^64: the Gaussian is even, so delta(E' - omega - E) is dp
+          const float y = ph ? g2c * f.dp * y_factor(yo, qt.bose[qs]) : 0.f;
+          if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * TWO_M64D * (double)y);
           if (d.g2) {
             int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
             if (off < d.cap) {
@@ -1252,7 +1327,7 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
               d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
               d.xp[off] = xp;
               d.xm[off] = xm;
-              if (d.yv) d.yv[off] = y;
+              if (d.yv) d.yv[off] = TWO_M64D * (double)y;
             }
           }
         }
@@ -1295,7 +1370,7 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
     const int i = code / NW, m = code % NW;
     const int p = d.sidx[i], pp = d.widx[ip];
     const double E = d.ens[(size_t)p * NW + m];
-    const float a_occ = (float)((E - rp.chempot) / (kB * rp.T));
+    const float ex = (float)fmin(exp((E - rp.chempot) / (kB * rp.T)), 3.0e38);
     const double inv_sig = 1.0 / rp.sigma;
     const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
     const int a1 = p % rp.mesh[0], a2 = (p / rp.mesh[0]) % rp.mesh[1], a3 = p / (rp.mesh[0] * rp.mesh[1]);
@@ -1305,7 +1380,7 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
     const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
     const float *rr = Cr + base, *ri = Ci + base;
     const bool ph = d.phr || d.yv;
-    const YOcc yo = ph ? y_occ(E, rp.chempot, kB * rp.T) : YOcc{0.f, 0.f};
+    const YOcc yo = y_occ(E, rp.chempot, kB * rp.T);   // also e^-x of the Fermi factors
     float acc = 0.0f;
     int rank_n = 0;
     for (int n = 0; n < NW; ++n) {
@@ -1337,7 +1412,7 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
         }
         h[s] = a;
       }
-      const float dn = (float)((E - eps) * inv_sig);
+      const F2 dn = f2_of((E - eps) * inv_sig);
 #pragma unroll
       for (int s = 0; s < EPR_NB; ++s) {
         if (s >= nb) break;
@@ -1349,15 +1424,13 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
           if (sp < nb) cfmaf(g, u[sp], h[sp]);
         if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
         const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
-        const float tp = dn + qt.w[qs], tm = dn - qt.w[qs];
-        const float fp = 1.0f / (__expf(a_occ + qt.v[qs]) + 1.0f);
-        const float fm = 1.0f / (__expf(a_occ - qt.v[qs]) + 1.0f);
-        const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-        const float xp = g2c * (qt.bose[qs] + fp) * dp;
-        const float xm = g2c * (1.0f + qt.bose[qs] - fm) * dm;
+        const VtxF f = vtx_factors<true>(dn, ex, yo.emx, qt.wv[qs], qt.bose[qs], dnorm);
+        const float xp = g2c * f.ap * (f.dp * TWO_M64);
+        const float xm = g2c * f.am * (f.dm * TWO_M64);
         acc += xp + xm;
-        const float y = ph ? g2c * dp * y_factor(yo, qt.bose[qs]) : 0.f;
-        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+        // Y, scaled by 2^64: the Gaussian is even, so delta(E' - omega - E) is dp
+        const float y = ph ? g2c * f.dp * y_factor(yo, qt.bose[qs]) : 0.f;
+        if (d.phr && y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * TWO_M64D * (double)y);
         if (d.g2) {
           int64_t off = (int64_t)j * d.per_state + ((int64_t)d.cum[ip] + rank_n) * nb + s;
           if (off < d.cap) {
@@ -1365,7 +1438,7 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
             d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
             d.xp[off] = xp;
             d.xm[off] = xm;
-            if (d.yv) d.yv[off] = y;
+            if (d.yv) d.yv[off] = TWO_M64D * (double)y;
           }
         }
       }
@@ -1414,7 +1487,7 @@ constexpr int F_SMEM = F_STAGES * F_STAGE + 1024 + 256;
 // entries of each table (a few cache lines per load instead of 32).
 struct StateRec {      // per initial state j
   double E;            // eV
-  float a_occ;         // (E - mu) / kT
+  float ex;            // e^x, x = (E - mu) / kT (FP64 exponential, clamped); e^-x is yo.emx
   int apack;           // mesh coordinates of k: a1 | a2 << 10 | a3 << 20
   YOcc yo;             // per-state part of the phonon-side occupation factor
   int urow;            // p * 8 + m: the state's U_k row in the fp32 eigenvector table
@@ -1428,7 +1501,8 @@ struct FusedTabs {
   const StateRec *state;   // [nst]
   const float4 *U4;        // row-blocked, fields n * 4 + h: U_k'[n][2h], U_k'[n][2h + 1] (fp32 complex)
   const double *ensw;      // row-blocked, fields n: window-k' band energies
-  const float4 *rec;       // q-blocked, fields s * 4 + f: u[s][0..1], u[s][2..3], u[s][4..5], (cx, bose, w, v)
+  const float4 *rec;       // q-blocked, fields s * 5 + f: u[s][0..1], u[s][2..3], u[s][4..5], (cx, bose, -, -),
+                           // (w as a double-float, e^(omega / kT): wv_pack)
   const float2 *glb;       // polar crystals: q-blocked, fields s: long_range_prefac(q, u_s) (else null)
   int MpB, N;
 };
@@ -1482,7 +1556,7 @@ __global__ void k_fused_states(int nst, const int *st_code, const int *widx, con
   const int p = widx[code >> 3];
   StateRec r;
   r.E = ens[(size_t)p * 8 + (code & 7)];
-  r.a_occ = (float)((r.E - chempot) / kT);
+  r.ex = (float)fmin(exp((r.E - chempot) / kT), 3.0e38);
   r.yo = y_occ(r.E, chempot, kT);
   r.urow = p * 8 + (code & 7);
   const int a1 = p % m0, a2 = (p / m0) % m1, a3 = p / (m0 * m1);
@@ -1490,16 +1564,17 @@ __global__ void k_fused_states(int nst, const int *st_code, const int *widx, con
   out[j] = r;
 }
 
-__global__ void k_fused_recs(int N, const float2 *uf, const float *cx, const float *bs, const float *w, const float *v,
+__global__ void k_fused_recs(int N, const float2 *uf, const float *cx, const float *bs, const float4 *wv,
                              float4 *rec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;   // (q, s) = (i / 6, i % 6)
   if (i >= N * 6) return;
   const int q = i / 6, s = i % 6;
   const float2 *u = uf + (size_t)i * 6;
-  rec[blk32(q, 24, s * 4 + 0)] = make_float4(u[0].x, u[0].y, u[1].x, u[1].y);
-  rec[blk32(q, 24, s * 4 + 1)] = make_float4(u[2].x, u[2].y, u[3].x, u[3].y);
-  rec[blk32(q, 24, s * 4 + 2)] = make_float4(u[4].x, u[4].y, u[5].x, u[5].y);
-  rec[blk32(q, 24, s * 4 + 3)] = make_float4(cx[i], bs[i], w[i], v[i]);
+  rec[blk32(q, 30, s * 5 + 0)] = make_float4(u[0].x, u[0].y, u[1].x, u[1].y);
+  rec[blk32(q, 30, s * 5 + 1)] = make_float4(u[2].x, u[2].y, u[3].x, u[3].y);
+  rec[blk32(q, 30, s * 5 + 2)] = make_float4(u[4].x, u[4].y, u[5].x, u[5].y);
+  rec[blk32(q, 30, s * 5 + 3)] = make_float4(cx[i], bs[i], 0.f, 0.f);
+  rec[blk32(q, 30, s * 5 + 4)] = wv[i];
 }
 
 __global__ void k_fused_glp(int N, const float2 *glpf, float2 *glb) {
@@ -1554,20 +1629,22 @@ __device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const 
 
 // the six vertices (s) of one (k', n) final state for one initial state; returns X+ + X-
 // rec = the lane's entry of field 0 of q's block: fields 32 float4 apart.
-// PH: also ys[s] += |g|^2 cx delta, the n-dependent part of Y; its occupation
-// factor depends on the initial state and the mode only and is applied once per
-// pair (y_factor).
+// dn = (E - E_n') / sigma as a double-float, ex = e^((E - mu) / kT).
+// PH: also ys[s] += |g|^2 cx delta * 2^64, the n-dependent part of Y; its
+// occupation factor depends on the initial state and the mode only and is
+// applied once per pair (y_factor).
 // POLAR: g += long_range_prefac(q, u_s) * <U_k'[n]|U_k[m]> (glb = the lane's
 // entry of field 0 of q's block of the prefactor table, unm the overlap).
 template <bool PH, bool POLAR>
-__device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, float dn, float a_occ,
+__device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, F2 dn, float ex,
                                                 float dnorm, const EpiData &d, int64_t voff, int q,
                                                 const YOcc &yo, float *ys, const float2 *glb, float2 unm) {
   float acc = 0.f;
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
-    const float4 u01 = __ldg(rec + (4 * s) * 32), u23 = __ldg(rec + (4 * s + 1) * 32),
-                 u45 = __ldg(rec + (4 * s + 2) * 32), sc = __ldg(rec + (4 * s + 3) * 32);
+    const float4 u01 = __ldg(rec + (5 * s) * 32), u23 = __ldg(rec + (5 * s + 1) * 32),
+                 u45 = __ldg(rec + (5 * s + 2) * 32), sc = __ldg(rec + (5 * s + 3) * 32),
+                 wv = __ldg(rec + (5 * s + 4) * 32);
     float2 g = make_float2(0.f, 0.f);
     cfmaf(g, make_float2(u01.x, u01.y), h[0]);
     cfmaf(g, make_float2(u01.z, u01.w), h[1]);
@@ -1576,16 +1653,14 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
     cfmaf(g, make_float2(u45.x, u45.y), h[4]);
     cfmaf(g, make_float2(u45.z, u45.w), h[5]);
     if (POLAR) cfmaf(g, __ldg(glb + s * 32), unm);
-    // sc = (cx, bose, w, v)
+    // sc = (cx, bose, -, -)
     const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
-    const float tp = dn + sc.z, tm = dn - sc.z;
-    const float fp = 1.0f / (__expf(a_occ + sc.w) + 1.0f);
-    const float fm = 1.0f / (__expf(a_occ - sc.w) + 1.0f);
-    const float dp = dnorm * __expf(-0.5f * tp * tp), dm = dnorm * __expf(-0.5f * tm * tm);
-    const float xp = g2c * (sc.y + fp) * dp;
-    const float xm = g2c * (1.0f + sc.y - fm) * dm;
+    // PH: the Gaussians x 2^64 (the phonon side's sums keep their tails)
+    const VtxF f = vtx_factors<PH>(dn, ex, yo.emx, wv, sc.y, dnorm);
+    const float xp = g2c * f.ap * (PH ? f.dp * TWO_M64 : f.dp);
+    const float xm = g2c * f.am * (PH ? f.dm * TWO_M64 : f.dm);
     acc += xp + xm;
-    if (PH) ys[s] = fmaf(g2c, dp, ys[s]);   // the Gaussian is even: delta(E' - omega - E) is dp
+    if (PH) ys[s] = fmaf(g2c, f.dp, ys[s]);   // the Gaussian is even: delta(E' - omega - E) is dp (x 2^64)
     if (d.g2) {
       const int64_t off = voff + s;
       if (off < d.cap) {
@@ -1593,11 +1668,26 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
         d.g2[off] = (om == 0.0) ? 0.0 : 0.5 * (double)(g.x * g.x + g.y * g.y) / om * g2unitfactor;
         d.xp[off] = xp;
         d.xm[off] = xm;
-        if (PH && d.yv) d.yv[off] = (g2c * dp) * y_factor(yo, sc.y);
+        if (PH && d.yv) d.yv[off] = TWO_M64D * (double)((g2c * f.dp) * y_factor(yo, sc.y));
       }
     }
   }
   return acc;
+}
+
+// Tile order of the fused stage B.  Tile t of mpairs x ntiles (m-tile pair,
+// state pair) walks the m-pairs in FB_MBANDS bands, each band over every state
+// pair before the next band starts, so that only a band's phase tiles have to
+// stay in L2 while the state operand streams past (the state operand is read
+// FB_MBANDS times from DRAM, the phase planes once).
+constexpr int FB_MBANDS = 2;
+__device__ __forceinline__ void fb_tile(int t, int mpairs, int ntiles, int &mp, int &nt) {
+  const int m0 = (mpairs + FB_MBANDS - 1) / FB_MBANDS;
+  const int band = t / (m0 * ntiles);
+  const int r = t - band * m0 * ntiles;
+  const int sz = min(m0, mpairs - band * m0);
+  mp = band * m0 + r % sz;
+  nt = r / sz;
 }
 
 // PH: the phonon side too (Y of every vertex into the ph-e rate of its (q, s)).
@@ -1653,7 +1743,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       uint32_t phase = 0;
       bool ok = true;
       for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
-        const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
+        int mp, nt;
+        fb_tile(t, mpairs, g.ntiles, mp, nt);
+        const int mt = 2 * mp + (int)crank;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
           uint8_t *sb = smem + stage * F_STAGE;
@@ -1726,7 +1818,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const int m0 = rp.mesh[0], m1 = rp.mesh[1], m2 = rp.mesh[2];
     int it = 0;
     for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
-      const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
+      int mp, nt;
+      fb_tile(t, mpairs, g.ntiles, mp, nt);
+      const int mt = 2 * mp + (int)crank;
       // ---- row and state data, before the accumulators are ready
       const int ip = mt * BM + quad * 32 + lane;      // < MpB
       const int j = nt * 2 + slot;                    // warp-uniform
@@ -1735,13 +1829,13 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       unsigned wmask = 0;
       int q = 0;
       double E = 0.0;
-      float a_occ = 0.f;
+      float ex = 0.f;
       YOcc yo{0.f, 0.f};
       const float2 *Uk = nullptr;   // the state's U_k[m] (polar)
       if (jvalid) {
         const StateRec sr = tb.state[j];
         E = sr.E;
-        a_occ = sr.a_occ;
+        ex = sr.ex;
         yo = sr.yo;
         if (POLAR) Uk = d.Uf + (size_t)sr.urow * 8;
         wmask = (unsigned)ri.y;
@@ -1755,7 +1849,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       const int n1 = nbw > 1 ? __ffs(rest) - 1 : 0;
       const float4 *ub = tb.U4 + blk32(ip, 32, 0);
       const double *eb = tb.ensw + blk32(ip, 8, 0);
-      const float4 *rq = tb.rec + blk32(q, 24, 0);
+      const float4 *rq = tb.rec + blk32(q, 30, 0);
       float2 u0[8], u1[8];
       if (nbw > 0) load_urow(ub, n0, u0);
       if (nbw > 1) load_urow(ub, n1, u1);
@@ -1802,12 +1896,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
             if (mine) hx[sp] = hrot(ux, gre, gim);
           }
           if (mine) {
-            const float dn = (float)((E - __ldg(eb + nb_ * 32)) * inv_sig);
+            const F2 dn = f2_of((E - __ldg(eb + nb_ * 32)) * inv_sig);
             float2 unmx = make_float2(0.f, 0.f);
             if (POLAR)
 #pragma unroll
               for (int c = 0; c < 8; ++c) cfmaf_cj(unmx, ux[c], __ldg(Uk + c));
-            acc += fused_vertices<PH, POLAR>(hx, rq, dn, a_occ, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys, glb,
+            acc += fused_vertices<PH, POLAR>(hx, rq, dn, ex, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys, glb,
                                              unmx);
           }
         }
@@ -1817,12 +1911,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       // ---- vertices of the first two bands, overlapping the next tile's MMAs
       float acc01 = 0.f;
       if (nbw > 0) {
-        const float dn = (float)((E - __ldg(eb + n0 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH, POLAR>(h0, rq, dn, a_occ, dnorm, d, vbase, q, yo, ys, glb, unm0);
+        const F2 dn = f2_of((E - __ldg(eb + n0 * 32)) * inv_sig);
+        acc01 += fused_vertices<PH, POLAR>(h0, rq, dn, ex, dnorm, d, vbase, q, yo, ys, glb, unm0);
       }
       if (nbw > 1) {
-        const float dn = (float)((E - __ldg(eb + n1 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH, POLAR>(h1, rq, dn, a_occ, dnorm, d, vbase + 6, q, yo, ys, glb, unm1);
+        const F2 dn = f2_of((E - __ldg(eb + n1 * 32)) * inv_sig);
+        acc01 += fused_vertices<PH, POLAR>(h1, rq, dn, ex, dnorm, d, vbase + 6, q, yo, ys, glb, unm1);
       }
       double v = (double)acc01 + (double)acc;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -1830,8 +1924,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       if (PH && jvalid && nbw > 0 && d.phr) {   // this pair's Y into the rates of (q, s), s = 0..5
 #pragma unroll
         for (int s = 0; s < 6; ++s) {
-          const float y = ys[s] * y_factor(yo, __ldg(rq + (4 * s + 3) * 32).y);
-          if (y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * (double)y);
+          const float y = ys[s] * y_factor(yo, __ldg(rq + (5 * s + 3) * 32).y);   // x 2^64
+          if (y != 0.f) atomicAdd(d.phr + q + (size_t)rp.N * s, d.ph_scale * TWO_M64D * (double)y);
         }
       }
     }
@@ -2239,19 +2333,19 @@ static inline int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 // fp32 copies of the eigenvectors and the per-(q, s) scalars of the epilogues
 struct EpiTables {
   float2 *Uf;
-  float *cx, *bs, *w, *v;
+  float *cx, *bs;
+  float4 *wv;
 };
 
 static int epi_tables(Workspace &ws, cudaStream_t st, const double2 *U, const RateParams &rp, const EpiData &ed_in,
                       int64_t *launches, EpiTables *t) {
   const int N = rp.N, nw = rp.nw, nb = rp.nb;
   if (wsget(ws, "tc_Uf", (size_t)N * nw * nw, &t->Uf) || wsget(ws, "tc_cx", (size_t)N * nb, &t->cx) ||
-      wsget(ws, "tc_bs", (size_t)N * nb, &t->bs) || wsget(ws, "tc_w", (size_t)N * nb, &t->w) ||
-      wsget(ws, "tc_v", (size_t)N * nb, &t->v))
+      wsget(ws, "tc_bs", (size_t)N * nb, &t->bs) || wsget(ws, "tc_wv", (size_t)N * nb, &t->wv))
     return tfail(6, ws.msg.c_str());
   k_to_f2<<<(unsigned)(((int64_t)N * nw * nw + 255) / 256), 256, 0, st>>>((int64_t)N * nw * nw, U, t->Uf);
   k_qtab<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.om, ed_in.bose, rp.sigma, kB * rp.T, rp.const_tp, t->cx,
-                                                t->bs, t->w, t->v);
+                                                t->bs, t->wv);
   TCK(cudaGetLastError());
   *launches += 2;
   return 0;
@@ -2383,7 +2477,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   if ((rc = epi_tables(ws, st, U, rp, ed_in, launches, &et))) return rc;
   EpiData ed = ed_in;
   ed.Uf = et.Uf;
-  QTab qt{et.cx, et.bs, et.w, et.v};
+  QTab qt{et.cx, et.bs, et.wv};
   for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
@@ -2485,13 +2579,13 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   double *tens;
   if ((rc = wsget(ws, "tc_frow", (size_t)Mp, &trow)) || (rc = wsget(ws, "tc_fst", (size_t)nst, &tst)) ||
       (rc = wsget(ws, "tc_fU4", (size_t)32 * Mp, &tU4)) || (rc = wsget(ws, "tc_fens", (size_t)8 * Mp, &tens)) ||
-      (rc = wsget(ws, "tc_frec", (size_t)24 * rup(N, 32), &trec)))
+      (rc = wsget(ws, "tc_frec", (size_t)30 * rup(N, 32), &trec)))
     return tfail(6, ws.msg.c_str());
   k_fused_rows<<<(Mp + 127) / 128, 128, 0, st>>>(nwv, Mp, widx, ed_in.ens, et.Uf, ed_in.cum, rp.enref, rp.fsthick,
                                                  mesh[0], mesh[1], trow, tU4, tens);
   k_fused_states<<<(nst + 127) / 128, 128, 0, st>>>(nst, st_code, arow, ed_in.ens, rp.chempot, kB * rp.T, mesh[0],
                                                     mesh[1], tst);
-  k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, et.cx, et.bs, et.w, et.v, trec);
+  k_fused_recs<<<(N * 6 + 255) / 256, 256, 0, st>>>(N, ed_in.uf, et.cx, et.bs, et.wv, trec);
   TCK(cudaGetLastError());
   *launches += 3;
   float2 *tglb = nullptr;   // polar: long_range_prefac(q, u_s), q-blocked

@@ -2,11 +2,14 @@
 
     python -m elphbolt_gb300.run_rates --mesh 12 --precision split --repeat 2
     python -m elphbolt_gb300.run_rates --mesh 12 --side ph --crystal sic
+    python -m elphbolt_gb300.run_rates --mesh 40 --crystal large --window 0.1
 
 The crystal is the Si-like synthetic one (fcc, 2 atoms, nw = 8, 6^3 WS
 supercell), or with --crystal sic the polar zincblende SiC-like one (same
-sizes, Born charges and dielectric tensor on); the window is +-0.5 eV about
-mid-gap + 0.6 eV, Gaussian delta 10 meV, 300 K.  --side el runs
+sizes, Born charges and dielectric tensor on), or with --crystal large the
+large instance (6-atom cell, nw = 32, nb = 18, 279 + 279 WS cells, 23 GB of
+g(Re,Rp)); the window is +-0.5 eV (--window) about mid-gap + 0.6 eV,
+Gaussian delta 10 meV, 300 K.  --side el runs
 ephg_el_rates (electron RTA rates), --side ph runs ephg_ph_rates with the
 electron rates (both sides in one sweep).  Useful for quick checks and for
 profiling a smaller case of the same kernels as the benchmark.
@@ -26,16 +29,20 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--nw", type=int, default=8)
     ap.add_argument("--side", choices=["el", "ph"], default="el")
-    ap.add_argument("--crystal", choices=["si", "sic"], default="si")
+    ap.add_argument("--crystal", choices=["si", "sic", "large"], default="si")
+    ap.add_argument("--window", type=float, default=0.5, help="window half width, eV")
     a = ap.parse_args(argv)
     from . import _lib, build, synthetic as S
     from .wannier import Wannier
     build.build()
     if a.crystal == "sic":
         wd = S.make_wannier(S.make_crystal_sic_like(), a.nw, supercell=(6, 6, 6), seed=20260105)
+    elif a.crystal == "large":
+        wd = S.large_instance()
     else:
         wd = S.si_like(nw=a.nw)
-    req = S.si_like_request(wd, (a.mesh,) * 3, delta_kind={"gaussian": 0, "triangle": 1, "tetra": 2}[a.delta])
+    req = S.si_like_request(wd, (a.mesh,) * 3, window=a.window,
+                            delta_kind={"gaussian": 0, "triangle": 1, "tetra": 2}[a.delta])
     W = Wannier(wd)
     prec = _lib.PREC_SPLIT_TF32 if a.precision == "split" else _lib.PREC_FP64
     for i in range(a.repeat):

@@ -1,6 +1,6 @@
 """Serving measurement: a Poisson stream of RTA-rate requests over resident crystals.
 
-    python -m elphbolt_gb300.serve_bench --requests 40 --load 0.8 --slots 8 --budget-gb 160
+    python -m elphbolt_gb300.serve_bench --requests 400 --load 0.8 --slots 8 --budget-gb 160
 
 Three synthetic Si-like crystals stay resident on the GPU: nw = 8 (the bench
 crystal, 6^3 WS sets), nw = 16 and nw = 32 (4^3 WS sets, so that g(Re,Rp)
@@ -47,7 +47,7 @@ def request_mix(wds, n, rng):
     return out
 
 
-def measure(n_requests=40, load=0.8, seed=20260104, budget_bytes=160 << 30, nslots=8, fp64_sample=2, wds=None):
+def measure(n_requests=400, load=0.8, seed=20260104, budget_bytes=160 << 30, nslots=8, fp64_sample=2, wds=None):
     """On one server: the isolated solve time of every request of a seeded stream
     (each run alone, which also trains the server's time models), capacity (the
     same requests submitted at once), then the stream with Poisson arrivals at
@@ -121,7 +121,7 @@ def measure(n_requests=40, load=0.8, seed=20260104, budget_bytes=160 << 30, nslo
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description="serving-loop latency / throughput on synthetic crystals")
-    ap.add_argument("--requests", type=int, default=40)
+    ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--load", type=float, default=0.8)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--budget-gb", type=float, default=160.0)

@@ -301,7 +301,7 @@ def make_crystal_multi(natoms: int, rng, mass_range=(12.0, 60.0)) -> Crystal:
 def make_wannier(crys: Crystal, nw: int, supercell=(6, 6, 6), seed: int = 20260101,
                  h_sigma_ev: float = 1.0, g_sigma_ev_ang: float = 0.1,
                  decay_ang: float = 2.0, spring_range=(5.0, 15.0),
-                 nvalence: int | None = None) -> WannierData:
+                 nvalence: int | None = None, lean: bool = False) -> WannierData:
     """Build the synthetic Wannier data for a crystal.
 
     H(Re) entries are N(0, h_sigma) eV * exp(-|Re|/decay); g(Re, Rp) entries
@@ -318,13 +318,24 @@ def make_wannier(crys: Crystal, nw: int, supercell=(6, 6, 6), seed: int = 202601
     D = _springs(crys, cells, supercell, rng, *spring_range)
     nws = cells.shape[0]
     shape = (nw, nw, nws, nb, nws)
-    # draw in C order of (Rp, s, Re, j, i) so the stream is the F-order layout
-    gr = rng.standard_normal(shape[::-1]) + 1j * rng.standard_normal(shape[::-1])
-    g = np.asfortranarray(gr.T) * (g_sigma_ev_ang / math.sqrt(2.0))
     env = np.exp(-rlen / decay_ang)
-    g *= env[None, None, :, None, None]
-    g *= env[None, None, None, None, :]
-    g *= EV_PER_ANG_TO_RY_PER_BOHR
+    if not lean:
+        # draw in C order of (Rp, s, Re, j, i) so the stream is the F-order layout
+        gr = rng.standard_normal(shape[::-1]) + 1j * rng.standard_normal(shape[::-1])
+        g = np.asfortranarray(gr.T) * (g_sigma_ev_ang / math.sqrt(2.0))
+        g *= env[None, None, :, None, None]
+        g *= env[None, None, None, None, :]
+        g *= EV_PER_ANG_TO_RY_PER_BOHR
+    else:
+        # one Rp slab at a time (same distribution, a different stream): the
+        # peak host memory is g itself plus one slab
+        g = np.empty(shape, dtype=np.complex128, order="F")
+        slab = shape[:4]
+        for rp in range(nws):
+            x = rng.standard_normal(slab[::-1]) + 1j * rng.standard_normal(slab[::-1])
+            x *= (g_sigma_ev_ang / math.sqrt(2.0)) * env[rp] * EV_PER_ANG_TO_RY_PER_BOHR
+            x *= env[None, :, None, None]            # C-order (s, Re, j, i): Re on axis 1
+            g[:, :, :, :, rp] = x.T
     wd = WannierData(crystal=crys, numwannbands=nw, numbranches=nb,
                      coarse_qmesh=np.asarray(supercell, dtype=np.int64),
                      rcells_k=cells.copy(), rcells_q=cells.copy(), rcells_g=cells.copy(),
@@ -467,6 +478,16 @@ def si_like_request(wd: WannierData, mesh=(12, 12, 12), T: float = 300.0,
     mu = wd.midgap + shift
     return RateRequest(mesh=tuple(int(x) for x in mesh), enref=mu, fsthick=window,
                        chempot=mu, T=T, delta_kind=delta_kind, sigma=sigma)
+
+
+def large_instance(supercell=(6, 6, 6), seed: int = 20260103) -> WannierData:
+    """The large single instance: a 6-atom fcc cell (``make_crystal_multi``,
+    masses U[12, 60] amu), nw = 32 Wannier bands, nb = 18 modes, Re and Rp
+    Wigner-Seitz sets of a 6x6x6 supercell (279 cells each): g(Re,Rp) is
+    32^2 x 18 x 279^2 complex128 = 23 GB.  Value distributions as si_like."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    crys = make_crystal_multi(6, rng)
+    return make_wannier(crys, 32, supercell=supercell, seed=seed + 1, lean=True)
 
 
 # The batched workload: many requests of uneven size on random crystals.

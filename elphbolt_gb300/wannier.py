@@ -229,6 +229,16 @@ class Wannier:
             out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
         return out
 
+    def average_degenerate(self, req, g2, mode=_lib.DEGAVG_MEAN, thres=1e-6):
+        """Degenerate-subspace gauge fixing of an ``el_rates`` |g|^2 vertex list
+        (``ephg_g2_average_degenerate``; plot_along_path, wannier.f90:1332-1384):
+        returns the averaged copy.  ``mode``: ``DEGAVG_REFERENCE`` (the
+        reference's in-place loops) or ``DEGAVG_MEAN`` (gauge-invariant means)."""
+        r = _rate_request(req, _lib.PREC_FP64)
+        out = np.array(g2, dtype=np.float64, copy=True)
+        check(self._L.ephg_g2_average_degenerate(self._h, ct.byref(r), int(mode), float(thres), out.size, _p(out)))
+        return out
+
     def ph_rates(self, req, precision=_lib.PREC_FP64, spindeg=2, electrons=False, vertices=False, cap=None):
         """Fused ibzq 'g' + 'Y' + ph-e RTA rates (``ephg_ph_rates``).
 

@@ -213,6 +213,27 @@ int ephg_ph_rates(ephg_handle *h, const ephg_rate_request *req, int64_t spindeg,
                   double *el_rates, int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *y,
                   int64_t cap);
 
+/* Degenerate-subspace gauge fixing of |g|^2 (plot_along_path, wannier.f90:
+ * 1332-1384; the same loops in test/check_interactions_symmetries.f90:330-384),
+ * FP64 on the device.  g2 (nv): a vertex list of req in the order
+ * ephg_el_rates writes it (every vertex: nv = stats.vertices, either
+ * precision, or read back from gk2.istate files), replaced in place.  Three
+ * passes in the reference's order: over the phonon branches s of q = k' - k
+ * (|omega_s - omega_s'| < thres), the initial bands m of each k and the final
+ * bands n of each k' (|E - E'| < thres); thres in eV (<= 0: the reference's
+ * 1e-6).  The band groups are the window bands, the only ones the list holds.
+ * mode EPHG_DEGAVG_REFERENCE: the reference's loops as written, in place -- a
+ * member averages values its predecessors in the group have already replaced,
+ * so its result still depends on the eigenvector gauge; EPHG_DEGAVG_MEAN:
+ * every member takes the mean of the group's values before the pass, which is
+ * gauge invariant.  Runs the request's set-up (energies, phonons, window), not
+ * its contractions.  The reference's rate path does not average; nor does
+ * ephg_el_rates. */
+#define EPHG_DEGAVG_REFERENCE 0
+#define EPHG_DEGAVG_MEAN 1
+int ephg_g2_average_degenerate(ephg_handle *h, const ephg_rate_request *req, int64_t mode, double thres,
+                               int64_t nv, double *g2);
+
 /* ---- Serving loop ----
  * No counterpart in the reference, which answers one request per run from
  * disk; this is the scope's serving form.  A server keeps the crystals of

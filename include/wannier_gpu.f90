@@ -29,6 +29,7 @@ module ephg_c
   integer(c_int64_t), parameter :: EPHG_DELTA_GAUSSIAN = 0, EPHG_DELTA_TRIANGLE = 1, &
        EPHG_DELTA_TETRA = 2
   integer(c_int64_t), parameter :: EPHG_WANNSPACE_EL = 0, EPHG_WANNSPACE_PH = 1
+  integer(c_int64_t), parameter :: EPHG_DEGAVG_REFERENCE = 0, EPHG_DEGAVG_MEAN = 1
 
   type, bind(C) :: ephg_wannier_desc
      integer(c_int64_t) :: numwannbands, numbranches, nwsk, nwsq, nwsg, numatoms
@@ -173,6 +174,16 @@ module ephg_c
        type(ephg_rate_request), intent(in) :: req
        integer(c_int64_t), value :: spindeg, cap
      end function ephg_ph_rates
+
+     integer(c_int) function ephg_g2_average_degenerate(h, req, mode, thres, nv, g2) &
+          bind(C, name="ephg_g2_average_degenerate")
+       !! mode 0: the reference's in-place loops (wannier.f90:1332-1384); 1: gauge-invariant means
+       import :: c_int, c_ptr, c_int64_t, c_double, ephg_rate_request
+       type(c_ptr), value :: h, g2
+       type(ephg_rate_request), intent(in) :: req
+       integer(c_int64_t), value :: mode, nv
+       real(c_double), value :: thres
+     end function ephg_g2_average_degenerate
 
      integer(c_int) function ephg_el_wann_noalloc(h, nk, kvecs, energies, evecs) &
           bind(C, name="ephg_el_wann_noalloc")

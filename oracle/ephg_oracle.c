@@ -220,10 +220,14 @@ int or_herm_eig(int64_t n, double *A_in, double *w, double *V_out) {
 void or_el_wann(const or_wannier *w, int64_t nk, const double *kvecs, double *energies,
                 double *evecs, double *velocities, const double *scissor) {
   const int64_t nw = w->nw, nwsk = w->nwsk;
+  /* the k-points are independent: OpenMP over them, buffers per thread */
+#pragma omp parallel
+  {
   double *H = (double *)malloc(sizeof(double) * 2 * nw * nw);
   double *dH = (double *)malloc(sizeof(double) * 2 * 3 * nw * nw);
   double *V = (double *)malloc(sizeof(double) * 2 * nw * nw);
   double *ev = (double *)malloc(sizeof(double) * nw);
+#pragma omp for schedule(dynamic, 16)
   for (int64_t ik = 0; ik < nk; ++ik) {
     cplx *Hc = (cplx *)calloc(nw * nw, sizeof(cplx));
     cplx *dHc = (cplx *)calloc(3 * nw * nw, sizeof(cplx));
@@ -272,6 +276,7 @@ void or_el_wann(const or_wannier *w, int64_t nk, const double *kvecs, double *en
     free(Hc); free(dHc);
   }
   free(H); free(dH); free(V); free(ev);
+  }
 }
 
 /* ws_wrapping_vectors: wannier.f90:532-582.  Returns the number of wrappers.
@@ -477,7 +482,35 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
   double *Dd = (double *)malloc(sizeof(double) * 2 * nb * nb);
   double *V = (double *)malloc(sizeof(double) * 2 * nb * nb * 3);
   double *om2 = (double *)malloc(sizeof(double) * nb);
-  int64_t wr[3 * 512];
+  /* ws_wrapping_vectors depends on the cell and the atom pair, not on q: the
+   * reference calls it per q (:642); here it runs once per call, with the same
+   * wrappers in the same order, so every sum below is unchanged */
+  const int64_t npair = nwsq * nat * nat;
+  int *wn = (int *)malloc(sizeof(int) * npair);
+  int64_t *woff = (int64_t *)malloc(sizeof(int64_t) * (npair + 1));
+  int64_t wcap = 8 * npair + 512, wtot = 0;
+  int64_t *wall = (int64_t *)malloc(sizeof(int64_t) * 3 * wcap);
+  {
+    int64_t wr[3 * 512];
+    for (int64_t iuc = 0; iuc < nwsq; ++iuc)
+      for (int64_t jat = 0; jat < nat; ++jat)
+        for (int64_t iat = 0; iat < nat; ++iat) {
+          double dist[3];
+          for (int d = 0; d < 3; ++d)
+            dist[d] = ((double)w->rcells_q[iuc + nwsq * d] - w->basis[d + 3 * iat] + w->basis[d + 3 * jat]) /
+                      (double)w->coarse_qmesh[d];
+          const int64_t pi = iat + nat * (jat + nat * iuc);
+          int nwrap = or_ws_wrapping_vectors(w->lattvecs, dist, 1.0e-6, wr, 512);
+          if (wtot + nwrap > wcap) {
+            wcap = 2 * (wtot + nwrap);
+            wall = (int64_t *)realloc(wall, sizeof(int64_t) * 3 * wcap);
+          }
+          wn[pi] = nwrap;
+          woff[pi] = wtot;
+          for (int i = 0; i < 3 * nwrap; ++i) wall[3 * wtot + i] = wr[i];
+          wtot += nwrap;
+        }
+  }
   for (int64_t iq = 0; iq < nq; ++iq) {
     for (int64_t i = 0; i < nb * nb; ++i) dyn[i] = 0.0;
     for (int64_t i = 0; i < 3 * nb * nb; ++i) ddyn[i] = 0.0;
@@ -485,11 +518,9 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
       for (int64_t i = 0; i < nb * nb; ++i) caux_mat[i] = 0.0;
       for (int64_t jat = 0; jat < nat; ++jat)
         for (int64_t iat = 0; iat < nat; ++iat) {
-          double dist[3];
-          for (int d = 0; d < 3; ++d)
-            dist[d] = ((double)w->rcells_q[iuc + nwsq * d] - w->basis[d + 3 * iat] + w->basis[d + 3 * jat]) /
-                      (double)w->coarse_qmesh[d];
-          int nwrap = or_ws_wrapping_vectors(w->lattvecs, dist, 1.0e-6, wr, 512);
+          const int64_t pi = iat + nat * (jat + nat * iuc);
+          const int nwrap = wn[pi];
+          const int64_t *wr = wall + 3 * woff[pi];
           for (int iw = 0; iw < nwrap; ++iw) {
             double dot = 0.0;
             for (int d = 0; d < 3; ++d)
@@ -582,6 +613,7 @@ int or_ph_wann(const or_wannier *w, int64_t nq, const double *qvecs, double *ene
     }
   }
   free(caux_mat); free(dyn); free(ddyn); free(Dd); free(V); free(om2);
+  free(wn); free(woff); free(wall);
   return status;
 }
 
@@ -590,19 +622,24 @@ void or_gkRp(const or_wannier *w, const double kvec[3], double *gmixed) {
   const int64_t nw = w->nw, nb = w->nb, nwsk = w->nwsk, nwsg = w->nwsg;
   const int64_t blk = nw * nw * nb;
   cplx *acc = (cplx *)calloc(blk * w->nwsq, sizeof(cplx));
+  cplx *caux = (cplx *)malloc(sizeof(cplx) * nwsk);
   for (int64_t iuc = 0; iuc < nwsk; ++iuc) {
     double dot = 0.0;
     for (int d = 0; d < 3; ++d) dot += kvec[d] * (double)w->rcells_k[iuc + nwsk * d];
-    cplx caux = expi(TWOPI * dot) / (double)w->elwsdeg[iuc];
-    for (int64_t rp = 0; rp < nwsg; ++rp)
+    caux[iuc] = expi(TWOPI * dot) / (double)w->elwsdeg[iuc];
+  }
+  /* the Rp blocks are independent: OpenMP over them, each element still summed over Re in order */
+#pragma omp parallel for schedule(static)
+  for (int64_t rp = 0; rp < nwsg; ++rp)
+    for (int64_t iuc = 0; iuc < nwsk; ++iuc)
       for (int64_t s = 0; s < nb; ++s)
         for (int64_t j = 0; j < nw; ++j)
           for (int64_t i = 0; i < nw; ++i)
             acc[i + nw * (j + nw * (s + nb * rp))] +=
-                caux * cget(w->gwann, i + nw * (j + nw * (iuc + nwsk * (s + nb * rp))));
-  }
+                caux[iuc] * cget(w->gwann, i + nw * (j + nw * (iuc + nwsk * (s + nb * rp))));
   for (int64_t i = 0; i < blk * w->nwsq; ++i) cset(gmixed, i, acc[i]);
   free(acc);
+  free(caux);
 }
 
 /* gReq: wannier.f90:1134-1188 (gmixed(nw,nw,nb,nwsk)) */
@@ -1238,6 +1275,98 @@ or_rates_ctx *or_rates_setup_sym(const or_wannier *w, const or_request *req, int
   cx->dc = dc;
   cx->us_setup = (int64_t)(wall_us() - t_start);
   return cx;
+}
+
+/* One group of a degenerate-subspace pass: c values v[0], v[st], ..., with
+ * energies e[0..c-1].  mode 0 restates the reference's loop literally, in
+ * place: member a becomes the mean over the members b with |e_a - e_b| <
+ * thres, summed in member order, of the values as they are at that moment, so
+ * later members see their predecessors' new values (wannier.f90:1335-1347,
+ * 1352-1364, 1369-1381).  mode 1: the same means, all of them taken from the
+ * values before the pass. */
+void or_degenerate_group(int mode, double thres, int64_t c, double *v, int64_t st, const double *e, double *tmp) {
+  for (int64_t a = 0; a < c; ++a) tmp[a] = v[a * st];
+  for (int64_t a = 0; a < c; ++a) {
+    int64_t cnt = 0;
+    double aux = 0.0;
+    for (int64_t b = 0; b < c; ++b)
+      if (fabs(e[a] - e[b]) < thres) {
+        ++cnt;
+        aux += mode == 0 ? v[b * st] : tmp[b];
+      }
+    v[a * st] = aux / (double)cnt;
+  }
+}
+
+/* Degenerate-subspace averaging of |g|^2 (plot_along_path, wannier.f90:1332-
+ * 1384; the same loops in test/check_interactions_symmetries.f90:330-384),
+ * applied to the vertex list of or_rates_run over every in-window initial
+ * state: (state j, final state f = (k', n), branch s), per_state = nin * nb
+ * entries per state.  Three passes in the reference's order: over phonon
+ * branches s of q = k' - k (|omega_s - omega_s'| < thres, eV); over the initial
+ * bands m of each k (with k', n, s fixed); over the final bands n of each k'
+ * (with the state and s fixed).  The band groups are the window bands, the
+ * only ones the list holds.  Returns 1 if nv is not the list's length. */
+int or_average_degenerate(or_rates_ctx *cx, int mode, double thres, double *g2, int64_t nv) {
+  const or_wannier *w = cx->w;
+  const or_request *req = &cx->req;
+  const int64_t nw = w->nw, nb = w->nb, nwv = cx->nwv, N = cx->N;
+  const int64_t *mesh = req->mesh;
+  const double *ens = cx->ens, *phe = cx->phe;
+  int64_t *sk = (int64_t *)malloc(sizeof(int64_t) * nwv * nw), *sm = (int64_t *)malloc(sizeof(int64_t) * nwv * nw);
+  int64_t nst = 0;
+  for (int64_t istate = 1; istate <= nwv * nw; ++istate) {   /* initial states in rank order */
+    int64_t m, ik;
+    or_demux_state(istate, nw, &m, &ik);
+    if (cx->irr_pos && cx->irr_pos[ik - 1] < 0) continue;
+    if (fabs(ens[(ik - 1) + nwv * (m - 1)] - req->enref) > req->fsthick) continue;
+    sk[nst] = ik;
+    sm[nst] = m;
+    ++nst;
+  }
+  int64_t *fcum = (int64_t *)malloc(sizeof(int64_t) * (nwv + 1)), *fn = (int64_t *)malloc(sizeof(int64_t) * nwv * nw);
+  int64_t nin = 0;
+  for (int64_t ikp = 1; ikp <= nwv; ++ikp) {                   /* final states, row-major */
+    fcum[ikp - 1] = nin;
+    for (int64_t n = 1; n <= nw; ++n)
+      if (fabs(ens[(ikp - 1) + nwv * (n - 1)] - req->enref) <= req->fsthick) fn[nin++] = n;
+  }
+  fcum[nwv] = nin;
+  const int64_t per = nin * nb;
+  if (nv != nst * per) {
+    free(sk); free(sm); free(fcum); free(fn);
+    return 1;
+  }
+  const int64_t gmax = nw > nb ? nw : nb;
+  double *e = (double *)malloc(sizeof(double) * gmax), *tmp = (double *)malloc(sizeof(double) * gmax);
+  double prim[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  /* 1. phonon branches, per (state, final state) */
+  for (int64_t j = 0; j < nst; ++j)
+    for (int64_t ikp = 1; ikp <= nwv; ++ikp) {
+      int64_t qi[3], iq;
+      double qf[3], qc[3];
+      or_vector_addsub(cx->indexlist[ikp - 1], cx->indexlist[sk[j] - 1], -1, mesh, prim, qi, &iq, qf, qc);
+      for (int64_t s = 0; s < nb; ++s) e[s] = phe[(iq - 1) + N * s];
+      for (int64_t f = fcum[ikp - 1]; f < fcum[ikp]; ++f) or_degenerate_group(mode, thres, nb, g2 + j * per + f * nb, 1, e, tmp);
+    }
+  /* 2. initial bands, per (k, final state, s): the states of one k are consecutive */
+  for (int64_t j0 = 0; j0 < nst;) {
+    int64_t j1 = j0;
+    while (j1 < nst && sk[j1] == sk[j0]) ++j1;
+    for (int64_t j = j0; j < j1; ++j) e[j - j0] = ens[(sk[j] - 1) + nwv * (sm[j] - 1)];
+    for (int64_t f = 0; f < nin; ++f)
+      for (int64_t s = 0; s < nb; ++s) or_degenerate_group(mode, thres, j1 - j0, g2 + j0 * per + f * nb + s, per, e, tmp);
+    j0 = j1;
+  }
+  /* 3. final bands, per (state, k', s) */
+  for (int64_t j = 0; j < nst; ++j)
+    for (int64_t ikp = 1; ikp <= nwv; ++ikp) {
+      const int64_t f0 = fcum[ikp - 1], c = fcum[ikp] - f0;
+      for (int64_t f = 0; f < c; ++f) e[f] = ens[(ikp - 1) + nwv * (fn[f0 + f] - 1)];
+      for (int64_t s = 0; s < nb; ++s) or_degenerate_group(mode, thres, c, g2 + j * per + f0 * nb + s, nb, e, tmp);
+    }
+  free(e); free(tmp); free(sk); free(sm); free(fcum); free(fn);
+  return 0;
 }
 
 void or_rates_free(or_rates_ctx *cx) {

@@ -157,6 +157,15 @@ int or_rates_run(or_rates_ctx *cx, int64_t state_begin, int64_t nstates, int nth
                  int literal, double *rates, int64_t *indexlist, int64_t *info,
                  double *g2, double *xp, double *xm, int64_t cap);
 void or_rates_free(or_rates_ctx *cx);
+/* Degenerate-subspace averaging (wannier.f90:1332-1384) of the |g|^2 list of
+ * or_rates_run over all in-window states, in place: phonon branches, then
+ * initial bands, then final bands, each group |E - E'| < thres (eV).  mode 0:
+ * the reference's in-place loops; mode 1: each member the mean of the group's
+ * values before the pass.  Returns 1 if nv is not the list's length. */
+int or_average_degenerate(or_rates_ctx *cx, int mode, double thres, double *g2, int64_t nv);
+/* One group of those passes: c values v[0], v[st], ... with energies e; tmp
+ * holds c doubles of scratch. */
+void or_degenerate_group(int mode, double thres, int64_t c, double *v, int64_t st, const double *e, double *tmp);
 
 /* ---- symmetry (symmetry.f90) ----
  * qrot / rotations: (3,3,n) column-major; indices 1-based muxed. */

@@ -355,6 +355,17 @@ def _request(req):
 
 
 # ---- misc.f90 / vector.f90 restatements ----
+def degenerate_group(values, energies, mode, thres=1e-6):
+    """One group of the degenerate-subspace passes (or_degenerate_group)."""
+    L = lib()
+    L.or_degenerate_group.argtypes = [ct.c_int, ct.c_double, ct.c_int64, c_dp, ct.c_int64, c_dp, c_dp]
+    v = np.array(values, dtype=np.float64, copy=True)
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    tmp = np.zeros(len(v))
+    L.or_degenerate_group(int(mode), float(thres), len(v), _p(v), 1, _p(e), _p(tmp))
+    return v
+
+
 def mux_vector(v, mesh, base):
     a = (ct.c_int64 * 3)(*v)
     m = (ct.c_int64 * 3)(*mesh)
@@ -464,17 +475,38 @@ class RatesRun:
         self.nthreads = nthreads
         self.ctx = L.or_rates_setup(ct.byref(W.s), ct.byref(r), nthreads)
 
-    def run(self, state_begin, nstates, literal=True):
+    def run(self, state_begin, nstates, literal=True, vertices=False):
         N, nw = self.N, self.W.nw
         rates = np.zeros((N, nw), order="F")
         idx = np.zeros(N, dtype=np.int64)
         info = np.zeros(8, dtype=np.int64)
+        cap = 0
+        g2 = xp = xm = None
+        if vertices:   # room for every vertex of the states asked for
+            cap = N * nw * N * nw * self.W.nb if nstates < 0 else nstates * N * nw * self.W.nb
+            g2, xp, xm = np.zeros(cap), np.zeros(cap), np.zeros(cap)
         lib().or_rates_run(self.ctx, state_begin, nstates, self.nthreads, 1 if literal else 0, _p(rates),
-                           _p(idx, c_i64p), _p(info, c_i64p), None, None, None, 0)
+                           _p(idx, c_i64p), _p(info, c_i64p), _p(g2) if vertices else None,
+                           _p(xp) if vertices else None, _p(xm) if vertices else None, cap)
         nwv = int(info[0])
-        return dict(nwv=nwv, nstates_inwindow=int(info[1]), nstates=int(info[2]), vertices=int(info[3]),
-                    status=int(info[5]), us_setup=int(info[6]), us_loop=int(info[7]),
-                    rates=np.asfortranarray(rates[:nwv]), indexlist=idx[:nwv].copy())
+        out = dict(nwv=nwv, nstates_inwindow=int(info[1]), nstates=int(info[2]), vertices=int(info[3]),
+                   status=int(info[5]), us_setup=int(info[6]), us_loop=int(info[7]),
+                   rates=np.asfortranarray(rates[:nwv]), indexlist=idx[:nwv].copy())
+        if vertices:
+            nv = int(info[3])
+            out.update(g2=g2[:nv].copy(), xp=xp[:nv].copy(), xm=xm[:nv].copy())
+        return out
+
+    def average_degenerate(self, g2, mode=1, thres=1e-6):
+        """or_average_degenerate on a copy of an all-states |g|^2 list (mode 0:
+        the reference's in-place loops, wannier.f90:1332-1384; 1: the means of
+        the values before each pass)."""
+        L = lib()
+        L.or_average_degenerate.argtypes = [ct.c_void_p, ct.c_int, ct.c_double, c_dp, ct.c_int64]
+        out = np.array(g2, dtype=np.float64, copy=True)
+        if L.or_average_degenerate(self.ctx, int(mode), float(thres), _p(out), out.size):
+            raise ValueError("the list is not the request's whole vertex list")
+        return out
 
     def run_ph(self, q_begin, nq, spindeg=2):
         """Phonon-side states of the q-points [q_begin, q_begin + nq) (or_ph_rates_run)."""

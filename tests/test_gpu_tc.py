@@ -131,9 +131,10 @@ def test_el_rates_split_vs_fp64_multi_tile():
     assert np.all(g["rates"][~mask] == 0)
 
 
-@pytest.mark.parametrize("nw,natoms", [(24, 2), (32, 2), (32, 4)])
+@pytest.mark.parametrize("nw,natoms", [(24, 2), (32, 2), (32, 4), (32, 6)])
 def test_el_rates_wide_bands_vs_oracle(oracle_lib, nw, natoms):
-    """Wide band sets (nw 24 and 32, nb 6 and 12) through the generic split
+    """Wide band sets (nw 24 and 32, nb 6, 12 and 18 -- the large instance's
+    nw 32 / nb 18 shape) through the generic split
     path (stage-A rotation tiled over modes, the per-row epilogue of that nw)
     and the FP64 form, against the oracle: rates within 1e-6 (split) and 1e-10
     (FP64) relative."""
