@@ -68,7 +68,8 @@ constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
 constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
 constexpr int TMEM_COLS = 512;                        // main re, main im, corr re, corr im (128 each)
-constexpr int GEMM_THREADS = 192;                     // 6 warps
+constexpr int GEMM_EPI_WARPS = 8;                     // two per TMEM lane quadrant
+constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS; // TMA warp, MMA warp, epilogue warps
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
 
@@ -220,6 +221,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
 // -------------------------------------------------------- the GEMM kernel
 struct GemmArgs {
   int mtiles, ntiles, nkb;   // tile counts, K blocks of BK
@@ -298,7 +307,8 @@ struct GroupGemm {
 
 // Warp-specialised 3xTF32 complex GEMM over the tiles [t0, t1) of a tile
 // space, strided by the grid: warp 0 lane 0 issues TMA loads, warp 1 lane 0
-// the MMAs, warps 2..5 drain TMEM.  Every wait is bounded (err).
+// the MMAs, warps 2..9 drain TMEM (two per lane quadrant, one column half
+// each).  Every wait is bounded (err).
 template <class Jobs>
 __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int *err) {
   extern __shared__ uint8_t smem_raw[];
@@ -318,7 +328,7 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 128);
+      mbar_init(&tempty[b], 32 * GEMM_EPI_WARPS);
     }
     mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -423,8 +433,10 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         mbar_wait(drain, 0, err);
       }
     }
-  } else {   // ---- epilogue: warps 2..5, TMEM lane quadrant = warp % 4
+  } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4, columns of half (w - 2) / 4
     const int quad = warp & 3;
+    constexpr int CW = BN / (GEMM_EPI_WARPS / 4);
+    const int cbeg = ((warp - 2) >> 2) * CW;
     const int row = quad * 32 + lane;
     int it = 0;
     for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x, ++it) {
@@ -435,16 +447,18 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
       float *cr = j.Cr + (int64_t)row * j.ldc;
       float *ci = j.Ci + (int64_t)row * j.ldc;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        float vr[16], vi[16], wr[16], wi[16];
-        tmem_ld16(tr + c0, vr);
-        tmem_ld16(tr + BN + c0, vi);
-        tmem_ld16(tr + 2 * BN + c0, wr);
-        tmem_ld16(tr + 3 * BN + c0, wi);
+      for (int c0 = cbeg; c0 < cbeg + CW; c0 += 16) {
+        uint32_t ar[16], ai[16], br[16], bi[16];
+        tmem_ld16_nowait(tr + c0, ar);            // four loads in flight, one wait
+        tmem_ld16_nowait(tr + BN + c0, ai);
+        tmem_ld16_nowait(tr + 2 * BN + c0, br);
+        tmem_ld16_nowait(tr + 3 * BN + c0, bi);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        float vr[16], vi[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          vr[q] += wr[q];
-          vi[q] += wi[q];
+          vr[q] = __uint_as_float(ar[q]) + __uint_as_float(br[q]);
+          vi[q] = __uint_as_float(ai[q]) + __uint_as_float(bi[q]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -1675,14 +1689,17 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
   return acc;
 }
 
-// Tile order of the fused stage B.  Tile t of mpairs x ntiles (m-tile pair,
-// state pair) walks the m-pairs in FB_MBANDS bands, each band over every state
-// pair before the next band starts, so that only a band's phase tiles have to
-// stay in L2 while the state operand streams past (the state operand is read
-// FB_MBANDS times from DRAM, the phase planes once).
-constexpr int FB_MBANDS = 2;
+// Tile order of the fused kernels.  Tile t of mpairs x ntiles (m-tile pair,
+// n-tile) walks the m-pairs in BANDS bands, each band over every n-tile before
+// the next band starts, so that only a band's phase tiles have to stay in L2
+// while the streamed operand (stage B: the state operand; stage A: the
+// g(Re,Rp) planes) passes: it is read BANDS times from DRAM, the phase planes
+// once.
+constexpr int FB_MBANDS = 2;   // stage B
+constexpr int FA_MBANDS = 2;   // stage A (its streamed operand is the g(Re,Rp) planes)
+template <int BANDS>
 __device__ __forceinline__ void fb_tile(int t, int mpairs, int ntiles, int &mp, int &nt) {
-  const int m0 = (mpairs + FB_MBANDS - 1) / FB_MBANDS;
+  const int m0 = (mpairs + BANDS - 1) / BANDS;
   const int band = t / (m0 * ntiles);
   const int r = t - band * m0 * ntiles;
   const int sz = min(m0, mpairs - band * m0);
@@ -1744,7 +1761,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       bool ok = true;
       for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
         int mp, nt;
-        fb_tile(t, mpairs, g.ntiles, mp, nt);
+        fb_tile<FB_MBANDS>(t, mpairs, g.ntiles, mp, nt);
         const int mt = 2 * mp + (int)crank;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -1819,7 +1836,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     int it = 0;
     for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
       int mp, nt;
-      fb_tile(t, mpairs, g.ntiles, mp, nt);
+      fb_tile<FB_MBANDS>(t, mpairs, g.ntiles, mp, nt);
       const int mt = 2 * mp + (int)crank;
       // ---- row and state data, before the accumulators are ready
       const int ip = mt * BM + quad * 32 + lane;      // < MpB
@@ -2160,7 +2177,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       uint32_t phase = 0;
       bool ok = true;
       for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
-        const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
+        int mp, nt;
+        fb_tile<FA_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+        const int mt = 2 * mp + (int)crank;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
           uint8_t *sb = smem + stage * A_STAGE;
@@ -2223,7 +2242,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
     int it = 0;
     for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
-      const int mt = 2 * (t % mpairs) + (int)crank, nt = t / mpairs;
+      int mp, nt;
+      fb_tile<FA_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+      const int mt = 2 * mp + (int)crank;
       const int kpb = nt % g.nkp16, ns = nt / g.nkp16;
       const int col0 = (ns & 7) + 8 * (ns >> 3);      // n' + 8 s'
       const int kp0 = kpb * 16 + half * 8;

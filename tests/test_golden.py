@@ -106,12 +106,13 @@ def test_library_reproduces_golden(name, prec):
 @pytest.mark.parametrize("prec", [_lib.PREC_FP64, _lib.PREC_SPLIT_TF32])
 def test_library_reproduces_golden_ph(name, prec):
     """ephg_ph_rates against the phonon-side fixtures: FP64 1e-10 relative; split
-    1e-5 relative on every rate (+1e-12 of the largest).  A phonon rate is one
-    mode's sum, and the split form's |g|^2 carries an error of ~1e-7 of the
-    crystal's largest coupling (FP32 accumulation), so weakly coupled modes of
-    these small random crystals show up to ~3e-6; the electron rates, summed
-    over all modes, keep 1e-6, as do the phonon rates of the bench workload
-    (test_gpu_ph.test_full_size_split_vs_fp64)."""
+    1e-5 relative on every rate.  A phonon rate is one mode's sum over the k of
+    the mesh; on these small meshes it sums a few hundred vertices, too few for
+    the scatter of the split form's per-vertex |g|^2 error (FP32 accumulation,
+    up to a few 1e-6) to average out, and up to 4e-6 is measured.  The electron
+    rates, summed over all modes, keep 1e-6, as do all the rates of the 24^3
+    bench workloads (test_gpu_ph.test_full_size_split_vs_fp64 and its polar
+    twin)."""
     from elphbolt_gb300.build import build
     from elphbolt_gb300.interactions import ibzq_order
     from elphbolt_gb300.wannier import Wannier
@@ -130,4 +131,4 @@ def test_library_reproduces_golden_ph(name, prec):
     if prec == _lib.PREC_FP64:
         check_ph(out["rates_phe"], g2, y, z, 1e-10, 0.0, 1e-10, 1e-12)
     else:
-        check_ph(out["rates_phe"], g2, y, z, 1e-5, 1e-12, 1e-5, 1e-6)
+        check_ph(out["rates_phe"], g2, y, z, 1e-5, 0.0, 1e-5, 1e-6)

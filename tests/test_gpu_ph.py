@@ -5,13 +5,14 @@ g(Re,q) from gReq, then k, k + q, m, n with the 'el' g2; the library forms the
 same vertices inside the electron-side sweep.  Tolerances:
 - FP64 form: ph-e rates |a-b| <= 1e-10 |b| (+1e-300), |g|^2 and Y per vertex
   1e-10 relative + 1e-12 of the largest;
-- split form: ph-e rates 1e-5 relative + 1e-12 of the largest rate, |g|^2 and
-  Y per vertex 1e-5 relative + 1e-6 of the largest.  The split form's |g|^2
-  error is ~1e-7 of the crystal's largest coupling (FP32 accumulation); a
-  phonon rate is one mode's sum, so the weakly coupled modes of these small
-  random crystals (acoustic branches near Gamma) show up to ~3e-6 relative.
-  On the bench workload every positive phonon rate keeps 1e-6
-  (test_full_size_split_vs_fp64).
+- split form: ph-e rates 1e-5 relative per rate, |g|^2 and Y per vertex 1e-5
+  relative + 1e-6 of the largest.  The split form's per-vertex |g|^2 carries
+  FP32 accumulation errors of up to a few 1e-6 (a bias of ~-2e-7 plus a
+  scatter); a phonon rate is one mode's sum over the k of the mesh, and on
+  these 4^3 / 5^3 meshes it sums a few hundred vertices, too few for the
+  scatter to average out: up to 4e-6 measured.  On the 24^3 bench workloads
+  every positive rate, electron and phonon, keeps 1e-6 relative with no floor
+  (test_full_size_split_vs_fp64, test_full_size_polar_split_vs_fp64).
 """
 import numpy as np
 import pytest
@@ -72,7 +73,7 @@ def test_ph_rates_vs_oracle(W_cache, oracle_lib, name, delta, prec):
             ok, worst = close(g[key][order], o[key], 1e-10, 1e-12)
             assert ok, (key, worst)
     else:
-        ok, worst = close(g["rates_phe"], o["rates_phe"], 1e-5, 1e-12)
+        ok, worst = close(g["rates_phe"], o["rates_phe"], 1e-5, 0.0, 1e-300)
         assert ok, worst
         for key in ("g2", "y"):
             ok, worst = close(g[key][order], o[key], 1e-5, 1e-6)
@@ -137,8 +138,8 @@ def test_ibzq_lists_reference_order(W_cache, oracle_lib):
 
 def test_full_size_split_vs_fp64():
     """The bench workload (nw 8, 6^3 WS sets, 24^3 mesh): split-form ph-e rates
-    against the FP64 form, 1e-6 relative on every rate above 1e-12 of the largest;
-    electron rates of the same sweep against ephg_el_rates."""
+    against the FP64 form, 1e-6 relative on every positive rate; electron
+    rates of the same sweep likewise."""
     from elphbolt_gb300.build import build
     from elphbolt_gb300.wannier import Wannier
     build()
@@ -151,8 +152,29 @@ def test_full_size_split_vs_fp64():
     finally:
         W.deallocate_wannier()
     assert f["vertices"] == s["vertices"] > 10 ** 8
-    ok, worst = close(s["rates_phe"], f["rates_phe"], 1e-6, 1e-12)
-    assert ok, worst
+    mp = f["rates_phe"] > 0
+    assert np.max(np.abs(s["rates_phe"][mp] - f["rates_phe"][mp]) / f["rates_phe"][mp]) < 1e-6
     m = f["rates"] > 0
     assert np.max(np.abs(s["rates"][m] - f["rates"][m]) / f["rates"][m]) < 1e-6
-    assert (f["rates_phe"] > 0).sum() > 0.5 * f["rates_phe"].size
+    assert mp.sum() > 0.5 * f["rates_phe"].size
+
+
+def test_full_size_polar_split_vs_fp64():
+    """The polar SiC-like crystal at the bench size (nw 8, 6^3 WS sets, 24^3
+    mesh, Born charges and dielectric tensor on): both rate sets of one split
+    sweep against the FP64 form, 1e-6 relative on every positive rate."""
+    from elphbolt_gb300.build import build
+    from elphbolt_gb300.wannier import Wannier
+    build()
+    wd = S.make_wannier(S.make_crystal_sic_like(), 8, supercell=(6, 6, 6), seed=20260105)
+    req = S.si_like_request(wd, (24, 24, 24))
+    W = Wannier(wd)
+    try:
+        f = W.ph_rates(req, precision=_lib.PREC_FP64, electrons=True)
+        s = W.ph_rates(req, precision=_lib.PREC_SPLIT_TF32, electrons=True)
+    finally:
+        W.deallocate_wannier()
+    mp, m = f["rates_phe"] > 0, f["rates"] > 0
+    assert mp.sum() > 0.5 * f["rates_phe"].size
+    assert np.max(np.abs(s["rates_phe"][mp] - f["rates_phe"][mp]) / f["rates_phe"][mp]) < 1e-6
+    assert np.max(np.abs(s["rates"][m] - f["rates"][m]) / f["rates"][m]) < 1e-6
