@@ -68,7 +68,7 @@ constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
 constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
 constexpr int TMEM_COLS = 512;                        // main re, main im, corr re, corr im (128 each)
-constexpr int GEMM_EPI_WARPS = 8;                     // two per TMEM lane quadrant
+constexpr int GEMM_EPI_WARPS = 4;                     // one per TMEM lane quadrant
 constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS; // TMA warp, MMA warp, epilogue warps
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
@@ -307,8 +307,9 @@ struct GroupGemm {
 
 // Warp-specialised 3xTF32 complex GEMM over the tiles [t0, t1) of a tile
 // space, strided by the grid: warp 0 lane 0 issues TMA loads, warp 1 lane 0
-// the MMAs, warps 2..9 drain TMEM (two per lane quadrant, one column half
-// each).  Every wait is bounded (err).
+// the MMAs, the GEMM_EPI_WARPS warps after them drain TMEM (with more than
+// four, each lane quadrant's columns are split between its warps; four
+// measured fastest).  Every wait is bounded (err).
 template <class Jobs>
 __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int *err) {
   extern __shared__ uint8_t smem_raw[];
@@ -433,7 +434,7 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         mbar_wait(drain, 0, err);
       }
     }
-  } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4, columns of half (w - 2) / 4
+  } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4, column block (w - 2) / 4
     const int quad = warp & 3;
     constexpr int CW = BN / (GEMM_EPI_WARPS / 4);
     const int cbeg = ((warp - 2) >> 2) * CW;
