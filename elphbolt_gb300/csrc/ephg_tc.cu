@@ -29,8 +29,6 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
-#include <atomic>
-#include <map>
 #include <condition_variable>
 #include <mutex>
 #include <cmath>
@@ -68,21 +66,11 @@ constexpr int BN = 128;          // tile columns per accumulator (UMMA N)
 constexpr int BK = 16;           // K per stage: 16 fp32 = 64 B rows, SWIZZLE_64B
 constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
+constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
 constexpr int TMEM_COLS = 512;                        // main re, main im, corr re, corr im (128 each)
 constexpr int GEMM_EPI_WARPS = 4;                     // one per TMEM lane quadrant
 constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS; // TMA warp, MMA warp, epilogue warps
-// The generic GEMM comes in two tile widths.  TBN = 128: one set of four
-// 128-column accumulators fills TMEM, so the MMAs of the next tile wait while
-// the epilogue drains.  TBN = 64: two sets of four 64-column accumulators, so
-// the next tile's MMAs run while the previous one drains, at the price of
-// 1.5x the shared-memory operand reads per flop; four 48 KB stages.
-template <int TBN> struct GemmShape {
-  static constexpr int BPLANE = TBN * BK * 4;                 // one B plane of a stage
-  static constexpr int STAGE = 4 * PLANE_BYTES + 4 * BPLANE;
-  static constexpr int NSTAGE = TBN == BN ? STAGES : 4;
-  static constexpr int NBUF = TBN == BN ? 1 : 2;             // TMEM accumulator sets
-  static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;
-};
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
 
 // ------------------------------------------------------------ PTX helpers
@@ -244,7 +232,6 @@ __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t *r) {
 // -------------------------------------------------------- the GEMM kernel
 struct GemmArgs {
   int mtiles, ntiles, nkb;   // tile counts, K blocks of BK
-  int bn;                    // tile width: BN or BN / 2 (gemm_width)
   int t0, t1;                // tiles [t0, t1) of this launch
   int64_t Astride, Bstride;  // rows between consecutive planes of the A / B stacks
   int64_t Aoff, Boff;        // first row of the operand inside plane 0
@@ -270,11 +257,11 @@ __host__ __device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, cons
   j.tA = tA;
   j.tB = tB;
   j.arow = (int)(g.Aoff + (int64_t)mt * BM);
-  j.brow = (int)(g.Boff + (int64_t)nt * g.bn);
+  j.brow = (int)(g.Boff + (int64_t)nt * BN);
   j.nkb = g.nkb;
   j.Astride = (int)g.Astride;
   j.Bstride = (int)g.Bstride;
-  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * g.bn;
+  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * BN;
   j.Cr = g.Cr + off;
   j.Ci = g.Ci + off;
   j.ldc = g.ldc;
@@ -323,22 +310,20 @@ struct GroupGemm {
 // the MMAs, the GEMM_EPI_WARPS warps after them drain TMEM (with more than
 // four, each lane quadrant's columns are split between its warps; four
 // measured fastest).  Every wait is bounded (err).
-template <class Jobs, int TBN>
+template <class Jobs>
 __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int *err) {
-  using G = GemmShape<TBN>;
-  constexpr int NST = G::NSTAGE;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *full = (uint64_t *)(smem + NST * G::STAGE);
-  uint64_t *empty = full + NST;
-  uint64_t *tfull = empty + NST;
+  uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *tfull = empty + STAGES;
   uint64_t *tempty = tfull + 2;
   uint64_t *drain = tempty + 2;
   uint32_t *tslot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < NST; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -379,47 +364,44 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         }
         for (int kb = 0; kb < j.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, err)) { ok = false; break; }
-          uint8_t *sb = smem + stage * G::STAGE;
-          mbar_expect_tx(&full[stage], G::STAGE);
+          uint8_t *sb = smem + stage * STAGE_BYTES;
+          mbar_expect_tx(&full[stage], STAGE_BYTES);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
             tma_load_2d_hint(sb + p * PLANE_BYTES, j.tA, &full[stage], kb * BK, p * j.Astride + j.arow, keep);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
-            tma_load_2d(sb + 4 * PLANE_BYTES + p * G::BPLANE, j.tB, &full[stage], kb * BK, p * j.Bstride + j.brow);
-          if (++stage == NST) { stage = 0; phase ^= 1; }
+            tma_load_2d(sb + (4 + p) * PLANE_BYTES, j.tB, &full[stage], kb * BK, p * j.Bstride + j.brow);
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       }
       // drain: wait until every issued stage has landed before the CTA can exit
-      for (int s = 0; s < NST; ++s) mbar_wait(&empty[stage], phase ^ 1, err), stage = (stage + 1) % NST,
-                                      phase ^= (stage == 0);
+      for (int s = 0; s < STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, err), stage = (stage + 1) % STAGES,
+                                         phase ^= (stage == 0);
     }
   } else if (warp == 1) {
     if (lane == 0) {   // ---- MMA issuer
-      constexpr uint32_t IDP = idesc_tf32_n(false, TBN), IDN = idesc_tf32_n(true, TBN);
+      constexpr uint32_t IDP = idesc_tf32(false), IDN = idesc_tf32(true);
       int stage = 0;
       uint32_t phase = 0;
       int it = 0;
       bool ok = true;
+      const uint32_t mr = tmem, mi = tmem + BN, cr = tmem + 2 * BN, ci = tmem + 3 * BN;
       for (int t = t0 + blockIdx.x; t < t1 && ok; t += gridDim.x, ++it) {
         const int nkb = jobs(t).nkb;
-        const int buf = G::NBUF == 1 ? 0 : (it & 1), use = it / G::NBUF;
-        const uint32_t base = tmem + (uint32_t)(buf * 4 * TBN);
-        const uint32_t mr = base, mi = base + TBN, cr = base + 2 * TBN, ci = base + 3 * TBN;
-        if (!mbar_wait(&tempty[buf], (use & 1) ^ 1, err)) { ok = false; break; }
+        if (!mbar_wait(&tempty[0], (it & 1) ^ 1, err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nkb; ++kb) {
           if (!mbar_wait(&full[stage], phase, err)) { ok = false; break; }
           tc_fence_after();
-          uint8_t *sb = smem + stage * G::STAGE;
-          uint8_t *bb = sb + 4 * PLANE_BYTES;
+          uint8_t *sb = smem + stage * STAGE_BYTES;
 #pragma unroll
           for (int ks = 0; ks < BK / 8; ++ks) {
             const int off = ks * 32;   // 8 tf32 = 32 B along K inside the swizzle atom
             const uint64_t Ahr = sdesc(sb + 0 * PLANE_BYTES + off), Ahi = sdesc(sb + 1 * PLANE_BYTES + off);
             const uint64_t Alr = sdesc(sb + 2 * PLANE_BYTES + off), Ali = sdesc(sb + 3 * PLANE_BYTES + off);
-            const uint64_t Bhr = sdesc(bb + 0 * G::BPLANE + off), Bhi = sdesc(bb + 1 * G::BPLANE + off);
-            const uint64_t Blr = sdesc(bb + 2 * G::BPLANE + off), Bli = sdesc(bb + 3 * G::BPLANE + off);
+            const uint64_t Bhr = sdesc(sb + 4 * PLANE_BYTES + off), Bhi = sdesc(sb + 5 * PLANE_BYTES + off);
+            const uint64_t Blr = sdesc(sb + 6 * PLANE_BYTES + off), Bli = sdesc(sb + 7 * PLANE_BYTES + off);
             const uint32_t acc = (kb == 0 && ks == 0) ? 0u : 1u;
             // corrections: hi*lo + lo*hi
             umma(cr, Ahr, Blr, IDP, acc);
@@ -442,9 +424,9 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
             umma(di, Ahi, Bhr, IDP, 1);
           }
           umma_commit(&empty[stage]);     // frees the smem stage when these MMAs retire
-          if (++stage == NST) { stage = 0; phase ^= 1; }
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
-        if (ok) umma_commit(&tfull[buf]);   // accumulators ready for the epilogue
+        if (ok) umma_commit(&tfull[0]);   // accumulators ready for the epilogue
       }
       // a wait gave up: let the MMAs already issued retire before TMEM is freed
       if (!ok) {
@@ -454,25 +436,24 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
     }
   } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4, column block (w - 2) / 4
     const int quad = warp & 3;
-    constexpr int CW = TBN / (GEMM_EPI_WARPS / 4);
+    constexpr int CW = BN / (GEMM_EPI_WARPS / 4);
     const int cbeg = ((warp - 2) >> 2) * CW;
     const int row = quad * 32 + lane;
     int it = 0;
     for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x, ++it) {
       const TileJob j = jobs(t);
-      const int buf = G::NBUF == 1 ? 0 : (it & 1), use = it / G::NBUF;
-      if (!mbar_wait(&tfull[buf], use & 1, err)) break;
+      if (!mbar_wait(&tfull[0], it & 1, err)) break;
       tc_fence_after();
-      const uint32_t tr = tmem + (uint32_t)(buf * 4 * TBN) + ((uint32_t)(quad * 32) << 16);
+      const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
       float *cr = j.Cr + (int64_t)row * j.ldc;
       float *ci = j.Ci + (int64_t)row * j.ldc;
 #pragma unroll 1
       for (int c0 = cbeg; c0 < cbeg + CW; c0 += 16) {
         uint32_t ar[16], ai[16], br[16], bi[16];
         tmem_ld16_nowait(tr + c0, ar);            // four loads in flight, one wait
-        tmem_ld16_nowait(tr + TBN + c0, ai);
-        tmem_ld16_nowait(tr + 2 * TBN + c0, br);
-        tmem_ld16_nowait(tr + 3 * TBN + c0, bi);
+        tmem_ld16_nowait(tr + BN + c0, ai);
+        tmem_ld16_nowait(tr + 2 * BN + c0, br);
+        tmem_ld16_nowait(tr + 3 * BN + c0, bi);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         float vr[16], vi[16];
 #pragma unroll
@@ -488,7 +469,7 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         }
       }
       tc_fence_before();
-      mbar_arrive(&tempty[buf]);
+      mbar_arrive(&tempty[0]);
     }
   }
   __syncthreads();
@@ -498,18 +479,15 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
   }
 }
 
-template <int TBN>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_cgemm_3xtf32(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, GemmArgs g) {
-  cgemm_body<OneGemm, TBN>(OneGemm{&tA, &tB, &g}, g.t0, g.t1, g.err);
+  cgemm_body(OneGemm{&tA, &tB, &g}, g.t0, g.t1, g.err);
 }
 
-// The grouped form: the GEMMs of many rate requests in one persistent launch
-// (every problem of the launch has the tile width TBN).
-template <int TBN>
+// The grouped form: the GEMMs of many rate requests in one persistent launch.
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_cgemm_group(const GroupProblem *tab, int np, int t0, int t1, int *err) {
-  cgemm_body<GroupGemm, TBN>(GroupGemm{tab, np}, t0, t1, err);
+  cgemm_body(GroupGemm{tab, np}, t0, t1, err);
 }
 
 // -------------------------------------------------------- tensor maps
@@ -615,51 +593,38 @@ class GemmBatcher {
   // one round (under the gate's lock): table upload, the grouped launch, and the
   // members' streams made to wait for it
   int launch_round(std::vector<std::pair<int, Pend>> &pend) {
-    // by tile width (one launch per width), and within a width the heaviest
-    // tiles (most K blocks) first: the strided tile order then ends on light tiles
+    // heaviest tiles (most K blocks) first: the strided tile order then ends on light tiles
     std::stable_sort(pend.begin(), pend.end(),
                      [](const std::pair<int, Pend> &a, const std::pair<int, Pend> &b) {
-                       if (a.second.p.g.bn != b.second.p.g.bn) return a.second.p.g.bn > b.second.p.g.bn;
                        return a.second.p.g.nkb > b.second.p.g.nkb;
                      });
     const int np = (int)pend.size();
     const int slot = (int)(nround_++ % kRing);
     GroupProblem *h = htab_ + (size_t)slot * cap_, *d = dtab_ + (size_t)slot * cap_;
     cudaEventSynchronize(slot_ev_[slot]);   // the copy that last read this staging slot has run
-    int64_t T = 0, Tw = 0;
-    int rc = 0;
+    int64_t T = 0;
     for (int i = 0; i < np; ++i) {
       h[i] = pend[i].second.p;
-      if (i > 0 && h[i].g.bn != h[i - 1].g.bn) Tw = 0;   // tile numbering per launch
-      h[i].tile0 = (int)Tw;
-      const int64_t n = (int64_t)h[i].g.mtiles * h[i].g.ntiles;
-      Tw += n;
-      T += n;
-      if (Tw > INT32_MAX) rc = tfail(1, "batch: too many tiles in one round");
+      h[i].tile0 = (int)T;
+      T += (int64_t)h[i].g.mtiles * h[i].g.ntiles;
     }
+    int rc = 0;
+    if (T > INT32_MAX) rc = tfail(1, "batch: too many tiles in one round");
     for (int i = 0; i < np && !rc; ++i)
       if (cudaStreamWaitEvent(gst_, ready_[pend[i].first], 0) != cudaSuccess)
         rc = tfail(2, "batch: stream wait failed");
     if (!rc && cudaMemcpyAsync(d, h, sizeof(GroupProblem) * np, cudaMemcpyHostToDevice, gst_) != cudaSuccess)
       rc = tfail(2, "batch: problem table upload failed");
-    if (!rc) cudaEventRecord(slot_ev_[slot], gst_);
-    for (int i0 = 0; i0 < np && !rc;) {   // one launch per tile width
-      int i1 = i0;
-      int64_t Tn = 0;
-      while (i1 < np && h[i1].g.bn == h[i0].g.bn) Tn += (int64_t)h[i1].g.mtiles * h[i1].g.ntiles, ++i1;
-      const int grid = (int)std::min<int64_t>(Tn, num_sms());
-      if (h[i0].g.bn == BN)
-        k_cgemm_group<BN><<<grid, GEMM_THREADS, GemmShape<BN>::SMEM, gst_>>>(d + i0, i1 - i0, 0, (int)Tn, derr_);
-      else
-        k_cgemm_group<BN / 2><<<grid, GEMM_THREADS, GemmShape<BN / 2>::SMEM, gst_>>>(d + i0, i1 - i0, 0, (int)Tn,
-                                                                                      derr_);
+    if (!rc) {
+      cudaEventRecord(slot_ev_[slot], gst_);
+      const int grid = (int)std::min<int64_t>(T, num_sms());
+      k_cgemm_group<<<grid, GEMM_THREADS, SMEM_BYTES, gst_>>>(d, np, 0, (int)T, derr_);
       if (cudaGetLastError() != cudaSuccess) rc = tfail(2, "batch: grouped GEMM launch failed");
-      ++launches_;
-      i0 = i1;
     }
     if (!rc && cudaEventRecord(done_, gst_) != cudaSuccess) rc = tfail(2, "batch: event record failed");
     for (auto &q : pend)
       if (!rc && cudaStreamWaitEvent(q.second.st, done_, 0) != cudaSuccess) rc = tfail(2, "batch: stream wait failed");
+    ++launches_;
     problems_ += np;
     tiles_ += T;
     max_group_ = std::max<int64_t>(max_group_, np);
@@ -681,9 +646,7 @@ GemmBatcher *batcher_create(int nmembers) {
   if (nmembers <= 0) return nullptr;
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(k_cgemm_group<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmShape<BN>::SMEM);
-    cudaFuncSetAttribute(k_cgemm_group<BN / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         GemmShape<BN / 2>::SMEM);
+    cudaFuncSetAttribute(k_cgemm_group, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
   });
   GemmBatcher *b = new GemmBatcher(nmembers);
   if (!b->ok()) {
@@ -700,72 +663,6 @@ void batcher_stats(const GemmBatcher *b, int64_t *launches, int64_t *problems, i
   b->stats(launches, problems, tiles, max_group);
 }
 
-// ------------------------------------------------- tile-width autotuner
-// Per problem class -- K blocks, and the row and column tile counts rounded up
-// to powers of two -- the first GEMM of the class runs once with each tile
-// width on its own stream, timed with CUDA events, and the class keeps the
-// faster width from then on.  The second run rewrites the first one's output
-// with the same values: an output element is the same chain of MMAs whichever
-// the width.  A batch member's GEMM is timed this way before it joins its
-// grouped launch.  ephg_debug_set_gemm_width can force a width (tests).
-class WidthTuner {
- public:
-  int get(uint64_t key) {
-    std::lock_guard<std::mutex> l(mu_);
-    auto it = m_.find(key);
-    return it == m_.end() ? 0 : it->second;
-  }
-  void set(uint64_t key, int w, float ms128, float ms64) {
-    std::lock_guard<std::mutex> l(mu_);
-    if (m_.emplace(key, w).second) {
-      (w == BN ? n128_ : n64_)++;
-      ms128_ += ms128;
-      ms64_ += ms64;
-    }
-  }
-  void stats(int64_t *n128, int64_t *n64, double *ms128, double *ms64) {
-    std::lock_guard<std::mutex> l(mu_);
-    *n128 = n128_, *n64 = n64_, *ms128 = ms128_, *ms64 = ms64_;
-  }
-  std::atomic<int> force{0};
-
- private:
-  std::mutex mu_;
-  std::map<uint64_t, int> m_;
-  int64_t n128_ = 0, n64_ = 0;
-  double ms128_ = 0, ms64_ = 0;
-};
-static WidthTuner g_tuner;
-
-static inline uint64_t ceil_log2(int64_t x) {
-  uint64_t l = 0;
-  while (((int64_t)1 << l) < x) ++l;
-  return l;
-}
-
-static void gemm_attrs_once() {
-  // once per process: changing a kernel attribute can wait for the device's queued work
-  static std::once_flag attr_once;
-  std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(k_cgemm_3xtf32<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmShape<BN>::SMEM);
-    cudaFuncSetAttribute(k_cgemm_3xtf32<BN / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         GemmShape<BN / 2>::SMEM);
-  });
-}
-
-// the tiles [t0, t1) of one GEMM at width w on stream st
-static int launch_width(int w, const CUtensorMap &ta, const CUtensorMap &tb, GemmArgs g, int t0, int t1, int grid,
-                        cudaStream_t st) {
-  g.t0 = t0;
-  g.t1 = t1;
-  if (w == BN)
-    k_cgemm_3xtf32<BN><<<grid, GEMM_THREADS, GemmShape<BN>::SMEM, st>>>(ta, tb, g);
-  else
-    k_cgemm_3xtf32<BN / 2><<<grid, GEMM_THREADS, GemmShape<BN / 2>::SMEM, st>>>(ta, tb, g);
-  TCK(cudaGetLastError());
-  return 0;
-}
-
 // C[Mp][ldc] (re, im planes) = A x B^T.  A: planes of Astride rows, rows
 // [Aoff, Aoff + Mp) of each; B: planes of Bstride rows, rows [Boff, Boff + Np).
 // With a batch member the GEMM joins its batcher's next grouped launch.
@@ -774,10 +671,35 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
                  int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr) {
   if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
   if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
-  gemm_attrs_once();
+  if (bm && bm->gb) {
+    GroupProblem p;
+    memset(&p, 0, sizeof p);
+    int rc;
+    if ((rc = make_map(&p.tA, Ap, Kp, 4 * Astride)) || (rc = make_map(&p.tB, Bp, Kp, 4 * Bstride))) return rc;
+    p.g.mtiles = Mp / BM;
+    p.g.ntiles = Np / BN;
+    p.g.nkb = Kp / BK;
+    p.g.Astride = Astride;
+    p.g.Bstride = Bstride;
+    p.g.Aoff = Aoff;
+    p.g.Boff = Boff;
+    p.g.Cr = Cr;
+    p.g.Ci = Ci;
+    p.g.ldc = ldc;
+    p.g.err = err;
+    return bm->gb->submit(bm->id, p, st);
+  }
+  CUtensorMap ta, tb;
+  int rc;
+  if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 4 * Bstride))) return rc;
+  // once per process: changing a kernel attribute can wait for the device's queued work
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(k_cgemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
   GemmArgs g;
-  memset(&g, 0, sizeof g);
   g.mtiles = Mp / BM;
+  g.ntiles = Np / BN;
   g.nkb = Kp / BK;
   g.Astride = Astride;
   g.Bstride = Bstride;
@@ -787,62 +709,18 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   g.Ci = Ci;
   g.ldc = ldc;
   g.err = err;
-  const uint64_t key = (uint64_t)g.nkb | ceil_log2(g.mtiles) << 20 | ceil_log2(Np / BN) << 28;
-  int w = g_tuner.force.load();
-  if (w == 0) w = g_tuner.get(key);
-  CUtensorMap ta, tb128, tb64;
-  int rc;
-  if ((rc = make_map(&ta, Ap, Kp, 4 * Astride))) return rc;
-  if (w == 0) {   // not timed yet: once with each width
-    if ((rc = make_map(&tb128, Bp, Kp, 4 * Bstride, BN)) || (rc = make_map(&tb64, Bp, Kp, 4 * Bstride, BN / 2)))
-      return rc;
-    cudaEvent_t ev[3];
-    for (auto &e : ev) TCK(cudaEventCreate(&e));
-    float ms[2] = {0.f, 0.f};
-    GemmArgs g2 = g;
-    g2.bn = BN;
-    g2.ntiles = Np / BN;
-    const int T128 = g2.mtiles * g2.ntiles;
-    GemmArgs g3 = g;
-    g3.bn = BN / 2;
-    g3.ntiles = Np / (BN / 2);
-    const int T64 = g3.mtiles * g3.ntiles;
-    rc = cudaEventRecord(ev[0], st) != cudaSuccess;
-    if (!rc) rc = launch_width(BN, ta, tb128, g2, 0, T128, std::min(T128, num_sms()), st);
-    if (!rc) rc = cudaEventRecord(ev[1], st) != cudaSuccess;
-    if (!rc) rc = launch_width(BN / 2, ta, tb64, g3, 0, T64, std::min(T64, num_sms()), st);
-    if (!rc) rc = cudaEventRecord(ev[2], st) != cudaSuccess;
-    if (!rc) rc = cudaEventSynchronize(ev[2]) != cudaSuccess;
-    if (!rc) {
-      cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
-      cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
-      w = ms[1] < ms[0] ? BN / 2 : BN;
-      g_tuner.set(key, w, ms[0], ms[1]);
-    }
-    for (auto &e : ev) cudaEventDestroy(e);
-    if (rc) return tfail(2, "cgemm: timing the tile widths failed");
-    if (!(bm && bm->gb)) return 0;   // the output is complete
-  }
-  g.bn = w;
-  g.ntiles = Np / w;
-  if (bm && bm->gb) {
-    GroupProblem p;
-    memset(&p, 0, sizeof p);
-    if ((rc = make_map(&p.tA, Ap, Kp, 4 * Astride)) || (rc = make_map(&p.tB, Bp, Kp, 4 * Bstride, w))) return rc;
-    p.g = g;
-    return bm->gb->submit(bm->id, p, st);
-  }
-  if ((rc = make_map(&tb128, Bp, Kp, 4 * Bstride, w))) return rc;
   int tiles = g.mtiles * g.ntiles;
   int grid = std::min(tiles, num_sms());
-  // chunk_us > 0: launches of about that length (a 128-wide tile is ~0.4 us per 16 K
-  // positions) so that other streams' kernels get the SMs between them
-  const int per_cta = chunk_us > 0 ? std::max(1, (int)((int64_t)chunk_us * 16 * 5 / 2 / std::max(1, Kp)) * (BN / w))
-                                   : 0;
+  // chunk_us > 0: launches of about that length (a tile is ~0.4 us per 16 K positions) so
+  // that other streams' kernels get the SMs between them
+  const int per_cta = chunk_us > 0 ? std::max(1, (int)((int64_t)chunk_us * 16 * 5 / 2 / std::max(1, Kp))) : 0;
   const int step = per_cta > 0 ? grid * per_cta : tiles;
   for (int t0 = 0; t0 < tiles; t0 += step) {
     if (t0 > 0) yield();
-    if ((rc = launch_width(w, ta, tb128, g, t0, std::min(tiles, t0 + step), grid, st))) return rc;
+    g.t0 = t0;
+    g.t1 = std::min(tiles, t0 + step);
+    k_cgemm_3xtf32<<<grid, GEMM_THREADS, SMEM_BYTES, st>>>(ta, tb, g);
+    TCK(cudaGetLastError());
   }
   return 0;
 }
@@ -2989,25 +2867,6 @@ extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A
 
 extern "C" const char *ephg_debug_last_error(void) { return ephg::tc::last_error(); }
 
-extern "C" int ephg_debug_set_gemm_width(int64_t width) {
-  using namespace ephg::tc;
-  if (width != 0 && width != BN && width != BN / 2) return tfail(1, "debug_set_gemm_width: 0, 64 or 128");
-  g_tuner.force.store((int)width);
-  return 0;
-}
-
-extern "C" int ephg_debug_gemm_widths(int64_t *classes128, int64_t *classes64, double *ms128, double *ms64) {
-  using namespace ephg::tc;
-  int64_t a, b;
-  double x, y;
-  g_tuner.stats(&a, &b, &x, &y);
-  if (classes128) *classes128 = a;
-  if (classes64) *classes64 = b;
-  if (ms128) *ms128 = x;
-  if (ms64) *ms64 = y;
-  return 0;
-}
-
 // The grouped GEMM's tile lookup on the host: np problems of mtiles[i] x
 // ntiles[i] tiles laid out as the batcher lays them out; every tile of the
 // launch is mapped and hits[tile0(i) + mt + mtiles[i] nt] counted.  Returns
@@ -3026,7 +2885,6 @@ extern "C" int ephg_debug_group_tiles(int np, const int *mtiles, const int *ntil
     tab[i].g.Astride = (int64_t)mtiles[i] * BM;
     tab[i].g.Bstride = (int64_t)ntiles[i] * BN;
     tab[i].g.ldc = (int64_t)ntiles[i] * BN;
-    tab[i].g.bn = BN;
     tab[i].tile0 = (int)T;
     T += (int64_t)mtiles[i] * ntiles[i];
   }

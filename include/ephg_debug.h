@@ -22,16 +22,6 @@ int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A, const dou
 /* message of the last failure of the hook */
 const char *ephg_debug_last_error(void);
 
-/* The split form's generic GEMM comes in two tile widths (128 columns, one set
- * of TMEM accumulators; 64 columns, two sets, so that a tile's MMAs overlap the
- * previous tile's drain).  The library times both on the first GEMM of each
- * problem class and keeps the faster (its autotuner).  width 64 or 128 forces
- * one width for every GEMM from then on; 0 returns to the autotuner. */
-int ephg_debug_set_gemm_width(int64_t width);
-/* The autotuner's decisions so far: problem classes that kept each width, and
- * the summed times of the timing runs of each width (ms).  Nullable outputs. */
-int ephg_debug_gemm_widths(int64_t *classes128, int64_t *classes64, double *ms128, double *ms64);
-
 /* The give-up path of the tcgen05 kernels' bounded barrier waits, on its own:
  * one CTA allocates TMEM, waits limit_cycles (0 .. ~4e9 SM cycles) on a
  * barrier that nothing arrives on (arrive != 0: one it arrived on itself),
