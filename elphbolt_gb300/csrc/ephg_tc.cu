@@ -1528,6 +1528,7 @@ __host__ __device__ __forceinline__ int64_t blk32(int64_t i, int nf, int f) {
 
 struct FusedArgs {
   int mtiles, ntiles, nkb;
+  int bands;                  // m-bands of the tile walk (fb_tile)
   int t0, t1;                 // tile pairs [t0, t1) of this launch
   int64_t Astride, Bstride;   // rows between planes of the phase / state operand stacks
   int nwv, nst;
@@ -1691,21 +1692,25 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
 }
 
 // Tile order of the fused kernels.  Tile t of mpairs x ntiles (m-tile pair,
-// n-tile) walks the m-pairs in BANDS bands, each band over every n-tile before
-// the next band starts, so that only a band's phase tiles have to stay in L2
-// while the streamed operand (stage B: the state operand; stage A: the
-// g(Re,Rp) planes) passes: it is read BANDS times from DRAM, the phase planes
-// once.
-constexpr int FB_MBANDS = 2;   // stage B
-constexpr int FA_MBANDS = 2;   // stage A (its streamed operand is the g(Re,Rp) planes)
-template <int BANDS>
-__device__ __forceinline__ void fb_tile(int t, int mpairs, int ntiles, int &mp, int &nt) {
-  const int m0 = (mpairs + BANDS - 1) / BANDS;
+// n-tile) walks the m-pairs in `bands` bands, each band over every n-tile
+// before the next band starts, so that only a band's phase tiles have to stay
+// in L2 while the streamed operand (stage B: the state operand; stage A: the
+// g(Re,Rp) planes) passes: it is read `bands` times from DRAM, the phase planes
+// once.  fused_bands picks the count from the phase planes' size.
+__device__ __forceinline__ void fb_tile(int t, int mpairs, int ntiles, int bands, int &mp, int &nt) {
+  const int m0 = (mpairs + bands - 1) / bands;
   const int band = t / (m0 * ntiles);
   const int r = t - band * m0 * ntiles;
   const int sz = min(m0, mpairs - band * m0);
   mp = band * m0 + r % sz;
   nt = r / sz;
+}
+// One band per 32 MB of phase planes (at most 4): measured at 24^3 (54 MB of
+// planes) 46.8 / 14.8 / 15.7 / 18.2 GB of stage-B DRAM reads for 1 / 2 / 3 / 4
+// bands; at 12^3 (7 MB) one band reads half of what two do.
+static inline int fused_bands(int64_t phase_bytes, int mpairs) {
+  const int64_t b = (phase_bytes + (32ll << 20) - 1) / (32ll << 20);
+  return (int)std::max<int64_t>(1, std::min<int64_t>({b, 4, (int64_t)mpairs}));
 }
 
 // PH: the phonon side too (Y of every vertex into the ph-e rate of its (q, s)).
@@ -1762,7 +1767,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       bool ok = true;
       for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
         int mp, nt;
-        fb_tile<FB_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+        fb_tile(t, mpairs, g.ntiles, g.bands, mp, nt);
         const int mt = 2 * mp + (int)crank;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -1837,7 +1842,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     int it = 0;
     for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
       int mp, nt;
-      fb_tile<FB_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+      fb_tile(t, mpairs, g.ntiles, g.bands, mp, nt);
       const int mt = 2 * mp + (int)crank;
       // ---- row and state data, before the accumulators are ready
       const int ip = mt * BM + quad * 32 + lane;      // < MpB
@@ -2011,6 +2016,7 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   g.mtiles = MpB / BM;
   g.ntiles = (nst + 1) / 2;
   g.nkb = KpB / BK;
+  g.bands = fused_bands(4 * (int64_t)MpB * KpB * 4, g.mtiles / 2);
   g.Astride = MpB;
   g.Bstride = Np2;
   g.nwv = nwv;
@@ -2068,6 +2074,7 @@ __device__ __forceinline__ uint64_t sdesc32(const void *p) {
 
 struct FusedAArgs {
   int mtiles, ntiles, nkb, nkp16;   // nkp16: 16-position blocks of the state operand's K
+  int bands;                        // m-bands of the tile walk (fb_tile)
   int t0, t1;                        // tile pairs [t0, t1) of this launch
   int64_t Astride, Bstride;          // rows between planes: phase operand, stage-A operand
   int KpB;
@@ -2179,7 +2186,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       bool ok = true;
       for (int t = g.t0 + cid; t < g.t1 && ok; t += ncl) {
         int mp, nt;
-        fb_tile<FA_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+        fb_tile(t, mpairs, g.ntiles, g.bands, mp, nt);
         const int mt = 2 * mp + (int)crank;
         for (int kb = 0; kb < g.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.err)) { ok = false; break; }
@@ -2244,7 +2251,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     int it = 0;
     for (int t = g.t0 + cid; t < g.t1; t += ncl, ++it) {
       int mp, nt;
-      fb_tile<FA_MBANDS>(t, mpairs, g.ntiles, mp, nt);
+      fb_tile(t, mpairs, g.ntiles, g.bands, mp, nt);
       const int mt = 2 * mp + (int)crank;
       const int kpb = nt % g.nkp16, ns = nt / g.nkp16;
       const int col0 = (ns & 7) + 8 * (ns >> 3);      // n' + 8 s'
@@ -2326,6 +2333,7 @@ static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA
   g.mtiles = MpA / BM;
   g.ntiles = (int)(NA / BM);
   g.nkb = KpA / A_BK;
+  g.bands = fused_bands(4 * (int64_t)MpA * KpA * 4, g.mtiles / 2);
   g.nkp16 = g.KpB / 16;
   g.Astride = MpA;
   g.Bstride = NA;
