@@ -62,23 +62,15 @@ static int tfail(int code, const char *m) {
 
 // ----------------------------------------------------------------- tiling
 constexpr int BM = 128;          // tile rows (UMMA M)
-constexpr int BN = 128;          // column padding of the GEMM operands
+constexpr int BN = 128;          // tile columns per accumulator (UMMA N)
 constexpr int BK = 16;           // K per stage: 16 fp32 = 64 B rows, SWIZZLE_64B
+constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = BM * BK * 4;              // 8 KB (A and B tiles alike)
-constexpr int TMEM_COLS = 512;
-// The generic GEMM: tiles of 128 rows x GBN complex columns.  The B operand is
-// stored as six TF32 planes (-hi_im, hi_re, hi_im, -lo_im, lo_re, lo_im) so that
-// [re; im] and [-im; re] are adjacent plane pairs: one complex product is two
-// MMAs of N = 2 GBN, (Ar Br | Ar Bi) and (-Ai Bi | Ai Br), into one accumulator
-// (re | im).  Main and correction accumulators take 256 TMEM columns, so two
-// sets fit: the MMAs of a tile run while the epilogue drains the previous one.
-constexpr int GBN = 64;
-constexpr int G_BPLANE = GBN * BK * 4;                  // 4 KB
-constexpr int G_STAGE = 4 * PLANE_BYTES + 6 * G_BPLANE;  // 56 KB
-constexpr int G_STAGES = 4;
-constexpr int GEMM_EPI_WARPS = 4;                     // one per TMEM lane quadrant (the drain assumes four)
+constexpr int STAGE_BYTES = 8 * PLANE_BYTES;          // 4 A planes + 4 B planes
+constexpr int TMEM_COLS = 512;                        // main re, main im, corr re, corr im (128 each)
+constexpr int GEMM_EPI_WARPS = 4;                     // one per TMEM lane quadrant
 constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS; // TMA warp, MMA warp, epilogue warps
-constexpr int SMEM_BYTES = G_STAGES * G_STAGE + 1024 + 256;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s at 2 GHz
 
 // ------------------------------------------------------------ PTX helpers
@@ -265,11 +257,11 @@ __host__ __device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, cons
   j.tA = tA;
   j.tB = tB;
   j.arow = (int)(g.Aoff + (int64_t)mt * BM);
-  j.brow = (int)(g.Boff + (int64_t)nt * GBN);
+  j.brow = (int)(g.Boff + (int64_t)nt * BN);
   j.nkb = g.nkb;
   j.Astride = (int)g.Astride;
   j.Bstride = (int)g.Bstride;
-  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * GBN;
+  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * BN;
   j.Cr = g.Cr + off;
   j.Ci = g.Ci + off;
   j.ldc = g.ldc;
@@ -315,22 +307,23 @@ struct GroupGemm {
 
 // Warp-specialised 3xTF32 complex GEMM over the tiles [t0, t1) of a tile
 // space, strided by the grid: warp 0 lane 0 issues TMA loads, warp 1 lane 0
-// the MMAs, warps 2..5 drain TMEM (warp w reads lane quadrant w % 4).  Tile it
-// of a CTA uses TMEM accumulator set it % 2.  Every wait is bounded (err).
+// the MMAs, the GEMM_EPI_WARPS warps after them drain TMEM (with more than
+// four, each lane quadrant's columns are split between its warps; four
+// measured fastest).  Every wait is bounded (err).
 template <class Jobs>
 __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *full = (uint64_t *)(smem + G_STAGES * G_STAGE);
-  uint64_t *empty = full + G_STAGES;
-  uint64_t *tfull = empty + G_STAGES;
+  uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *tfull = empty + STAGES;
   uint64_t *tempty = tfull + 2;
   uint64_t *drain = tempty + 2;
   uint32_t *tslot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < G_STAGES; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -371,63 +364,69 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         }
         for (int kb = 0; kb < j.nkb; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, err)) { ok = false; break; }
-          uint8_t *sb = smem + stage * G_STAGE;
-          mbar_expect_tx(&full[stage], G_STAGE);
+          uint8_t *sb = smem + stage * STAGE_BYTES;
+          mbar_expect_tx(&full[stage], STAGE_BYTES);
 #pragma unroll
           for (int p = 0; p < 4; ++p)
             tma_load_2d_hint(sb + p * PLANE_BYTES, j.tA, &full[stage], kb * BK, p * j.Astride + j.arow, keep);
 #pragma unroll
-          for (int p = 0; p < 6; ++p)
-            tma_load_2d(sb + 4 * PLANE_BYTES + p * G_BPLANE, j.tB, &full[stage], kb * BK, p * j.Bstride + j.brow);
-          if (++stage == G_STAGES) { stage = 0; phase ^= 1; }
+          for (int p = 0; p < 4; ++p)
+            tma_load_2d(sb + (4 + p) * PLANE_BYTES, j.tB, &full[stage], kb * BK, p * j.Bstride + j.brow);
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       }
       // drain: wait until every issued stage has landed before the CTA can exit
-      for (int s = 0; s < G_STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, err), stage = (stage + 1) % G_STAGES,
-                                           phase ^= (stage == 0);
+      for (int s = 0; s < STAGES; ++s) mbar_wait(&empty[stage], phase ^ 1, err), stage = (stage + 1) % STAGES,
+                                         phase ^= (stage == 0);
     }
   } else if (warp == 1) {
     if (lane == 0) {   // ---- MMA issuer
-      constexpr uint32_t ID2 = idesc_tf32_n(false, 2 * GBN);
+      constexpr uint32_t IDP = idesc_tf32(false), IDN = idesc_tf32(true);
       int stage = 0;
       uint32_t phase = 0;
       int it = 0;
       bool ok = true;
+      const uint32_t mr = tmem, mi = tmem + BN, cr = tmem + 2 * BN, ci = tmem + 3 * BN;
       for (int t = t0 + blockIdx.x; t < t1 && ok; t += gridDim.x, ++it) {
         const int nkb = jobs(t).nkb;
-        const int buf = it & 1;
-        const uint32_t dm = tmem + (uint32_t)(buf * 256), dc = dm + 128;   // main, correction (re | im each)
-        if (!mbar_wait(&tempty[buf], ((it >> 1) & 1) ^ 1, err)) { ok = false; break; }
+        if (!mbar_wait(&tempty[0], (it & 1) ^ 1, err)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nkb; ++kb) {
           if (!mbar_wait(&full[stage], phase, err)) { ok = false; break; }
           tc_fence_after();
-          uint8_t *sb = smem + stage * G_STAGE;
-          uint8_t *bb = sb + 4 * PLANE_BYTES;
+          uint8_t *sb = smem + stage * STAGE_BYTES;
 #pragma unroll
           for (int ks = 0; ks < BK / 8; ++ks) {
             const int off = ks * 32;   // 8 tf32 = 32 B along K inside the swizzle atom
             const uint64_t Ahr = sdesc(sb + 0 * PLANE_BYTES + off), Ahi = sdesc(sb + 1 * PLANE_BYTES + off);
             const uint64_t Alr = sdesc(sb + 2 * PLANE_BYTES + off), Ali = sdesc(sb + 3 * PLANE_BYTES + off);
-            // [hi_re; hi_im], [-hi_im; hi_re], [lo_re; lo_im], [-lo_im; lo_re]
-            const uint64_t BhP = sdesc(bb + 1 * G_BPLANE + off), BhN = sdesc(bb + 0 * G_BPLANE + off);
-            const uint64_t BlP = sdesc(bb + 4 * G_BPLANE + off), BlN = sdesc(bb + 3 * G_BPLANE + off);
+            const uint64_t Bhr = sdesc(sb + 4 * PLANE_BYTES + off), Bhi = sdesc(sb + 5 * PLANE_BYTES + off);
+            const uint64_t Blr = sdesc(sb + 6 * PLANE_BYTES + off), Bli = sdesc(sb + 7 * PLANE_BYTES + off);
             const uint32_t acc = (kb == 0 && ks == 0) ? 0u : 1u;
-            umma(dc, Ahr, BlP, ID2, acc);   // hi x lo
-            umma(dc, Ahi, BlN, ID2, 1);
-            umma(dc, Alr, BhP, ID2, 1);     // lo x hi
-            umma(dc, Ali, BhN, ID2, 1);
-            // hi x hi.  The last K block holds the nearest cells, the largest
-            // terms: they go to the short correction chain, not the long main one.
+            // corrections: hi*lo + lo*hi
+            umma(cr, Ahr, Blr, IDP, acc);
+            umma(cr, Alr, Bhr, IDP, 1);
+            umma(cr, Ahi, Bli, IDN, 1);
+            umma(cr, Ali, Bhi, IDN, 1);
+            umma(ci, Ahr, Bli, IDP, acc);
+            umma(ci, Alr, Bhi, IDP, 1);
+            umma(ci, Ahi, Blr, IDP, 1);
+            umma(ci, Ali, Bhr, IDP, 1);
+            // main: Re = Ar Br - Ai Bi, Im = Ar Bi + Ai Br (hi parts).  The last K
+            // block holds the nearest cells, the largest terms: they go to the
+            // short correction chain instead of the long main chain.
             const bool nearblk = (kb == nkb - 1) && nkb > 1;
-            const uint32_t dd = nearblk ? dc : dm;
-            umma(dd, Ahr, BhP, ID2, nearblk ? 1u : acc);
-            umma(dd, Ahi, BhN, ID2, 1);
+            const uint32_t dr = nearblk ? cr : mr, di = nearblk ? ci : mi;
+            const uint32_t am = nearblk ? 1u : acc;
+            umma(dr, Ahr, Bhr, IDP, am);
+            umma(dr, Ahi, Bhi, IDN, 1);
+            umma(di, Ahr, Bhi, IDP, am);
+            umma(di, Ahi, Bhr, IDP, 1);
           }
           umma_commit(&empty[stage]);     // frees the smem stage when these MMAs retire
-          if (++stage == G_STAGES) { stage = 0; phase ^= 1; }
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
-        if (ok) umma_commit(&tfull[buf]);   // accumulators ready for the epilogue
+        if (ok) umma_commit(&tfull[0]);   // accumulators ready for the epilogue
       }
       // a wait gave up: let the MMAs already issued retire before TMEM is freed
       if (!ok) {
@@ -435,31 +434,32 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         mbar_wait(drain, 0, err);
       }
     }
-  } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4
+  } else {   // ---- epilogue: warp w drains TMEM lane quadrant w % 4, column block (w - 2) / 4
     const int quad = warp & 3;
+    constexpr int CW = BN / (GEMM_EPI_WARPS / 4);
+    const int cbeg = ((warp - 2) >> 2) * CW;
     const int row = quad * 32 + lane;
     int it = 0;
     for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x, ++it) {
       const TileJob j = jobs(t);
-      const int buf = it & 1;
-      if (!mbar_wait(&tfull[buf], (it >> 1) & 1, err)) break;
+      if (!mbar_wait(&tfull[0], it & 1, err)) break;
       tc_fence_after();
-      const uint32_t tr = tmem + (uint32_t)(buf * 256) + ((uint32_t)(quad * 32) << 16);
+      const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
       float *cr = j.Cr + (int64_t)row * j.ldc;
       float *ci = j.Ci + (int64_t)row * j.ldc;
 #pragma unroll 1
-      for (int c0 = 0; c0 < GBN; c0 += 16) {
-        uint32_t mr[16], mi[16], xr[16], xi[16];
-        tmem_ld16_nowait(tr + c0, mr);              // four loads in flight, one wait
-        tmem_ld16_nowait(tr + GBN + c0, mi);
-        tmem_ld16_nowait(tr + 128 + c0, xr);
-        tmem_ld16_nowait(tr + 128 + GBN + c0, xi);
+      for (int c0 = cbeg; c0 < cbeg + CW; c0 += 16) {
+        uint32_t ar[16], ai[16], br[16], bi[16];
+        tmem_ld16_nowait(tr + c0, ar);            // four loads in flight, one wait
+        tmem_ld16_nowait(tr + BN + c0, ai);
+        tmem_ld16_nowait(tr + 2 * BN + c0, br);
+        tmem_ld16_nowait(tr + 3 * BN + c0, bi);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         float vr[16], vi[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          vr[q] = __uint_as_float(mr[q]) + __uint_as_float(xr[q]);
-          vi[q] = __uint_as_float(mi[q]) + __uint_as_float(xi[q]);
+          vr[q] = __uint_as_float(ar[q]) + __uint_as_float(br[q]);
+          vi[q] = __uint_as_float(ai[q]) + __uint_as_float(bi[q]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -469,7 +469,7 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
         }
       }
       tc_fence_before();
-      mbar_arrive(&tempty[buf]);
+      mbar_arrive(&tempty[0]);
     }
   }
   __syncthreads();
@@ -663,22 +663,21 @@ void batcher_stats(const GemmBatcher *b, int64_t *launches, int64_t *problems, i
   b->stats(launches, problems, tiles, max_group);
 }
 
-// C[Mp][ldc] (re, im planes) = A x B^T.  A: four planes (hi_re, hi_im, lo_re,
-// lo_im) of Astride rows, rows [Aoff, Aoff + Mp) of each; B: six planes (put6)
-// of Bstride rows, rows [Boff, Boff + Np).  With a batch member the GEMM joins
-// its batcher's next grouped launch.
+// C[Mp][ldc] (re, im planes) = A x B^T.  A: planes of Astride rows, rows
+// [Aoff, Aoff + Mp) of each; B: planes of Bstride rows, rows [Boff, Boff + Np).
+// With a batch member the GEMM joins its batcher's next grouped launch.
 static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const float *Bp, int64_t Bstride,
                  int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st,
                  int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr) {
-  if (Mp % BM || Np % GBN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
-  if (4 * Astride > INT32_MAX || 6 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
+  if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
+  if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
   if (bm && bm->gb) {
     GroupProblem p;
     memset(&p, 0, sizeof p);
     int rc;
-    if ((rc = make_map(&p.tA, Ap, Kp, 4 * Astride)) || (rc = make_map(&p.tB, Bp, Kp, 6 * Bstride, GBN))) return rc;
+    if ((rc = make_map(&p.tA, Ap, Kp, 4 * Astride)) || (rc = make_map(&p.tB, Bp, Kp, 4 * Bstride))) return rc;
     p.g.mtiles = Mp / BM;
-    p.g.ntiles = Np / GBN;
+    p.g.ntiles = Np / BN;
     p.g.nkb = Kp / BK;
     p.g.Astride = Astride;
     p.g.Bstride = Bstride;
@@ -692,7 +691,7 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   }
   CUtensorMap ta, tb;
   int rc;
-  if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 6 * Bstride, GBN))) return rc;
+  if ((rc = make_map(&ta, Ap, Kp, 4 * Astride)) || (rc = make_map(&tb, Bp, Kp, 4 * Bstride))) return rc;
   // once per process: changing a kernel attribute can wait for the device's queued work
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
@@ -700,7 +699,7 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   });
   GemmArgs g;
   g.mtiles = Mp / BM;
-  g.ntiles = Np / GBN;
+  g.ntiles = Np / BN;
   g.nkb = Kp / BK;
   g.Astride = Astride;
   g.Bstride = Bstride;
@@ -712,9 +711,9 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   g.err = err;
   int tiles = g.mtiles * g.ntiles;
   int grid = std::min(tiles, num_sms());
-  // chunk_us > 0: launches of about that length (a tile is ~0.2 us per 16 K positions) so
+  // chunk_us > 0: launches of about that length (a tile is ~0.4 us per 16 K positions) so
   // that other streams' kernels get the SMs between them
-  const int per_cta = chunk_us > 0 ? std::max(1, (int)((int64_t)chunk_us * 16 * 5 / std::max(1, Kp))) : 0;
+  const int per_cta = chunk_us > 0 ? std::max(1, (int)((int64_t)chunk_us * 16 * 5 / 2 / std::max(1, Kp))) : 0;
   const int step = per_cta > 0 ? grid * per_cta : tiles;
   for (int t0 = 0; t0 < tiles; t0 += step) {
     if (t0 > 0) yield();
@@ -804,8 +803,8 @@ __global__ void k_phase_planes(int nrows, const int *rowp, int m1, int m2, int m
   put4(P, (int64_t)Mp * Kp, (int64_t)row * Kp + kpos[r], v);
 }
 
-// B planes of the stage-A matrix: G64[Re][n] -> six planes [6][Np][Kp] (put6;
-// transposed, column of Re = kpos[Re], or Re itself when kpos is null)
+// B planes of the stage-A matrix: G64[Re][n] -> planes [4][Np][Kp] (transposed,
+// column of Re = kpos[Re], or Re itself when kpos is null)
 __global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, const int *kpos, float *P, int64_t Np, int Kp) {
   __shared__ double2 tile[32][33];
   int64_t n0 = (int64_t)blockIdx.x * 32;
@@ -819,12 +818,12 @@ __global__ void k_gplanes(int64_t Nn, int nwsk, const double2 *G, const int *kpo
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     int64_t n = n0 + i;
     int re = r0 + threadIdx.x;
-    if (n < Nn && re < nwsk) put6(P, Np * Kp, n * Kp + (kpos ? kpos[re] : re), tile[threadIdx.x][i]);
+    if (n < Nn && re < nwsk) put4(P, Np * Kp, n * Kp + (kpos ? kpos[re] : re), tile[threadIdx.x][i]);
   }
 }
 
-// Rotation over the initial band + k-half of the Rp phase, split into the six
-// B planes of stage B (put6): Bp[6][Np2][Kp2], column c = (j - j0)*ncol + n' + nw*s'.
+// Rotation over the initial band + k-half of the Rp phase, split into the B
+// planes of stage B: Bp[4][Np2][Kp2], column c = (j - j0)*ncol + n' + nw*s'.
 __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int nw, int nb, int nws,
                                 const int *widx, const double2 *U, const float *gr, const float *gi, int64_t ldg,
                                 int m1, int m2, int m3, int L, const double2 *roots, const int *Rq,
@@ -848,14 +847,14 @@ __global__ void k_rotate_planes(int j0, int j1, int i0, const int *st_code, int 
       cfma(acc, Uk[mp], make_double2((double)gr[off], (double)gi[off]));
     }
     const int64_t col = (int64_t)(j - jbase) * ncol + c;
-    put6(Bp, Np2 * Kp2, col * Kp2 + kpos[rp], cmul(ph, acc));
+    put4(Bp, Np2 * Kp2, col * Kp2 + kpos[rp], cmul(ph, acc));
   }
   // the K padding [nws, Kp2) of the state's rows: zero (the workspace holds
   // whatever an earlier request left there, and 0 x NaN is NaN)
   const int npad = Kp2 - nws;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ncol * npad; e += gridDim.x * blockDim.x) {
     const int64_t col = (int64_t)(j - jbase) * ncol + e / npad;
-    put6(Bp, Np2 * Kp2, col * Kp2 + nws + e % npad, make_double2(0.0, 0.0));
+    put4(Bp, Np2 * Kp2, col * Kp2 + nws + e % npad, make_double2(0.0, 0.0));
   }
 }
 
@@ -945,7 +944,7 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
       __syncthreads();
       // a thread forms the ROT_KT positions of one operand row: lanes walk
       // consecutive bands n' (conflict-free shared reads) and each writes whole
-      // 32-byte sectors of the six planes (put6's order)
+      // 32-byte sectors of the four planes
       for (int o = threadIdx.x; o < nsk * nc; o += blockDim.x) {
         const int c = o % nc, js = o / nc;
         const int np = c % nw, s = c / nw;
@@ -959,23 +958,21 @@ __global__ void __launch_bounds__(256) k_rotate_k(int i0, const int *first_state
 #pragma unroll
           for (int kk = 0; kk < ROT_KT; ++kk) cfmaf(acc[kk], um, g[kk * pc + nw * mp]);
         }
-        float pl[6][ROT_KT];
+        float pl[4][ROT_KT];
 #pragma unroll
         for (int kk = 0; kk < ROT_KT; ++kk) {
           const float2 ph = sph[kk];
           float hr, lr, hi, li;
           split2((double)(ph.x * acc[kk].x - ph.y * acc[kk].y), hr, lr);
           split2((double)(ph.x * acc[kk].y + ph.y * acc[kk].x), hi, li);
-          pl[0][kk] = -hi;
-          pl[1][kk] = hr;
-          pl[2][kk] = hi;
-          pl[3][kk] = -li;
-          pl[4][kk] = lr;
-          pl[5][kk] = li;
+          pl[0][kk] = hr;
+          pl[1][kk] = hi;
+          pl[2][kk] = lr;
+          pl[3][kk] = li;
         }
         const int64_t col = (int64_t)(j0 + js) * ncol + np + nw * (s0 + s);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
+        for (int q = 0; q < 4; ++q) {
           float4 *dst = (float4 *)(Bp + q * plane + col * Kp2 + kp0);
           dst[0] = make_float4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
           dst[1] = make_float4(pl[q][4], pl[q][5], pl[q][6], pl[q][7]);
@@ -2402,9 +2399,9 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   {
   std::lock_guard<std::mutex> build_lock(*build_mu);
   if (!s.G) {
-    TCK(cudaMalloc(&s.G, (size_t)6 * NpA * KpA * sizeof(float)));
-    s.bytes += (int64_t)6 * NpA * KpA * sizeof(float);
-    TCK(cudaMemsetAsync(s.G, 0, (size_t)6 * NpA * KpA * sizeof(float), st));
+    TCK(cudaMalloc(&s.G, (size_t)4 * NpA * KpA * sizeof(float)));
+    s.bytes += (int64_t)4 * NpA * KpA * sizeof(float);
+    TCK(cudaMemsetAsync(s.G, 0, (size_t)4 * NpA * KpA * sizeof(float), st));
     dim3 grid((unsigned)((Nn + 31) / 32), (unsigned)((KpA + 31) / 32));
     k_gplanes<<<grid, dim3(32, 8), 0, st>>>(Nn, nwsk, G64, kposA, s.G, NpA, KpA);
     TCK(cudaGetLastError());
@@ -2426,12 +2423,12 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   const int64_t Np2 = rup((int64_t)nst * ncol, BN);
   float *PA, *CAr, *CAi, *B2;
   if ((rc = wsget(ws, "tc_PA", (size_t)4 * kc * KpA, &PA)) || (rc = wsget(ws, "tc_CAr", (size_t)kc * NpA, &CAr)) ||
-      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)6 * Np2 * KpB, &B2)))
+      (rc = wsget(ws, "tc_CAi", (size_t)kc * NpA, &CAi)) || (rc = wsget(ws, "tc_B2", (size_t)4 * Np2 * KpB, &B2)))
     return tfail(6, ws.msg.c_str());
   // the rotation writes every K position of every state row; zero the padding rows only
   {
     const int64_t used = (int64_t)nst * ncol;
-    for (int pl = 0; pl < 6; ++pl)
+    for (int pl = 0; pl < 4; ++pl)
       if (Np2 > used)
         TCK(cudaMemsetAsync(B2 + ((int64_t)pl * Np2 + used) * KpB, 0, (size_t)(Np2 - used) * KpB * sizeof(float), st));
   }
@@ -2849,7 +2846,7 @@ extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A
       if (p) cudaFree(p);
   };
   if (cudaMalloc(&dA, M * K * 16) || cudaMalloc(&dB, K * N * 16) || cudaMalloc(&dC, M * N * 16) ||
-      cudaMalloc(&PA, 4 * Mp * Kp * 4) || cudaMalloc(&PB, 6 * Np * Kp * 4) || cudaMalloc(&Cr, Mp * Np * 4) ||
+      cudaMalloc(&PA, 4 * Mp * Kp * 4) || cudaMalloc(&PB, 4 * Np * Kp * 4) || cudaMalloc(&Cr, Mp * Np * 4) ||
       cudaMalloc(&Ci, Mp * Np * 4) || cudaMalloc(&err, 4)) {
     cleanup();
     return tfail(6, "debug_cgemm: cudaMalloc failed");
@@ -2857,7 +2854,7 @@ extern "C" int ephg_debug_cgemm(int64_t M, int64_t N, int64_t K, const double *A
   cudaMemcpy(dA, A, M * K * 16, cudaMemcpyHostToDevice);
   cudaMemcpy(dB, B, K * N * 16, cudaMemcpyHostToDevice);
   cudaMemset(PA, 0, 4 * Mp * Kp * 4);
-  cudaMemset(PB, 0, 6 * Np * Kp * 4);
+  cudaMemset(PB, 0, 4 * Np * Kp * 4);
   cudaMemset(err, 0, 4);
   k_planes_rows<<<(unsigned)((M * K + 255) / 256), 256>>>(M, (int)K, dA, PA, Mp, (int)Kp);
   dim3 grid((unsigned)((N + 31) / 32), (unsigned)((Kp + 31) / 32));
@@ -2894,8 +2891,8 @@ extern "C" int ephg_debug_group_tiles(int np, const int *mtiles, const int *ntil
     tab[i].g.ntiles = ntiles[i];
     tab[i].g.nkb = 1;
     tab[i].g.Astride = (int64_t)mtiles[i] * BM;
-    tab[i].g.Bstride = (int64_t)ntiles[i] * GBN;
-    tab[i].g.ldc = (int64_t)ntiles[i] * GBN;
+    tab[i].g.Bstride = (int64_t)ntiles[i] * BN;
+    tab[i].g.ldc = (int64_t)ntiles[i] * BN;
     tab[i].tile0 = (int)T;
     T += (int64_t)mtiles[i] * ntiles[i];
   }
@@ -2906,10 +2903,10 @@ extern "C" int ephg_debug_group_tiles(int np, const int *mtiles, const int *ntil
     const int64_t p = (const uint8_t *)j.tA - (const uint8_t *)&tab[0].tA;
     if (p < 0 || p % (int64_t)sizeof(GroupProblem)) return EPHG_ERR_INDEX;
     const int i = (int)(p / (int64_t)sizeof(GroupProblem));
-    if (i >= np || j.tB != &tab[i].tB || j.arow % BM || j.brow % GBN) return EPHG_ERR_INDEX;
-    const int mt = j.arow / BM, nt = j.brow / GBN;
+    if (i >= np || j.tB != &tab[i].tB || j.arow % BM || j.brow % BN) return EPHG_ERR_INDEX;
+    const int mt = j.arow / BM, nt = j.brow / BN;
     if (mt >= mtiles[i] || nt >= ntiles[i] || t - tab[i].tile0 != mt + mtiles[i] * nt) return EPHG_ERR_INDEX;
-    if ((int64_t)(j.Cr - (float *)nullptr) != (int64_t)mt * BM * tab[i].g.ldc + (int64_t)nt * GBN)
+    if ((int64_t)(j.Cr - (float *)nullptr) != (int64_t)mt * BM * tab[i].g.ldc + (int64_t)nt * BN)
       return EPHG_ERR_INDEX;
     hits[tab[i].tile0 + mt + mtiles[i] * nt]++;
   }
