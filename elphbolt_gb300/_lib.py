@@ -35,10 +35,11 @@ EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count"
            "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
            "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates", "ephg_set_polar",
            "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge", "ephg_el_rates_batch",
-           "ephg_g2_average_degenerate"]
+           "ephg_g2_average_degenerate", "ephg_el_rates_sets", "ephg_server_set_merge"]
 
 TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
 DEGAVG_REFERENCE, DEGAVG_MEAN = 0, 1
+MAX_SETS = 8   # EPHG_MAX_SETS
 
 
 class EphgError(RuntimeError):
@@ -80,7 +81,8 @@ class ServerStats(ct.Structure):
     _fields_ = [("submitted", ct.c_int64), ("completed", ct.c_int64), ("failed", ct.c_int64),
                 ("rejected", ct.c_int64), ("vertices", ct.c_int64), ("p50_ms", ct.c_double),
                 ("p99_ms", ct.c_double), ("max_ms", ct.c_double), ("mean_ms", ct.c_double),
-                ("wall_s", ct.c_double), ("vertices_per_s", ct.c_double), ("peak_device_bytes", ct.c_int64)]
+                ("wall_s", ct.c_double), ("vertices_per_s", ct.c_double), ("peak_device_bytes", ct.c_int64),
+                ("merged", ct.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -126,6 +128,8 @@ def load(path: str = LIB_PATH):
     L.ephg_kq_index.argtypes = [vp, c_i64p, ct.c_int64, c_i64p, ct.c_int64, c_i64p, c_i64p]
     L.ephg_el_rates.argtypes = [vp, ct.POINTER(RateRequest), c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, c_dp, ct.c_int64]
+    L.ephg_el_rates_sets.argtypes = [vp, ct.c_int64, ct.POINTER(RateRequest), ct.POINTER(c_dp), c_i64p,
+                                     ct.POINTER(RateStats)]
     L.ephg_ph_rates.argtypes = [vp, ct.POINTER(RateRequest), ct.c_int64, c_dp, c_dp, c_i64p, ct.POINTER(RateStats),
                                 c_dp, c_dp, ct.c_int64]
     L.ephg_set_polar.argtypes = [vp, c_dp, c_dp]
@@ -139,6 +143,7 @@ def load(path: str = LIB_PATH):
     L.ephg_el_rates_batch.argtypes = [ct.c_int64, ct.POINTER(vp), ct.POINTER(RateRequest), ct.POINTER(c_dp),
                                       ct.POINTER(c_i64p), ct.POINTER(RateStats), ct.POINTER(ct.c_int),
                                       ct.POINTER(BatchOpts), ct.POINTER(BatchStats)]
+    L.ephg_server_set_merge.argtypes = [vp, ct.c_int]
     L.ephg_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_int64, ct.c_int, ct.POINTER(vp)]
     L.ephg_server_destroy.argtypes = [vp]
     L.ephg_submit.argtypes = [vp, ct.c_int, ct.POINTER(RateRequest), c_i64p]

@@ -815,11 +815,37 @@ static int check_err_view(const ExecView &x) {
 
 #define WSFAILX(rc) fail((rc), "%s", x.ws->msg.c_str())
 
+static_assert(ephg::MAX_SETS == EPHG_MAX_SETS, "parameter-set bound of the C interface");
+
+int ephg::check_sets(int64_t n, const ephg_rate_request *reqs) {
+  if (n < 1 || n > MAX_SETS) return fail(EPHG_ERR_ARG, "el_rates_sets: nsets must be 1..%d", MAX_SETS);
+  const ephg_rate_request &a = reqs[0];
+  for (int64_t p = 0; p < n; ++p) {
+    const ephg_rate_request &b = reqs[p];
+    if (b.mesh[0] != a.mesh[0] || b.mesh[1] != a.mesh[1] || b.mesh[2] != a.mesh[2] || b.enref != a.enref ||
+        b.fsthick != a.fsthick || b.delta_kind != a.delta_kind || b.precision != a.precision)
+      return fail(EPHG_ERR_ARG, "el_rates_sets: set %lld differs from set 0 in more than T, sigma and chempot",
+                  (long long)p);
+    if (!(b.T > 0)) return fail(EPHG_ERR_ARG, "el_rates_sets: T must be > 0 (set %lld)", (long long)p);
+    if (b.delta_kind == 0 && !(b.sigma > 0))
+      return fail(EPHG_ERR_ARG, "el_rates_sets: sigma must be > 0 (set %lld)", (long long)p);
+  }
+  return EPHG_OK;
+}
+
 int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
                         int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus,
-                        int64_t cap, const PhOut *ph, const DegAvgReq *avg) {
+                        int64_t cap, const PhOut *ph, const DegAvgReq *avg, const SetsOut *sets) {
   if (!h || !req || (!ph && !avg && (!rates || !indexlist)) || (ph && !ph->rates_phe) || (avg && (ph || !avg->g2)))
     return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
+  if (sets) {
+    if (ph || avg || g2 || sets->reqs != req || !sets->rates) return fail(EPHG_ERR_ARG, "el_rates_sets: bad arguments");
+    int rc0 = check_sets(sets->n, sets->reqs);
+    if (rc0) return rc0;
+    for (int p = 0; p < sets->n; ++p)
+      if (!sets->rates[p]) return fail(EPHG_ERR_ARG, "el_rates_sets: rates[%d] is NULL", p);
+  }
+  const int nsets = sets ? sets->n : 1;
   for (int i = 0; i < 3; ++i)
     if (req->mesh[i] <= 0) return fail(EPHG_ERR_ARG, "el_rates: bad mesh");
   if (req->delta_kind < 0 || req->delta_kind > 2) return fail(EPHG_ERR_ARG, "el_rates: bad delta_kind");
@@ -925,6 +951,15 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   launch_ph_post(N, nb, iota, nullptr, wq, Vq, nullptr, 0, h->masses, nullptr, nullptr, nullptr, om,
                  u, uf, x.err, st);
   launch_bose(N, nb, om, req->T, bose, st);
+  RateSets rs;
+  memset(&rs, 0, sizeof rs);
+  rs.n = nsets;
+  for (int p = 1; p < nsets; ++p) {   // the other parameter sets' Bose factors
+    if ((rc = wsget((*x.ws), ("r_bose" + std::to_string(p)).c_str(), (size_t)N * nb, &rs.bose[p])))
+      return WSFAILX(rc);
+    launch_bose(N, nb, om, sets->reqs[p].T, rs.bose[p], st);
+    (*x.launches) += 1;
+  }
   if (h->polar_on) {   // long_range_prefac(q, u_s) for every (q, s)
     launch_glprefac(N, nb, Lq, u, glp, glpf, st);
     (*x.launches) += 1;
@@ -1099,6 +1134,17 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   const int nblk_max = std::max((nwv + 15) / 16, (nwv + 255) / 256 * 8);
   double *partial;
   if ((rc = wsget((*x.ws), "r_partial", (size_t)nst * nblk_max, &partial))) return WSFAILX(rc);
+  rs.rp[0] = rp;
+  rs.bose[0] = bose;
+  rs.partial[0] = partial;
+  for (int p = 1; p < nsets; ++p) {
+    rs.rp[p] = rp;
+    rs.rp[p].T = sets->reqs[p].T;
+    rs.rp[p].sigma = sets->reqs[p].sigma;
+    rs.rp[p].chempot = sets->reqs[p].chempot;
+    if ((rc = wsget((*x.ws), ("r_partial" + std::to_string(p)).c_str(), (size_t)nst * nblk_max, &rs.partial[p])))
+      return WSFAILX(rc);
+  }
   if (!split) {
     double2 *Pk, *gk, *B, *Pq, *Cb;
     const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(nA, ((int64_t)1 << 31) / (Nn * 16)));
@@ -1133,6 +1179,13 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
       launch_zgemm(nwv, ns * ncol, nwsq, Pq, nwsq, B + j0 * ncol, ldb, Cb, (int64_t)ns * ncol, st);
       (*x.tb).end(st);
       launch_epilogue_fp64(nwv, (int)j0, (int)j0 + ns, Cb, (int64_t)ns * ncol, rp, ed, partial, nblk, st);
+      for (int p = 1; p < nsets; ++p) {   // the same GEMM output under the other parameter sets
+        EpiData ep = ed;
+        ep.bose = rs.bose[p];
+        launch_epilogue_fp64(nwv, (int)j0, (int)j0 + ns, Cb, (int64_t)ns * ncol, rs.rp[p], ep, rs.partial[p], nblk,
+                             st);
+        (*x.launches) += 1;
+      }
       (*x.launches) += 2;
     }
   } else {
@@ -1140,15 +1193,25 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
                                mesh, L, roots, widx, arow, nA, st_code, first_state, h->Rk, h->degk, h->kposk,
                                h->Rq, h->degq, h->kposq, V, rp, ed, partial, nblk_max, &nblk,
                                ev.e[2], x.launches, x.ta, x.tb, &h->split_mu, x.chunk_us, x.yield, &x.bm,
-                               x.chunk_bytes);
+                               x.chunk_bytes, nsets > 1 ? &rs : nullptr);
     if (rc) return fail(rc, "split path: %s", tc::last_error());
   }
   CKL();
   CK(cudaMemsetAsync(rates_d, 0, (size_t)N * nw * sizeof(double), st));
   launch_rate_final(nst, nblk, partial, st_code, nw, N, rates_d, st);
   (*x.launches) += 1;
+  std::vector<double *> rates_sets(nsets, rates_d);
+  for (int p = 1; p < nsets; ++p) {
+    if ((rc = wsget((*x.ws), ("r_rates" + std::to_string(p)).c_str(), (size_t)N * nw, &rates_sets[p])))
+      return WSFAILX(rc);
+    CK(cudaMemsetAsync(rates_sets[p], 0, (size_t)N * nw * sizeof(double), st));
+    launch_rate_final(nst, nblk, rs.partial[p], st_code, nw, N, rates_sets[p], st);
+    (*x.launches) += 1;
+  }
   CK(cudaEventRecord(ev.e[3], st));
   if (rates) CK(cudaMemcpyAsync(rates, rates_d, (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+  for (int p = 1; p < nsets; ++p)
+    CK(cudaMemcpyAsync(sets->rates[p], rates_sets[p], (size_t)N * nw * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (ph) CK(cudaMemcpyAsync(ph->rates_phe, phr, (size_t)N * nb * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (indexlist)   // the rows of the rates: the A-rows
@@ -1193,6 +1256,17 @@ extern "C" int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, doubl
   if (!h) return fail(EPHG_ERR_ARG, "el_rates: bad arguments");
   const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
   return el_rates_view(h, x, req, rates, indexlist, stats, g2, xplus, xminus, cap);
+}
+
+extern "C" int ephg_el_rates_sets(ephg_handle *h, int64_t nsets, const ephg_rate_request *reqs, double *const *rates,
+                                  int64_t *indexlist, ephg_rate_stats *stats) {
+  if (!h || !reqs || !rates || !indexlist) return fail(EPHG_ERR_ARG, "el_rates_sets: bad arguments");
+  int rc = check_sets(nsets, reqs);
+  if (rc) return rc;
+  const ExecView x{h->st, h->err, &h->ws, &h->timer_a, &h->timer_b, &h->launches};
+  const SetsOut so{(int)nsets, reqs, rates};
+  return el_rates_view(h, x, &reqs[0], rates[0], indexlist, stats, nullptr, nullptr, nullptr, 0, nullptr, nullptr,
+                       &so);
 }
 
 extern "C" int ephg_g2_average_degenerate(ephg_handle *h, const ephg_rate_request *req, int64_t mode, double thres,

@@ -80,12 +80,24 @@ struct DegAvgReq {
   int mode;
   double thres;
 };
+// Parameter sets of a merged request (ephg_el_rates_sets): the request is set
+// 0; reqs[1..n-1] differ from it only in T, sigma and chempot, and rates[p]
+// receives set p's rates (rates[0] is el_rates_view's own `rates`).
+struct SetsOut {
+  int n;
+  const ephg_rate_request *reqs;
+  double *const *rates;
+};
 // ph == nullptr: the electron side only (ephg_el_rates); otherwise rates and
 // indexlist may be NULL.  avg != nullptr: the request's set-up only, then the
-// averaging of avg->g2 (rates and indexlist may be NULL).
+// averaging of avg->g2 (rates and indexlist may be NULL).  sets != nullptr:
+// the electron side under every set (not with ph, avg or vertex lists).
 int el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus, double *xminus, int64_t cap,
-                  const PhOut *ph = nullptr, const DegAvgReq *avg = nullptr);
+                  const PhOut *ph = nullptr, const DegAvgReq *avg = nullptr, const SetsOut *sets = nullptr);
+// reqs[0..n-1] may share one contraction: equal but for T, sigma and chempot,
+// each with valid T / sigma.  Returns 0 or EPHG_ERR_ARG with the reason recorded.
+int check_sets(int64_t n, const ephg_rate_request *reqs);
 // record a failure message for ephg_last_error() and return code
 int api_fail(int code, const char *fmt, ...);
 // read, clear and translate the handle's device error word

@@ -149,6 +149,18 @@ struct EpiData {
   const double2 *glp;
   const float2 *glpf;   // same in fp32 (split path)
 };
+// Parameter sets of a merged request (ephg_el_rates_sets): requests that differ
+// only in T, sigma and chempot share their vertices and |g|^2, so the
+// contractions run once and the rate epilogue once per set.  Set 0 is the
+// request itself (its RateParams, EpiData.bose and partial buffer); sets 1..n-1
+// carry their own parameters, FP64 Bose factors and rate partials.
+constexpr int MAX_SETS = 8;   // EPHG_MAX_SETS
+struct RateSets {
+  int n;
+  RateParams rp[MAX_SETS];
+  double *bose[MAX_SETS];      // [q][s] per set (set 0: EpiData.bose)
+  double *partial[MAX_SETS];   // [j][iblk] per set (set 0: the caller's partial)
+};
 // per (k', state) epilogue on an FP64 C chunk: rates partial sums [j][iblk]
 void launch_epilogue_fp64(int nwv, int j0, int j1, const double2 *C, int64_t ldc,
                           const RateParams &rp, const EpiData &d, double *partial,

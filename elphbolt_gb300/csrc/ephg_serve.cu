@@ -80,8 +80,9 @@ struct Executor {
   virtual int64_t min_bytes(int c, const ephg_rate_request &r) const = 0;   // lower bound of a request's workspace
   virtual void set_grow(int slot, bool (*fn)(void *, int64_t), void *ctx) = 0;   // reservation hook of a workspace
   virtual void release(int slot) = 0;
-  virtual int run(int slot, int c, const ephg_rate_request &r, bool urgent, const ephg::Yield &y, Result &out,
-                  std::string &msg) = 0;
+  // reqs[0..n-1] on crystal c, equal but for T, sigma and chempot (one contraction); out[i] per request
+  virtual int run(int slot, int c, const ephg_rate_request *reqs, int n, bool urgent, const ephg::Yield &y,
+                  Result *out, std::string &msg) = 0;
   virtual void drain(int slot) = 0;   // wait for the slot's queued device work
 };
 
@@ -96,8 +97,20 @@ struct Ticket {
   double est = 1.0;        // estimated isolated solve time (ms; the work itself without any time model)
   bool urgent = false;
   bool alone = true;       // no other request ran at any time while this one did
+  std::vector<Ticket *> partners;   // queued requests merged into this one's run (it leads them)
   clk::time_point t_submit, t_done;
 };
+
+// Can b share a's contraction (ephg_el_rates_sets)?  Same crystal, mesh,
+// window, delta and precision; both with a valid T (and sigma for the
+// Gaussian), so that one bad request cannot fail another.
+bool mergeable(const Ticket &a, const Ticket &b) {
+  const ephg_rate_request &x = a.req, &y = b.req;
+  auto valid = [](const ephg_rate_request &r) { return r.T > 0 && (r.delta_kind != 0 || r.sigma > 0); };
+  return a.crystal == b.crystal && x.mesh[0] == y.mesh[0] && x.mesh[1] == y.mesh[1] && x.mesh[2] == y.mesh[2] &&
+         x.enref == y.enref && x.fsthick == y.fsthick && x.delta_kind == y.delta_kind &&
+         x.precision == y.precision && valid(x) && valid(y);
+}
 
 // Least-squares fit of isolated solve time (ms) against work, per crystal.
 struct TimeModel {
@@ -133,6 +146,7 @@ struct ephg_server {
   int excl_waiting = 0;            // slots waiting to take the whole budget: no new request starts meanwhile
   int excl_owner = -1;             // slot holding the whole budget
   int64_t reserved = 0;            // bytes reserved by all slots' workspaces
+  int max_sets = EPHG_MAX_SETS;    // requests per merged run (1: no merging)
   std::vector<char> busy;          // slot runs a request
   std::vector<double> run_work;    // estimated work of each slot's running request (0: idle or waiting)
   std::vector<double> run_est;     // its estimated isolated time
@@ -209,7 +223,7 @@ struct ephg_server {
   std::vector<std::thread> workers;
   // statistics
   std::vector<double> lat_ms;
-  int64_t submitted = 0, completed = 0, failed = 0, rejected = 0, vertices = 0, peak = 0;
+  int64_t submitted = 0, completed = 0, failed = 0, rejected = 0, vertices = 0, peak = 0, merged = 0;
   bool any_submit = false;
   clk::time_point t_first, t_last;
 
@@ -230,9 +244,21 @@ struct ephg_server {
   // Run t on `slot` (called with running already counting it); if its workspace
   // cannot be reserved, idle slots give back theirs, then it runs alone.
   int execute(int slot, Ticket &t, std::unique_lock<std::mutex> &lk) {
-    lk.unlock();
-    int rc = ex->run(slot, t.crystal, t.req, t.urgent, hook(slot), t.res, t.msg);
-    lk.lock();
+    const int n = 1 + (int)t.partners.size();
+    std::vector<ephg_rate_request> reqs{t.req};
+    for (Ticket *o : t.partners) reqs.push_back(o->req);
+    std::vector<Result> res(n);
+    auto run = [&]() {
+      lk.unlock();
+      const int rc = ex->run(slot, t.crystal, reqs.data(), n, t.urgent, hook(slot), res.data(), t.msg);
+      lk.lock();
+      if (rc == EPHG_OK) {
+        t.res = std::move(res[0]);
+        for (int i = 1; i < n; ++i) t.partners[i - 1]->res = std::move(res[i]);
+      }
+      return rc;
+    };
+    int rc = run();
     if (rc != EPHG_ERR_NOMEM) return rc;
     bool freed = false;
     for (int o = 0; o < nslots; ++o)
@@ -242,9 +268,7 @@ struct ephg_server {
       }
     if (freed) {
       t.msg.clear();
-      lk.unlock();
-      rc = ex->run(slot, t.crystal, t.req, t.urgent, hook(slot), t.res, t.msg);
-      lk.lock();
+      rc = run();
       if (rc != EPHG_ERR_NOMEM) return rc;
     }
     // exclusive: stop new starts, wait until no other slot runs, take the whole budget
@@ -263,9 +287,7 @@ struct ephg_server {
     for (int o = 0; o < nslots; ++o)
       if (o != slot) release_slot(o);   // idle: no other slot runs now
     t.msg.clear();
-    lk.unlock();
-    rc = ex->run(slot, t.crystal, t.req, t.urgent, hook(slot), t.res, t.msg);
-    lk.lock();
+    rc = run();
     excl_owner = -1;
     cv_work.notify_all();
     cv_idle.notify_all();
@@ -287,6 +309,19 @@ struct ephg_server {
       queue.erase(queue.begin() + (std::ptrdiff_t)pick);
       Ticket *t = tickets[id].get();
       t->state = EPHG_TICKET_RUNNING;
+      // queued requests that differ only in T, sigma and chempot share this run's contraction
+      t->partners.clear();
+      for (size_t i = 0; i < queue.size() && 1 + (int)t->partners.size() < max_sets;) {
+        Ticket *o = tickets[queue[i]].get();
+        if (mergeable(*t, *o)) {
+          o->state = EPHG_TICKET_RUNNING;
+          t->partners.push_back(o);
+          queue.erase(queue.begin() + (std::ptrdiff_t)i);
+        } else {
+          ++i;
+        }
+      }
+      if (!t->partners.empty()) t->alone = false;   // a merged run trains no time model
       double bigger = 0.0;
       for (int o = 0; o < nslots; ++o) bigger = std::max(bigger, run_work[o]);
       t->urgent = t->work < 0.25 * bigger;
@@ -307,23 +342,29 @@ struct ephg_server {
       run_ticket[slot] = nullptr;
       cv_gpu.notify_all();
       const clk::time_point now = clk::now();
-      t->t_done = now;
-      t->rc = rc;
-      if (rc == EPHG_OK) {
-        t->state = EPHG_TICKET_DONE;
-        completed++;
-        vertices += t->res.stats.vertices;
-        const double l = std::chrono::duration<double, std::milli>(now - t->t_submit).count();
-        lat_ms.push_back(l);
-        if (t->alone) {   // an isolated solve time
-          model[t->crystal].add(t->work, l);
-          rekey();
+      std::vector<Ticket *> group{t};
+      group.insert(group.end(), t->partners.begin(), t->partners.end());
+      for (Ticket *g : group) {
+        g->t_done = now;
+        g->rc = rc;
+        if (rc == EPHG_OK) {
+          g->state = EPHG_TICKET_DONE;
+          completed++;
+          merged += g != t;
+          vertices += g->res.stats.vertices;
+          lat_ms.push_back(std::chrono::duration<double, std::milli>(now - g->t_submit).count());
+          t_last = now;
+        } else {
+          g->msg = t->msg;
+          g->state = EPHG_TICKET_FAILED;
+          failed++;
         }
-        t_last = now;
-      } else {
-        t->state = EPHG_TICKET_FAILED;
-        failed++;
       }
+      if (rc == EPHG_OK && t->alone) {   // an isolated solve time
+        model[t->crystal].add(t->work, std::chrono::duration<double, std::milli>(now - t->t_submit).count());
+        rekey();
+      }
+      t->partners.clear();
       cv_done.notify_all();
       cv_idle.notify_all();
       cv_work.notify_all();
@@ -412,20 +453,30 @@ struct HandleExecutor : Executor {
     cudaStreamSynchronize(slots[s]->st);
     cudaStreamSynchronize(slots[s]->st_hi);
   }
-  int run(int s, int c, const ephg_rate_request &r, bool urgent, const ephg::Yield &y, Result &out,
+  int run(int s, int c, const ephg_rate_request *reqs, int n, bool urgent, const ephg::Yield &y, Result *out,
           std::string &msg) override {
     ephg_handle *h = hs[c];
     Slot &S = *slots[s];
     cudaSetDevice(device);
+    const ephg_rate_request &r = reqs[0];
     const int64_t N = r.mesh[0] * r.mesh[1] * r.mesh[2];
-    out.rates.assign((size_t)(N * h->nw), 0.0);
-    out.idx.assign((size_t)N, 0);
+    std::vector<double *> rates(n);
+    for (int i = 0; i < n; ++i) {
+      out[i].rates.assign((size_t)(N * h->nw), 0.0);
+      rates[i] = out[i].rates.data();
+    }
+    out[0].idx.assign((size_t)N, 0);
     // the previous request of this slot ended with a host sync, so its buffers may move between the slot's streams
     S.ws.st = urgent ? S.st_hi : S.st;
     const ephg::ExecView x{S.ws.st, S.err, &S.ws, &S.ta, &S.tb, &S.launches, kChunkUs, y};
-    const int rc = ephg::el_rates_view(h, x, &r, out.rates.data(), out.idx.data(), &out.stats, nullptr, nullptr,
-                                       nullptr, 0);
+    const ephg::SetsOut so{n, reqs, rates.data()};
+    const int rc = ephg::el_rates_view(h, x, &r, rates[0], out[0].idx.data(), &out[0].stats, nullptr, nullptr,
+                                       nullptr, 0, nullptr, nullptr, n > 1 ? &so : nullptr);
     if (rc != EPHG_OK) msg = ephg_last_error();
+    for (int i = 1; i < n; ++i) {   // the indexlist and stats are common to a merged run
+      out[i].idx = out[0].idx;
+      out[i].stats = out[0].stats;
+    }
     return rc;
   }
 };
@@ -453,9 +504,12 @@ struct FakeExecutor : Executor {
   }
   void release(int s) override { ws[s] = 0; }
   void drain(int) override {}
-  // simulated device time service_ms x (mesh / 8)^3, in four parts with yield points between them
-  int run(int s, int c, const ephg_rate_request &r, bool, const ephg::Yield &y, Result &out,
+  int merged_runs = 0;
+  // simulated device time service_ms x (mesh / 8)^3, in four parts with yield points between them; a merged
+  // run takes the time of one request, and request i's result is crystal + 1000 T_i
+  int run(int s, int c, const ephg_rate_request *reqs, int nreq, bool, const ephg::Yield &y, Result *out,
           std::string &msg) override {
+    const ephg_rate_request &r = reqs[0];
     const int64_t need = per_request * r.mesh[0] * r.mesh[1] * r.mesh[2] / 1000;
     if (need > ws[s]) {
       if (!grow(grow_ctx, need - ws[s])) {
@@ -476,11 +530,14 @@ struct FakeExecutor : Executor {
     {
       std::lock_guard<std::mutex> g(m);
       --concurrent;
+      merged_runs += nreq > 1;
     }
-    out.stats = ephg_rate_stats{};
-    out.stats.vertices = r.mesh[0] * r.mesh[1] * r.mesh[2];
-    out.rates.assign(1, (double)c);
-    out.idx.assign(1, 1);
+    for (int i = 0; i < nreq; ++i) {
+      out[i].stats = ephg_rate_stats{};
+      out[i].stats.vertices = r.mesh[0] * r.mesh[1] * r.mesh[2];
+      out[i].rates.assign(1, (double)c + 1000.0 * reqs[i].T);
+      out[i].idx.assign(1, 1);
+    }
     return EPHG_OK;
   }
 };
@@ -542,6 +599,7 @@ void fill_stats(ephg_server *s, ephg_server_stats *o) {
   o->rejected = s->rejected;
   o->vertices = s->vertices;
   o->peak_device_bytes = s->peak;
+  o->merged = s->merged;
   std::vector<double> l = s->lat_ms;
   std::sort(l.begin(), l.end());
   if (!l.empty()) {
@@ -642,6 +700,13 @@ int ephg_wait(ephg_server *s, int64_t ticket, double *rates, int64_t *indexlist,
   return EPHG_OK;
 }
 
+int ephg_server_set_merge(ephg_server *s, int max_sets) {
+  if (!s || max_sets < 1 || max_sets > EPHG_MAX_SETS) return ephg::api_fail(EPHG_ERR_ARG, "server_set_merge: bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->max_sets = max_sets;
+  return EPHG_OK;
+}
+
 int ephg_server_stats_get(ephg_server *s, ephg_server_stats *out) {
   if (!s || !out) return ephg::api_fail(EPHG_ERR_ARG, "server_stats: null argument");
   fill_stats(s, out);
@@ -649,7 +714,8 @@ int ephg_server_stats_get(ephg_server *s, ephg_server_stats *out) {
 }
 
 int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t budget, int64_t per_request_bytes,
-                               const int64_t *meshes, ephg_server_stats *out, int *max_concurrent, double *lat_ms) {
+                               const int64_t *meshes, const double *temps, int max_sets, ephg_server_stats *out,
+                               int *max_concurrent, double *lat_ms) {
   if (nreq <= 0 || nslots < 1 || !meshes || !out) return ephg::api_fail(EPHG_ERR_ARG, "selftest: bad arguments");
   auto ex = std::make_unique<FakeExecutor>();
   FakeExecutor *fx = ex.get();
@@ -659,10 +725,15 @@ int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t 
   ex->per_request = per_request_bytes;
   ex->ws.assign(nslots, 0);
   ephg_server *s = make_server(std::move(ex), budget, nslots);
+  if (max_sets >= 1 && max_sets <= EPHG_MAX_SETS) s->max_sets = max_sets;
   std::vector<std::pair<int64_t, int>> tk(nreq, {0, -1});   // (ticket, crystal) per request
   for (int i = 0; i < nreq; ++i) {
     ephg_rate_request r{};
     r.mesh[0] = r.mesh[1] = r.mesh[2] = meshes[i];
+    if (temps) {   // a valid T (and sigma) makes the request mergeable
+      r.T = temps[i];
+      r.sigma = 0.01;
+    }
     int64_t id = 0;
     if (submit(s, i % 2, &r, &id) == EPHG_OK) tk[i] = {id, i % 2};
     if (i == 0) std::this_thread::sleep_for(std::chrono::microseconds(200));   // the first one starts alone
@@ -676,7 +747,8 @@ int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t 
       continue;
     }
     const int rc = ephg_wait(s, tk[i].first, &rate, &idx, nullptr, &lat);
-    if (rc == EPHG_OK && rate != (double)tk[i].second) bad++;   // the fake writes its crystal index
+    // the fake writes the crystal index + 1000 T
+    if (rc == EPHG_OK && rate != (double)tk[i].second + (temps ? 1000.0 * temps[i] : 0.0)) bad++;
     if (lat_ms) lat_ms[i] = rc == EPHG_OK ? lat : -1.0;
   }
   fill_stats(s, out);

@@ -1057,8 +1057,15 @@ __device__ __forceinline__ F2 f2_half_sq(F2 t) {
   const float e = __fmaf_rn(t.hi, t.hi, -p);
   return F2{0.5f * p, 0.5f * __fmaf_rn(2.0f * t.hi, t.lo, e)};
 }
+// a b for double-floats, to about 2^-46 relative (the hi product's error by FMA)
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+  const float s = __fadd_rn(p, e);
+  return F2{s, __fadd_rn(e, __fsub_rn(p, s))};
+}
 // e^(hi + lo)
-__device__ __forceinline__ float f2_exp(F2 a) { return expf(a.hi) * (1.0f + a.lo); }
+__device__ __forceinline__ float f2_exp(F2 a) { return __fmul_rn(expf(a.hi), __fadd_rn(1.0f, a.lo)); }
 
 // The phonon side's Gaussian factors are formed scaled by 2^64
 // (e^(64 ln 2 - t^2/2)), so that its sums keep the tails down to e^-131 in
@@ -1093,15 +1100,23 @@ __device__ __forceinline__ VtxF vtx_factors(F2 dn, float ex, float emx, float4 w
   const F2 ap = f2_half_sq(tp), am = f2_half_sq(tm);
   if (SHIFT) {
     const F2 sh{LN2X64_HI, LN2X64_LO};
-    r.dp = dnorm * f2_exp(f2_add(sh, F2{-ap.hi, -ap.lo}));
-    r.dm = dnorm * f2_exp(f2_add(sh, F2{-am.hi, -am.lo}));
+    r.dp = __fmul_rn(dnorm, f2_exp(f2_add(sh, F2{-ap.hi, -ap.lo})));
+    r.dm = __fmul_rn(dnorm, f2_exp(f2_add(sh, F2{-am.hi, -am.lo})));
   } else {
-    r.dp = dnorm * f2_exp(F2{-ap.hi, -ap.lo});
-    r.dm = dnorm * f2_exp(F2{-am.hi, -am.lo});
+    r.dp = __fmul_rn(dnorm, f2_exp(F2{-ap.hi, -ap.lo}));
+    r.dm = __fmul_rn(dnorm, f2_exp(F2{-am.hi, -am.lo}));
   }
-  r.ap = bose + __frcp_rn(1.0f + ex * wv.z);
-  r.am = bose + __frcp_rn(1.0f + emx * wv.z);
+  r.ap = __fadd_rn(bose, __frcp_rn(__fmaf_rn(ex, wv.z, 1.0f)));
+  r.am = __fadd_rn(bose, __frcp_rn(__fmaf_rn(emx, wv.z, 1.0f)));
   return r;
+}
+// X+ + X- of one vertex: |g|^2 cx (n + f) delta+ + |g|^2 cx (n + 1 - f) delta-.
+// Every rounding is explicit, so that the fused kernel's parameter sets and a
+// lone request form the same bits from the same inputs.
+__device__ __forceinline__ float vtx_x(float g2c, const VtxF &f, float &xp, float &xm) {
+  xp = __fmul_rn(__fmul_rn(g2c, f.ap), f.dp);
+  xm = __fmul_rn(__fmul_rn(g2c, f.am), f.dm);
+  return __fadd_rn(xp, xm);
 }
 
 __global__ void k_qtab(int n, const double *om, const double *bose, double sigma, double kT, double const_tp,
@@ -1537,6 +1552,30 @@ struct FusedArgs {
   int nblk;
 };
 
+// Sets 1..n-1 of a merged request (RateSets) in the fused kernel's layouts.
+struct FusedSets {
+  int n;                           // 1: the request alone
+  float isg_hi[MAX_SETS], isg_lo[MAX_SETS];   // 1 / sigma_p as a double-float
+  float dnorm[MAX_SETS];           // 1 / (sigma_p sqrt(2 pi) N_k)
+  const float2 *occ;               // [(p - 1) * nst + j]: (e^x, e^-x), x = (E_j - mu_p) / kT_p, as StateRec / YOcc
+  const float4 *mode;              // set p at (p - 1) * mode_stride, q-blocked, fields s:
+  int64_t mode_stride;             //   (w = omega / sigma_p as a double-float, e^(omega / kT_p), n_p(omega))
+  double *partial[MAX_SETS];
+};
+
+__global__ void k_fused_set_tabs(int nst, int N, const StateRec *srec, double chempot, double kT, const float *bs,
+                                 const float4 *wv, float2 *occ, float4 *mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nst) {
+    const double E = srec[i].E;
+    occ[i] = make_float2((float)fmin(exp((E - chempot) / kT), 3.0e38), y_occ(E, chempot, kT).emx);
+  }
+  if (i < N * 6) {
+    const float4 w = wv[i];
+    mode[blk32(i / 6, 6, i % 6)] = make_float4(w.x, w.y, w.z, bs[i]);
+  }
+}
+
 __global__ void k_fused_rows(int nwv, int MpB, const int *widx, const double *ens, const float2 *Uf, const int *cum,
                              double enref, double fsthick, int m0, int m1, int4 *row, float4 *U4, double *ensw) {
   const int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1651,10 +1690,12 @@ __device__ __forceinline__ float2 hrot(const float2 *u, const float *gre, const 
 // applied once per pair (y_factor).
 // POLAR: g += long_range_prefac(q, u_s) * <U_k'[n]|U_k[m]> (glb = the lane's
 // entry of field 0 of q's block of the prefactor table, unm the overlap).
-template <bool PH, bool POLAR>
+// OUT: also g2o[s] = |g|^2 cx of the six vertices (the parameter sets reuse them).
+template <bool PH, bool POLAR, bool OUT = false>
 __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *rec, F2 dn, float ex,
                                                 float dnorm, const EpiData &d, int64_t voff, int q,
-                                                const YOcc &yo, float *ys, const float2 *glb, float2 unm) {
+                                                const YOcc &yo, float *ys, const float2 *glb, float2 unm,
+                                                float *g2o = nullptr) {
   float acc = 0.f;
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
@@ -1670,12 +1711,18 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
     cfmaf(g, make_float2(u45.z, u45.w), h[5]);
     if (POLAR) cfmaf(g, __ldg(glb + s * 32), unm);
     // sc = (cx, bose, -, -)
-    const float g2c = (g.x * g.x + g.y * g.y) * sc.x;
+    const float g2c = __fmul_rn(__fmaf_rn(g.x, g.x, __fmul_rn(g.y, g.y)), sc.x);
+    if (OUT) g2o[s] = g2c;
     // PH: the Gaussians x 2^64 (the phonon side's sums keep their tails)
     const VtxF f = vtx_factors<PH>(dn, ex, yo.emx, wv, sc.y, dnorm);
-    const float xp = g2c * f.ap * (PH ? f.dp * TWO_M64 : f.dp);
-    const float xm = g2c * f.am * (PH ? f.dm * TWO_M64 : f.dm);
-    acc += xp + xm;
+    float xp, xm;
+    if (PH) {
+      xp = g2c * f.ap * (f.dp * TWO_M64);
+      xm = g2c * f.am * (f.dm * TWO_M64);
+      acc += xp + xm;
+    } else {
+      acc = __fadd_rn(acc, vtx_x(g2c, f, xp, xm));
+    }
     if (PH) ys[s] = fmaf(g2c, f.dp, ys[s]);   // the Gaussian is even: delta(E' - omega - E) is dp (x 2^64)
     if (d.g2) {
       const int64_t off = voff + s;
@@ -1687,6 +1734,23 @@ __device__ __forceinline__ float fused_vertices(const float2 *h, const float4 *r
         if (PH && d.yv) d.yv[off] = TWO_M64D * (double)((g2c * f.dp) * y_factor(yo, sc.y));
       }
     }
+  }
+  return acc;
+}
+
+// The electron side's X+ + X- of one (k', n) final state under another
+// parameter set, from the six |g|^2 cx of fused_vertices<..., OUT>: that set's
+// dn, e^x, e^-x, dnorm and mode factors (mrec = the lane's entry of field 0 of
+// q's block of the set's mode table: (w, e^v, bose)), vertex factors as there.
+__device__ __forceinline__ float fused_set_band(const float *g2c, const float4 *mrec, F2 dn, float ex, float emx,
+                                                float dnorm) {
+  float acc = 0.f;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const float4 wb = __ldg(mrec + s * 32);
+    const VtxF f = vtx_factors<false>(dn, ex, emx, wb, wb.w, dnorm);
+    float xp, xm;
+    acc = __fadd_rn(acc, vtx_x(g2c[s], f, xp, xm));
   }
   return acc;
 }
@@ -1715,10 +1779,13 @@ static inline int fused_bands(int64_t phase_bytes, int mpairs) {
 
 // PH: the phonon side too (Y of every vertex into the ph-e rate of its (q, s)).
 // POLAR: the long-range term of polar crystals in every vertex.
-template <bool PH, bool POLAR>
+// SETS: the electron side's rates under the parameter sets 1..xs.n-1 as well
+// (not with PH); each set's partials are formed in the same order as set 0's.
+template <bool PH, bool POLAR, bool SETS>
 __global__ void __launch_bounds__(F_THREADS, 1)
     k_stageB_fused86(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, FusedArgs g,
-                     FusedTabs tb, RateParams rp, EpiData d) {
+                     FusedTabs tb, RateParams rp, EpiData d, FusedSets xs) {
+  static_assert(!(PH && SETS), "parameter sets are an electron-side form");
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + F_STAGES * F_STAGE);
@@ -1836,7 +1903,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   } else {   // ---- epilogue: warps 2..9
     const int quad = warp & 3, slot = (warp - 2) >> 2;
     const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
-    const double inv_sig = 1.0 / rp.sigma;
+    // dn = (E - E') / sigma as the double-float product of E - E' and 1 / sigma,
+    // formed the same way for the parameter sets (FusedSets)
+    const F2 isg = f2_of(1.0 / rp.sigma);
     const float dnorm = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / rp.sigma * rp.inv_nk);
     const int m0 = rp.mesh[0], m1 = rp.mesh[1], m2 = rp.mesh[2];
     int it = 0;
@@ -1889,6 +1958,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       const int64_t vbase = (nbw > 0 && d.g2) ? (int64_t)j * d.per_state + (int64_t)ri.z * 6 : 0;
       float acc = 0.f;
       float ys[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float accr[SETS ? MAX_SETS : 1];   // the other sets' sums over the bands after n0, n1
+      if (SETS)
+        for (int p = 0; p < MAX_SETS; ++p) accr[p] = 0.f;
       if (!mbar_wait(tfull, it & 1, g.err)) break;
       tc_fence_after();
       // ---- drain: h for the first two window bands
@@ -1919,13 +1991,23 @@ __global__ void __launch_bounds__(F_THREADS, 1)
             if (mine) hx[sp] = hrot(ux, gre, gim);
           }
           if (mine) {
-            const F2 dn = f2_of((E - __ldg(eb + nb_ * 32)) * inv_sig);
+            const F2 dn = f2_mul(f2_of(E - __ldg(eb + nb_ * 32)), isg);
             float2 unmx = make_float2(0.f, 0.f);
             if (POLAR)
 #pragma unroll
               for (int c = 0; c < 8; ++c) cfmaf_cj(unmx, ux[c], __ldg(Uk + c));
-            acc += fused_vertices<PH, POLAR>(hx, rq, dn, ex, dnorm, d, vbase + (int64_t)b * 6, q, yo, ys, glb,
-                                             unmx);
+            float g2x[6];
+            acc = __fadd_rn(acc, fused_vertices<PH, POLAR, SETS>(hx, rq, dn, ex, dnorm, d, vbase + (int64_t)b * 6, q,
+                                                                 yo, ys, glb, unmx, g2x));
+            if (SETS) {
+              const F2 dd = f2_of(E - __ldg(eb + nb_ * 32));
+              for (int p = 1; p < xs.n; ++p) {
+                const float2 oc = xs.occ[(size_t)(p - 1) * g.nst + j];
+                accr[p] = __fadd_rn(accr[p], fused_set_band(g2x, xs.mode + (p - 1) * xs.mode_stride + blk32(q, 6, 0),
+                                                            f2_mul(dd, F2{xs.isg_hi[p], xs.isg_lo[p]}), oc.x, oc.y,
+                                                            xs.dnorm[p]));
+              }
+            }
           }
         }
       }
@@ -1933,17 +2015,36 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       mbar_arrive(tempty);
       // ---- vertices of the first two bands, overlapping the next tile's MMAs
       float acc01 = 0.f;
+      float g2a[SETS ? 6 : 1], g2b[SETS ? 6 : 1];   // |g|^2 cx of the first two bands, for the other sets
       if (nbw > 0) {
-        const F2 dn = f2_of((E - __ldg(eb + n0 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH, POLAR>(h0, rq, dn, ex, dnorm, d, vbase, q, yo, ys, glb, unm0);
+        const F2 dn = f2_mul(f2_of(E - __ldg(eb + n0 * 32)), isg);
+        acc01 = __fadd_rn(acc01,
+                          fused_vertices<PH, POLAR, SETS>(h0, rq, dn, ex, dnorm, d, vbase, q, yo, ys, glb, unm0, g2a));
       }
       if (nbw > 1) {
-        const F2 dn = f2_of((E - __ldg(eb + n1 * 32)) * inv_sig);
-        acc01 += fused_vertices<PH, POLAR>(h1, rq, dn, ex, dnorm, d, vbase + 6, q, yo, ys, glb, unm1);
+        const F2 dn = f2_mul(f2_of(E - __ldg(eb + n1 * 32)), isg);
+        acc01 = __fadd_rn(acc01, fused_vertices<PH, POLAR, SETS>(h1, rq, dn, ex, dnorm, d, vbase + 6, q, yo, ys,
+                                                                  glb, unm1, g2b));
       }
       double v = (double)acc01 + (double)acc;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0 && jvalid) g.partial[(size_t)j * g.nblk + mt * 4 + quad] = v;
+      if (SETS) {   // the same sums under the other parameter sets
+        const F2 dd0 = f2_of(E - __ldg(eb + n0 * 32)), dd1 = f2_of(E - __ldg(eb + n1 * 32));
+        for (int p = 1; p < xs.n; ++p) {
+          float a01 = 0.f;
+          if (jvalid && nbw > 0) {
+            const float2 oc = xs.occ[(size_t)(p - 1) * g.nst + j];
+            const F2 isgp{xs.isg_hi[p], xs.isg_lo[p]};
+            const float4 *mq = xs.mode + (p - 1) * xs.mode_stride + blk32(q, 6, 0);
+            a01 = __fadd_rn(a01, fused_set_band(g2a, mq, f2_mul(dd0, isgp), oc.x, oc.y, xs.dnorm[p]));
+            if (nbw > 1) a01 = __fadd_rn(a01, fused_set_band(g2b, mq, f2_mul(dd1, isgp), oc.x, oc.y, xs.dnorm[p]));
+          }
+          double vp = (double)a01 + (double)accr[p];
+          for (int o = 16; o > 0; o >>= 1) vp += __shfl_down_sync(0xffffffffu, vp, o);
+          if (lane == 0 && jvalid) xs.partial[p][(size_t)j * g.nblk + mt * 4 + quad] = vp;
+        }
+      }
       if (PH && jvalid && nbw > 0 && d.phr) {   // this pair's Y into the rates of (q, s), s = 0..5
 #pragma unroll
         for (int s = 0; s < 6; ++s) {
@@ -1997,7 +2098,7 @@ static int launch_pairs(const void *kernel, int smem, int64_t pairs, cudaStream_
 
 static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2, int KpB, int nwv, int nst,
                           const RateParams &rp, const EpiData &ed, const FusedTabs &tabs, double *partial, int nblk,
-                          int *err, cudaStream_t st, int chunk, const Yield &yield) {
+                          int *err, cudaStream_t st, int chunk, const Yield &yield, const FusedSets &xs) {
   if (MpB % BM || Np2 % FBN || KpB % BK) return tfail(1, "stage B: shapes not tile multiples");
   if (4 * (int64_t)MpB > INT32_MAX || 6 * Np2 > INT32_MAX) return tfail(1, "stage B: operand too tall for TMA coords");
   CUtensorMap ta, tb;
@@ -2006,12 +2107,15 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
   // once per process: changing a kernel attribute can wait for the device's queued work
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
-    cudaFuncSetAttribute(k_stageB_fused86<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
-    cudaFuncSetAttribute(k_stageB_fused86<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
-    cudaFuncSetAttribute(k_stageB_fused86<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
-    cudaFuncSetAttribute(k_stageB_fused86<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
+    cudaFuncSetAttribute(k_stageB_fused86<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM);
   });
-  const bool ph = ed.phr || ed.yv, polar = tabs.glb != nullptr;
+  const bool ph = ed.phr || ed.yv, polar = tabs.glb != nullptr, sets = xs.n > 1;
+  if (ph && sets) return tfail(1, "stage B: parameter sets are an electron-side form");
   FusedArgs g;
   g.mtiles = MpB / BM;
   g.ntiles = (nst + 1) / 2;
@@ -2033,11 +2137,12 @@ static int stageB_fused86(const float *PB, int MpB, const float *B2, int64_t Np2
                         [&](cudaLaunchConfig_t &cfg, int t0, int t1) {
                           g.t0 = t0;
                           g.t1 = t1;
-                          return cudaLaunchKernelEx(&cfg, kernel, ta, tb, g, tabs, rp, ed);
+                          return cudaLaunchKernelEx(&cfg, kernel, ta, tb, g, tabs, rp, ed, xs);
                         });
   };
-  if (polar) return ph ? run(k_stageB_fused86<true, true>) : run(k_stageB_fused86<false, true>);
-  return ph ? run(k_stageB_fused86<true, false>) : run(k_stageB_fused86<false, false>);
+  if (sets) return polar ? run(k_stageB_fused86<false, true, true>) : run(k_stageB_fused86<false, false, true>);
+  if (polar) return ph ? run(k_stageB_fused86<true, true, false>) : run(k_stageB_fused86<false, true, false>);
+  return ph ? run(k_stageB_fused86<true, false, false>) : run(k_stageB_fused86<false, false, false>);
 }
 
 // ------------------------------- stage A fused with the initial-band rotation
@@ -2391,7 +2496,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
                                cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
                                std::mutex *build_mu, int chunk_us, const Yield &yield, const BatchMember *bm,
-                               int64_t chunk_bytes) {
+                               int64_t chunk_bytes, const RateSets *sets) {
   int rc;
   const int KpA = (int)rup(nwsk, BK), KpB = (int)rup(nwsq, BK);
   const int64_t NpA = rup(Nn, BN);
@@ -2508,6 +2613,31 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   EpiData ed = ed_in;
   ed.Uf = et.Uf;
   QTab qt{et.cx, et.bs, et.wv};
+  // the other parameter sets: their mode tables; no vertex lists
+  const int nsets = sets ? sets->n : 1;
+  QTab qts[MAX_SETS];
+  qts[0] = qt;
+  if (nsets > 1) {
+    const int N = rp.N;
+    float *cxp, *bsp;
+    float4 *wvp;
+    if ((rc = wsget(ws, "tc_scx", (size_t)N * nb, &cxp)) || (rc = wsget(ws, "tc_sbs", (size_t)(nsets - 1) * N * nb, &bsp)) ||
+        (rc = wsget(ws, "tc_swv", (size_t)(nsets - 1) * N * nb, &wvp)))
+      return tfail(6, ws.msg.c_str());
+    for (int p = 1; p < nsets; ++p) {
+      const RateParams &r = sets->rp[p];
+      float *bs = bsp + (size_t)(p - 1) * N * nb;
+      float4 *wv = wvp + (size_t)(p - 1) * N * nb;
+      k_qtab<<<(N * nb + 255) / 256, 256, 0, st>>>(N * nb, ed_in.om, sets->bose[p], r.sigma, kB * r.T, r.const_tp,
+                                                    cxp, bs, wv);
+      TCK(cudaGetLastError());
+      *launches += 1;
+      qts[p] = QTab{et.cx, bs, wv};
+    }
+  }
+  const RateParams &rp0 = rp;
+  double *const partial0 = partial;
+  const EpiData eds = ed, eds_in = ed_in;
   for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
@@ -2518,6 +2648,16 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     tB->end(st);
     const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
     const bool rows_kernel = rp.delta_kind == 0 && nb <= EPR_NB && (nw == 8 || nw == 16 || nw == 24 || nw == 32);
+    for (int set = 0; set < nsets; ++set) {   // one epilogue per parameter set over the same GEMM output
+    const RateParams &rp = set ? sets->rp[set] : rp0;
+    const QTab &qt = qts[set];
+    double *partial = set ? sets->partial[set] : partial0;
+    EpiData ed = eds, ed_in = eds_in;
+    if (set) {
+      ed.bose = ed_in.bose = sets->bose[set];
+      ed.g2 = ed.xp = ed.xm = ed.yv = ed_in.g2 = ed_in.xp = ed_in.xm = ed_in.yv = nullptr;
+      ed.phr = ed_in.phr = nullptr;
+    }
     if (rows_kernel) {
       dim3 grid(nblk, ns);
       if (nw == 8)
@@ -2548,7 +2688,9 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     } else {
       launch_epilogue_fp32(nwv, (int)j0, (int)j0 + ns, CBr, CBi, NpC, rp, ed_in, partial, nblk, st);
     }
-    *launches += 2;
+    *launches += 1;
+    }
+    *launches += 1;
   }
   return 0;
 }
@@ -2563,7 +2705,7 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
                                const int *kposA, const int *Rq, const double *degq, const int *kposB, const double2 *U,
                                const RateParams &rp, const EpiData &ed_in, double *partial, int nblk, int *err,
                                cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
-                               std::mutex *build_mu, int chunk_us, const Yield &yield) {
+                               std::mutex *build_mu, int chunk_us, const Yield &yield, const RateSets *sets) {
   int rc;
   const int ncol = 48;
   const int KpA = (int)rup(nwsk, 16), KpB = (int)rup(nwsq, 16);
@@ -2626,6 +2768,37 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
     *launches += 1;
   }
   const FusedTabs tabs{trow, tst, tU4, tens, trec, tglb, Mp, N};
+  // the other parameter sets' state and mode tables
+  FusedSets xs{};
+  xs.n = sets ? sets->n : 1;
+  if (xs.n > 1) {
+    float2 *occ;
+    float4 *mode, *wvp;
+    float *cxp, *bsp;
+    const int64_t mstride = (int64_t)6 * rup(N, 32);
+    if ((rc = wsget(ws, "tc_socc", (size_t)(xs.n - 1) * nst, &occ)) ||
+        (rc = wsget(ws, "tc_smode", (size_t)(xs.n - 1) * mstride, &mode)) ||
+        (rc = wsget(ws, "tc_scx", (size_t)N * 6, &cxp)) || (rc = wsget(ws, "tc_sbs", (size_t)N * 6, &bsp)) ||
+        (rc = wsget(ws, "tc_swv", (size_t)N * 6, &wvp)))
+      return tfail(6, ws.msg.c_str());
+    for (int p = 1; p < xs.n; ++p) {
+      const RateParams &r = sets->rp[p];
+      k_qtab<<<(N * 6 + 255) / 256, 256, 0, st>>>(N * 6, ed_in.om, sets->bose[p], r.sigma, kB * r.T, r.const_tp, cxp,
+                                                  bsp, wvp);
+      k_fused_set_tabs<<<(std::max(nst, N * 6) + 127) / 128, 128, 0, st>>>(
+          nst, N, tst, r.chempot, kB * r.T, bsp, wvp, occ + (size_t)(p - 1) * nst, mode + (p - 1) * mstride);
+      TCK(cudaGetLastError());
+      *launches += 2;
+      const F2 isg = f2_of(1.0 / r.sigma);
+      xs.isg_hi[p] = isg.hi;
+      xs.isg_lo[p] = isg.lo;
+      xs.dnorm[p] = (float)((1.0 / sqrt(2.0 * 3.141592653589793)) / r.sigma * r.inv_nk);
+      xs.partial[p] = sets->partial[p];
+    }
+    xs.occ = occ;
+    xs.mode = mode;
+    xs.mode_stride = mstride;
+  }
   // stage A's row tables: the window rows, or the A-rows with their first states
   FusedTabs tabsA = tabs;
   if (own_a) {
@@ -2703,7 +2876,7 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   ed.Uf = et.Uf;
   tB->begin(st);
   if ((rc = stageB_fused86(PB, Mp, B2, Np2, KpB, nwv, nst, rp, ed, tabs, partial, nblk, err, st,
-                           chunk_us > 0 ? std::max(1, chunk_us / 13) : 0, yield)))
+                           chunk_us > 0 ? std::max(1, chunk_us / 13) : 0, yield, xs)))
     return rc;
   tB->end(st);
   (*launches)++;
@@ -2718,7 +2891,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       const double2 *U, const RateParams &rp, const EpiData &ed_in, double *partial, int nblk_max,
                       int *nblk_used, cudaEvent_t ev_stage_a, int64_t *launches, LaunchTimer *tA, LaunchTimer *tB,
                       std::mutex *build_mu, int chunk_us, const Yield &yield, const BatchMember *bm,
-                      int64_t chunk_bytes) {
+                      int64_t chunk_bytes, const RateSets *sets) {
   // The fused path packs mesh coordinates in 10 bits each.
   const bool fast86 = (nw == 8 && nb == 6 && rp.delta_kind == 0 && mesh[0] <= 1024 && mesh[1] <= 1024 &&
                        mesh[2] <= 1024);
@@ -2734,13 +2907,13 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
   if (fast86) {
     if ((rc = split_rates_fused86(s, ws, st, G64, nwsk, nwsq, Nn, nwv, nst, mesh, L, roots, widx, arow, nA, st_code,
                                   first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in, partial, nblk, err,
-                                  ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield)))
+                                  ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield, sets)))
       return rc;
   } else if ((rc = split_rates_generic(s, ws, st, G64, nwsk, nwsq, Nn, nw, nb, nwv, nst, mesh, L, roots, widx, arow,
                                        nA, st_code, first_state, Rk, degk, kposA, Rq, degq, kposB, U, rp, ed_in,
                                        partial, nblk, err,
                                        ev_stage_a, launches, tA, tB, build_mu, chunk_us, yield, bm,
-                                       std::max<int64_t>(chunk_bytes, (int64_t)1 << 24)))) {
+                                       std::max<int64_t>(chunk_bytes, (int64_t)1 << 24), sets))) {
     return rc;
   }
   int herr = 0;

@@ -68,7 +68,7 @@ int split_rates_stage(SplitOperands &s, Workspace &ws, cudaStream_t st, const do
                       double *partial, int nblk_max, int *nblk_used, cudaEvent_t ev_stage_a,
                       int64_t *launches, LaunchTimer *tA, LaunchTimer *tB, std::mutex *build_mu,
                       int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr,
-                      int64_t chunk_bytes = (int64_t)1 << 31);
+                      int64_t chunk_bytes = (int64_t)1 << 31, const RateSets *sets = nullptr);
 
 }  // namespace tc
 }  // namespace ephg

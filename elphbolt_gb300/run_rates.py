@@ -11,8 +11,10 @@ large instance (6-atom cell, nw = 32, nb = 18, 279 + 279 WS cells, 23 GB of
 g(Re,Rp)); the window is +-0.5 eV (--window) about mid-gap + 0.6 eV,
 Gaussian delta 10 meV, 300 K.  --side el runs
 ephg_el_rates (electron RTA rates), --side ph runs ephg_ph_rates with the
-electron rates (both sides in one sweep).  Useful for quick checks and for
-profiling a smaller case of the same kernels as the benchmark.
+electron rates (both sides in one sweep); --sets K > 1 runs ephg_el_rates_sets
+on K requests at temperatures spread over 100-600 K (one contraction, an
+epilogue per temperature).  Useful for quick checks and for profiling a smaller
+case of the same kernels as the benchmark.
 """
 from __future__ import annotations
 
@@ -31,6 +33,7 @@ def main(argv=None):
     ap.add_argument("--side", choices=["el", "ph"], default="el")
     ap.add_argument("--crystal", choices=["si", "sic", "large"], default="si")
     ap.add_argument("--window", type=float, default=0.5, help="window half width, eV")
+    ap.add_argument("--sets", type=int, default=1, help="temperatures sharing one contraction (electron side)")
     a = ap.parse_args(argv)
     from . import _lib, build, synthetic as S
     from .wannier import Wannier
@@ -46,12 +49,20 @@ def main(argv=None):
     W = Wannier(wd)
     prec = _lib.PREC_SPLIT_TF32 if a.precision == "split" else _lib.PREC_FP64
     for i in range(a.repeat):
+        sets = 1
         if a.side == "ph":
             out = W.ph_rates(req, precision=prec, electrons=True)
+        elif a.sets > 1:
+            reqs = [S.RateRequest(mesh=req.mesh, enref=req.enref, fsthick=req.fsthick, chempot=req.chempot, T=T,
+                                  delta_kind=req.delta_kind, sigma=req.sigma)
+                    for T in [100.0 + 500.0 * k / (a.sets - 1) for k in range(a.sets)]]
+            out = W.el_rates_sets(reqs, precision=prec)[0]
+            sets = a.sets
         else:
             out = W.el_rates(req, precision=prec)
         st = out["stats"]
-        st["vertices_per_s"] = st["vertices"] / (st["ms_total"] * 1e-3)
+        st["sets"] = sets
+        st["vertices_per_s"] = sets * st["vertices"] / (st["ms_total"] * 1e-3)
         st["repeat"] = i
         print(json.dumps(st), flush=True)
     W.deallocate_wannier()

@@ -64,6 +64,10 @@ class Server:
         return dict(nwv=nwv, indexlist=idx[:nwv].copy(), rates=np.asfortranarray(rates[:nwv]), stats=st.as_dict(),
                     latency_ms=lat.value)
 
+    def set_merge(self, max_sets: int):
+        """Requests per merged run (``ephg_server_set_merge``); 1 turns merging off."""
+        check(self._L.ephg_server_set_merge(self._s, int(max_sets)))
+
     def stats(self) -> dict:
         s = _lib.ServerStats()
         check(self._L.ephg_server_stats_get(self._s, ct.byref(s)))
@@ -81,20 +85,23 @@ class Server:
             pass
 
 
-def selftest(meshes, nslots=1, service_ms=1.0, budget=10 ** 9, per_request_bytes=1000):
-    """Run the server's slots / queue / admission / GPU hand-over / statistics
-    against a simulated executor (no GPU; ``ephg_debug_server_selftest``).
-    Returns (status, statistics incl. per-request latency_ms, most requests in
-    flight at once)."""
+def selftest(meshes, nslots=1, service_ms=1.0, budget=10 ** 9, per_request_bytes=1000, temps=None, max_sets=0):
+    """Run the server's slots / queue / admission / GPU hand-over / merging /
+    statistics against a simulated executor (no GPU;
+    ``ephg_debug_server_selftest``).  ``temps``: per-request T, which makes
+    requests mergeable.  Returns (status, statistics incl. per-request
+    latency_ms, most requests in flight at once)."""
     L = _lib.load()
-    L.ephg_debug_server_selftest.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_int64, ct.c_int64, c_i64p,
-                                             ct.POINTER(_lib.ServerStats), ct.POINTER(ct.c_int), c_dp]
+    L.ephg_debug_server_selftest.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_int64, ct.c_int64, c_i64p, c_dp,
+                                             ct.c_int, ct.POINTER(_lib.ServerStats), ct.POINTER(ct.c_int), c_dp]
     m = np.ascontiguousarray(meshes, dtype=np.int64)
+    tp = None if temps is None else np.ascontiguousarray(temps, dtype=np.float64)
     out = _lib.ServerStats()
     mc = ct.c_int()
     lat = np.zeros(len(m))
     rc = L.ephg_debug_server_selftest(len(m), int(nslots), float(service_ms), int(budget), int(per_request_bytes),
-                                      m.ctypes.data_as(c_i64p), ct.byref(out), ct.byref(mc), lat.ctypes.data_as(c_dp))
+                                      m.ctypes.data_as(c_i64p), None if tp is None else tp.ctypes.data_as(c_dp),
+                                      int(max_sets), ct.byref(out), ct.byref(mc), lat.ctypes.data_as(c_dp))
     d = out.as_dict()
     d["latency_ms"] = lat
     return rc, d, mc.value

@@ -229,6 +229,24 @@ class Wannier:
             out.update(g2=g2[:nv], xp=xp[:nv], xm=xm[:nv])
         return out
 
+    def el_rates_sets(self, reqs, precision=_lib.PREC_FP64):
+        """``el_rates`` for requests that differ only in T, sigma and chempot
+        (``ephg_el_rates_sets``): one contraction, one rate epilogue per request.
+        Returns one output per request, laid out as ``el_rates``'s; the
+        indexlist and stats are common to all."""
+        n = len(reqs)
+        R = (_lib.RateRequest * n)(*[_rate_request(q, precision) for q in reqs])
+        N = int(np.prod(reqs[0].mesh))
+        nw = self.numwannbands
+        rates = [np.zeros((N, nw), order="F") for _ in range(n)]
+        RP = (c_dp * n)(*[_p(a) for a in rates])
+        idx = np.zeros(N, dtype=np.int64)
+        st = _lib.RateStats()
+        check(self._L.ephg_el_rates_sets(self._h, n, R, RP, _p(idx, c_i64p), ct.byref(st)))
+        nwv = int(st.nwv)
+        return [dict(nwv=nwv, indexlist=idx[:nwv].copy(), rates=np.asfortranarray(r[:nwv]), stats=st.as_dict(),
+                     nstates=int(st.nstates), vertices=int(st.vertices)) for r in rates]
+
     def average_degenerate(self, req, g2, mode=_lib.DEGAVG_MEAN, thres=1e-6):
         """Degenerate-subspace gauge fixing of an ``el_rates`` |g|^2 vertex list
         (``ephg_g2_average_degenerate``; plot_along_path, wannier.f90:1332-1384):

@@ -197,6 +197,18 @@ int ephg_el_rates(ephg_handle *h, const ephg_rate_request *req, double *rates,
                   int64_t *indexlist, ephg_rate_stats *stats, double *g2, double *xplus,
                   double *xminus, int64_t cap);
 
+/* ephg_el_rates for nsets requests (1 <= nsets <= EPHG_MAX_SETS) that differ
+ * only in T, sigma and chempot: mesh, window (enref, fsthick), delta_kind
+ * and precision equal, else EPHG_ERR_ARG.  The vertices and |g|^2 depend on
+ * none of the three, so the contractions run once and the rate epilogue once
+ * per set: rates[i] (N_k,nw) receives what ephg_el_rates returns for reqs[i];
+ * indexlist and stats (nullable; stats counts one set's vertices) are common.
+ * The reference takes one temperature and chemical potential per run
+ * (input.nml); a sweep over them there is one run per point. */
+#define EPHG_MAX_SETS 8
+int ephg_el_rates_sets(ephg_handle *h, int64_t nsets, const ephg_rate_request *reqs, double *const *rates,
+                       int64_t *indexlist, ephg_rate_stats *stats);
+
 /* calculate_eph_interaction_ibzq 'g' + 'Y' (interactions.f90:1673-1930, the 'Y'
  * pass as calculate_Y_OTF :1932-2093) fused with the ph-e part of
  * calculate_ph_rta_rates (interactions.f90:2723-2828), identity point group,
@@ -249,11 +261,14 @@ int ephg_g2_average_degenerate(ephg_handle *h, const ephg_rate_request *req, int
  * cannot fit; a request that does not fit its slot's share waits for the other
  * slots to go idle (no new request starts meanwhile), takes the whole budget,
  * and fails with EPHG_ERR_NOMEM before allocating only if that is still too
- * little.  A free slot takes the waiting request of least estimated work (the
- * oldest once it has waited a second); a request much smaller than a running
+ * little.  A free slot takes the waiting request of highest response ratio
+ * (its age over its estimated isolated solve time, from a per-crystal fit of
+ * the solve times seen), with the queued requests that can share its
+ * contraction (ephg_server_set_merge); a request much smaller than a running
  * one runs on a high-priority stream, and served requests run their persistent
- * kernels as launches of a few ms so that it gets the SMs at the next launch
- * boundary.  Latency is the wall time from ephg_submit to completion. */
+ * kernels as launches of a few ms, between which the GPU goes to the running
+ * request of highest ratio.  Latency is the wall time from ephg_submit to
+ * completion. */
 typedef struct ephg_server ephg_server;
 
 #define EPHG_TICKET_QUEUED 0
@@ -268,6 +283,7 @@ typedef struct {
   double wall_s;                /* first submit -> last completion */
   double vertices_per_s;        /* vertices / wall_s */
   int64_t peak_device_bytes;    /* largest resident + workspace total seen after a request */
+  int64_t merged;               /* completed requests that shared another request's contraction */
 } ephg_server_stats;
 
 int ephg_server_create(ephg_handle *const *crystals, int ncrystals, int64_t hbm_budget_bytes, int nslots,
@@ -285,6 +301,12 @@ int ephg_poll(ephg_server *s, int64_t ticket, int *state);
 int ephg_wait(ephg_server *s, int64_t ticket, double *rates, int64_t *indexlist, ephg_rate_stats *stats,
               double *latency_ms);
 int ephg_server_stats_get(ephg_server *s, ephg_server_stats *out);
+/* Merging (default EPHG_MAX_SETS): a free slot that takes a request also
+ * takes, up to max_sets in all, the queued requests of the same crystal that
+ * differ from it only in T, sigma and chempot, and runs them as one
+ * ephg_el_rates_sets call (one contraction, an epilogue per request); each
+ * result still equals its request run alone.  max_sets = 1 turns it off. */
+int ephg_server_set_merge(ephg_server *s, int max_sets);
 
 /* ---- Batched form ----
  * No counterpart in the reference (one crystal, one request per run).  n rate

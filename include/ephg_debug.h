@@ -40,9 +40,14 @@ int ephg_debug_wait_timeout(int64_t limit_cycles, int64_t arrive, int *device_er
  * 0 is submitted 0.2 ms before the others.  Fills *out with the server's
  * statistics, *max_concurrent with the most requests seen in flight at once
  * and lat_ms[i] (nullable) with each request's latency (-1: refused or
- * failed); returns EPHG_ERR_INDEX if a result reached the wrong ticket. */
+ * failed); returns EPHG_ERR_INDEX if a result reached the wrong ticket.
+ * temps (nullable): request i's T, which makes it mergeable with the queued
+ * requests of its crystal and mesh (ephg_server_set_merge; max_sets in
+ * 1..EPHG_MAX_SETS, else the default); a merged run takes one request's
+ * simulated time and writes crystal + 1000 T as each request's result. */
 int ephg_debug_server_selftest(int nreq, int nslots, double service_ms, int64_t budget, int64_t per_request_bytes,
-                               const int64_t *meshes, ephg_server_stats *out, int *max_concurrent, double *lat_ms);
+                               const int64_t *meshes, const double *temps, int max_sets, ephg_server_stats *out,
+                               int *max_concurrent, double *lat_ms);
 
 /* The batched form's round logic (the grouped launches' gate) under nmembers
  * host threads, no GPU: members alternate active stretches of 1-4 submissions

@@ -68,7 +68,7 @@ module ephg_c
   type, bind(C) :: ephg_server_stats
      integer(c_int64_t) :: submitted, completed, failed, rejected, vertices
      real(c_double) :: p50_ms, p99_ms, max_ms, mean_ms, wall_s, vertices_per_s
-     integer(c_int64_t) :: peak_device_bytes
+     integer(c_int64_t) :: peak_device_bytes, merged
   end type ephg_server_stats
 
   interface
@@ -167,6 +167,15 @@ module ephg_c
        integer(c_int64_t), value :: cap
      end function ephg_el_rates
 
+     integer(c_int) function ephg_el_rates_sets(h, nsets, reqs, rates, indexlist, stats) &
+          bind(C, name="ephg_el_rates_sets")
+       !! nsets (<= 8) requests equal but for T, sigma and chempot: one contraction;
+       !! reqs: nsets requests; rates: an array of nsets C pointers (c_loc of each (N,nw) array)
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: h, reqs, rates, indexlist, stats
+       integer(c_int64_t), value :: nsets
+     end function ephg_el_rates_sets
+
      integer(c_int) function ephg_ph_rates(h, req, spindeg, rates_phe, el_rates, indexlist, stats, &
           g2, y, cap) bind(C, name="ephg_ph_rates")
        import :: c_int, c_ptr, c_int64_t, ephg_rate_request
@@ -236,6 +245,12 @@ module ephg_c
        type(c_ptr), value :: srv, rates, indexlist, stats, latency_ms
        integer(c_int64_t), value :: ticket
      end function ephg_wait
+
+     integer(c_int) function ephg_server_set_merge(srv, max_sets) bind(C, name="ephg_server_set_merge")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: srv
+       integer(c_int), value :: max_sets
+     end function ephg_server_set_merge
 
      integer(c_int) function ephg_server_stats_get(srv, st) bind(C, name="ephg_server_stats_get")
        import :: c_int, c_ptr, ephg_server_stats

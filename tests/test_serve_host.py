@@ -59,3 +59,32 @@ def test_nearest_rank_percentiles():
     rc, st, _ = serve.selftest([4] * 100, nslots=1, service_ms=0.2, budget=10 ** 9, per_request_bytes=1)
     assert rc == _lib.EPHG_OK and st["completed"] == 100
     assert st["p99_ms"] >= st["p50_ms"] * 1.5         # all submitted at once: latency grows with queue position
+
+
+def test_queued_requests_of_one_crystal_and_mesh_merge():
+    # request 0 starts alone; the others queue behind it on one slot.  Requests
+    # of one crystal and mesh that differ only in T share a run, and each gets
+    # its own result (the fake writes crystal + 1000 T).
+    meshes = [8] + [8, 8, 12, 8, 8, 12, 8, 8]
+    temps = [100.0 + 10 * i for i in range(len(meshes))]
+    rc, st, _ = serve.selftest(meshes, nslots=1, service_ms=2.0, temps=temps)
+    assert rc == _lib.EPHG_OK                          # every result reached its own ticket
+    assert st["completed"] == len(meshes) and st["failed"] == 0
+    assert st["merged"] >= 4
+    rc1, st1, _ = serve.selftest(meshes, nslots=1, service_ms=2.0, temps=temps, max_sets=1)
+    assert rc1 == _lib.EPHG_OK and st1["completed"] == len(meshes) and st1["merged"] == 0
+    assert st["max_ms"] < 0.7 * st1["max_ms"]          # merged runs take one request's time
+
+
+def test_merge_respects_max_sets():
+    meshes = [8] * 12
+    temps = [100.0 + i for i in range(12)]
+    rc, st, _ = serve.selftest(meshes, nslots=1, service_ms=1.0, temps=temps, max_sets=3)
+    assert rc == _lib.EPHG_OK and st["completed"] == 12
+    # request 0 alone, then 11 queued in runs of at most 3: at most 2 merged per run
+    assert 0 < st["merged"] <= 2 * 4
+
+
+def test_requests_without_a_valid_temperature_do_not_merge():
+    rc, st, _ = serve.selftest([8] * 6, nslots=1, service_ms=0.5)   # T = 0
+    assert rc == _lib.EPHG_OK and st["completed"] == 6 and st["merged"] == 0
