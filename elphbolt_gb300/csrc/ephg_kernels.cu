@@ -157,7 +157,132 @@ void launch_zgemm(int M, int N, int K, const double2 *A, int64_t lda, const doub
 // round-robin ordering: n/2 disjoint rotations per step, n-1 steps per sweep
 // (Golub & Van Loan sec. 8.5.4).  Stands in for zheev('V','U') at
 // wannier.f90:489 and :732.
+//
+// Mixed precision, because GB300's FP64 rate is a sixtieth of its FP32 rate:
+//  1. FP32 sweeps bring the matrix to near-diagonal form (off-diagonal norm
+//     ~1e-5 of the total) and accumulate their rotations in Q;
+//  2. two Newton-Schulz steps X <- X (3I - X^H X) / 2 in FP64 make Q unitary to
+//     FP64 rounding (from ~1e-6);
+//  3. B = Q^H A Q in FP64 has A's eigenvalues to FP64 rounding;
+//  4. FP64 sweeps on B, accumulating into V = Q, converge quadratically from
+//     there: two or three sweeps instead of six or seven from A.
 constexpr int EIG_MAXSWEEP = 40;
+constexpr int EIG_MAXSWEEP32 = 12;
+
+// round-robin pair `lane` (< m / 2) of step r, m players: (p, q) with p < q
+__device__ __forceinline__ void rr_pair(int r, int m, int lane, int &p, int &q) {
+  int a, b;
+  if (lane == 0) {
+    a = 0;
+    b = (r % (m - 1)) + 1;
+  } else {
+    a = ((r + lane) % (m - 1)) + 1;
+    b = ((r - lane + (m - 1)) % (m - 1)) + 1;
+  }
+  p = min(a, b);
+  q = max(a, b);
+}
+
+// FP32 sweeps on A (float2, column-major n x n) accumulating into Q until the
+// off-diagonal norm is 1e-10 of the total or stalls below 1e-6 of it; P4 / PI:
+// the step's rotations (c, s, e^{i phi}) and pairs.
+__device__ void jacobi_f32(int n, float2 *A, float2 *Q, float4 *P4, int2 *PI, int lane) {
+  const int nn = n * n, m = n + (n & 1), half = m / 2;
+  float prev = INFINITY;
+  for (int sweep = 0; sweep < EIG_MAXSWEEP32; ++sweep) {
+    float off = 0.f, tot = 0.f;
+    for (int idx = lane; idx < nn; idx += 32) {
+      const float2 a = A[idx];
+      const float a2 = a.x * a.x + a.y * a.y;
+      tot += a2;
+      if (idx % n != idx / n) off += a2;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    // done at 1e-10 of the total, or once it stalls near FP32's floor; a
+    // non-finite norm also stops it (Q is then not used)
+    if (!(off > 1e-10f * tot) || (off <= 1e-6f * tot && off > 0.25f * prev)) return;
+    prev = off;
+    for (int r = 0; r < m - 1; ++r) {
+      if (lane < half) {
+        int p, q;
+        rr_pair(r, m, lane, p, q);
+        float c = 1.f, sn = 0.f, phx = 1.f, phy = 0.f;
+        if (q < n) {
+          const float2 apq = A[p + n * q];
+          const float rr = hypotf(apq.x, apq.y);
+          if (rr > 0.f) {
+            const float tau = (A[q + n * q].x - A[p + n * p].x) / (2.f * rr);
+            const float tf = fabsf(tau) > 1e18f ? 0.5f / tau
+                                                : (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+            c = rsqrtf(1.f + tf * tf);
+            sn = tf * c;
+            phx = apq.x / rr;
+            phy = apq.y / rr;
+          }
+        }
+        P4[lane] = make_float4(c, sn, phx, phy);
+        PI[lane] = make_int2(p, q < n ? q : -1);
+      }
+      __syncwarp();
+      // columns: A <- A J, Q <- Q J;  J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
+      for (int idx = lane; idx < half * n; idx += 32) {
+        const int k = idx / n, i = idx % n;
+        const int2 pq = PI[k];
+        if (pq.y < 0) continue;
+        const float4 r4 = P4[k];
+        const float2 aip = A[i + n * pq.x], aiq = A[i + n * pq.y];
+        float2 t = make_float2(r4.z * aiq.x + r4.w * aiq.y, r4.z * aiq.y - r4.w * aiq.x);
+        A[i + n * pq.x] = make_float2(r4.x * aip.x - r4.y * t.x, r4.x * aip.y - r4.y * t.y);
+        A[i + n * pq.y] = make_float2(r4.y * aip.x + r4.x * t.x, r4.y * aip.y + r4.x * t.y);
+        const float2 vip = Q[i + n * pq.x], viq = Q[i + n * pq.y];
+        t = make_float2(r4.z * viq.x + r4.w * viq.y, r4.z * viq.y - r4.w * viq.x);
+        Q[i + n * pq.x] = make_float2(r4.x * vip.x - r4.y * t.x, r4.x * vip.y - r4.y * t.y);
+        Q[i + n * pq.y] = make_float2(r4.y * vip.x + r4.x * t.x, r4.y * vip.y + r4.x * t.y);
+      }
+      __syncwarp();
+      // rows: A <- J^H A
+      for (int idx = lane; idx < half * n; idx += 32) {
+        const int k = idx / n, jj = idx % n;
+        const int2 pq = PI[k];
+        if (pq.y < 0) continue;
+        const float4 r4 = P4[k];
+        const float2 apj = A[pq.x + n * jj], aqj = A[pq.y + n * jj];
+        const float2 t = make_float2(r4.z * aqj.x - r4.w * aqj.y, r4.z * aqj.y + r4.w * aqj.x);
+        A[pq.x + n * jj] = make_float2(r4.x * apj.x - r4.y * t.x, r4.x * apj.y - r4.y * t.y);
+        A[pq.y + n * jj] = make_float2(r4.y * apj.x + r4.x * t.x, r4.y * apj.y + r4.x * t.y);
+      }
+      __syncwarp();
+      if (lane < half) {
+        const int2 pq = PI[lane];
+        if (pq.y >= 0) {
+          A[pq.x + n * pq.x].y = 0.f;   // the diagonal of a Hermitian matrix is real
+          A[pq.y + n * pq.y].y = 0.f;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// C = op(X) Y for n x n complex FP64 matrices in shared memory (column-major),
+// op(X) = X^H if XH; one warp.
+template <bool XH>
+__device__ void wmatmul(int n, const double2 *X, const double2 *Y, double2 *C, int lane) {
+  for (int idx = lane; idx < n * n; idx += 32) {
+    const int i = idx % n, jj = idx / n;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = 0; k < n; ++k) {
+      if (XH) cfma_cj(acc, X[k + n * i], Y[k + n * jj]);
+      else cfma(acc, X[i + n * k], Y[k + n * jj]);
+    }
+    C[idx] = acc;
+  }
+  __syncwarp();
+}
 
 __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t stride,
                        double *__restrict__ w, double2 *__restrict__ V, int *err) {
@@ -165,9 +290,10 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const int mat = blockIdx.x * wpb + wib;
   const int nn = n * n;
-  double2 *sA = sm + (size_t)wib * (2 * nn + 3 * 16);
-  double2 *sV = sA + nn;
-  double2 *sP = sV + nn;   // per pair: (c, s), (ph.x, ph.y), (p, q) packed
+  double2 *sA = sm + (size_t)wib * (4 * nn + 3 * 16);
+  double2 *sV = sA + nn, *sT = sV + nn, *sT2 = sT + nn;
+  double2 *sP = sT2 + nn;   // per pair: (c, s), (ph.x, ph.y), (p, q) packed
+  float2 *fA = (float2 *)sT, *fQ = fA + nn;   // the FP32 phase, inside sT
   if (mat >= batch) return;
   const double2 *Am = A + (size_t)mat * stride;
   for (int idx = lane; idx < nn; idx += 32) {
@@ -183,9 +309,51 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
       v = make_double2(Am[i + n * i].x, 0.0);
     }
     sA[idx] = v;
-    sV[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    fA[idx] = make_float2((float)v.x, (float)v.y);
+    fQ[idx] = make_float2(i == j ? 1.f : 0.f, 0.f);
   }
   __syncwarp();
+  // 1. FP32 sweeps
+  jacobi_f32(n, fA, fQ, (float4 *)sP, (int2 *)((float4 *)sP + 16), lane);
+  bool finite = true;
+  for (int idx = lane; idx < nn; idx += 32) {
+    const float2 q = fQ[idx];
+    finite = finite && isfinite(q.x) && isfinite(q.y);
+    sV[idx] = make_double2((double)q.x, (double)q.y);
+  }
+  __syncwarp();
+  if (!__all_sync(0xffffffffu, finite)) {   // FP32 overflowed: the FP64 sweeps start from A itself
+    for (int idx = lane; idx < nn; idx += 32) sV[idx] = make_double2(idx % n == idx / n ? 1.0 : 0.0, 0.0);
+    __syncwarp();
+  }
+  // 2. Q unitary to FP64 rounding: X <- X (3I - X^H X) / 2, twice
+  for (int it = 0; it < 2; ++it) {
+    wmatmul<true>(n, sV, sV, sT, lane);
+    for (int idx = lane; idx < nn; idx += 32) {
+      const double2 t = sT[idx];
+      sT[idx] = make_double2((idx % n == idx / n ? 3.0 : 0.0) - t.x, -t.y);
+    }
+    __syncwarp();
+    wmatmul<false>(n, sV, sT, sT2, lane);
+    for (int idx = lane; idx < nn; idx += 32) sV[idx] = cscale(sT2[idx], 0.5);
+    __syncwarp();
+  }
+  // 3. B = Q^H A Q, made exactly Hermitian (its rounding is below the FP64 sweeps' floor)
+  wmatmul<false>(n, sA, sV, sT, lane);
+  wmatmul<true>(n, sV, sT, sA, lane);
+  for (int idx = lane; idx < nn; idx += 32) {
+    const int i = idx % n, j = idx / n;
+    if (i < j) {
+      const double2 bij = sA[i + n * j], bji = sA[j + n * i];
+      const double2 v = make_double2(0.5 * (bij.x + bji.x), 0.5 * (bij.y - bji.y));
+      sA[i + n * j] = v;
+      sA[j + n * i] = cconj(v);
+    } else if (i == j) {
+      sA[idx].y = 0.0;
+    }
+  }
+  __syncwarp();
+  // 4. FP64 sweeps on B, accumulating into V = Q
   const int m = n + (n & 1);         // even number of players (dummy = n)
   const int half = m / 2;
   bool converged = false;
@@ -215,13 +383,8 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
     prev_off = off;
     for (int r = 0; r < m - 1; ++r) {
       if (lane < half) {
-        int a, b;
-        if (lane == 0) { a = 0; b = (r % (m - 1)) + 1; }
-        else {
-          a = ((r + lane) % (m - 1)) + 1;
-          b = ((r - lane + (m - 1)) % (m - 1)) + 1;
-        }
-        int p = min(a, b), q = max(a, b);
+        int p, q;
+        rr_pair(r, m, lane, p, q);
         double c = 1.0, s = 0.0, phx = 1.0, phy = 0.0;
         if (q < n) {
           // The rotation angle is computed in FP32 on operands scaled by the
@@ -324,8 +487,8 @@ __global__ void k_heig(int batch, int n, const double2 *__restrict__ A, int64_t 
 void launch_heig(int batch, int n, const double2 *A, int64_t stride, double *w, double2 *V,
                  int *err, cudaStream_t st) {
   if (batch <= 0) return;
-  int wpb = n <= 16 ? 4 : 2;
-  size_t smem = (size_t)wpb * (2 * n * n + 3 * 16) * sizeof(double2);
+  int wpb = n <= 8 ? 4 : n <= 16 ? 2 : 1;
+  size_t smem = (size_t)wpb * (4 * n * n + 3 * 16) * sizeof(double2);   // 67 KB at most (n = 32)
   // once per process: changing a kernel attribute can wait for the device's queued work
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
