@@ -120,8 +120,11 @@ int ephg::api_check_err(ephg_handle *h) {
 #define WSFAIL(rc) fail((rc), "%s", h->ws.msg.c_str())
 
 template <typename T>
-static int upload(T **dst, const T *src, size_t n, cudaStream_t st) {
-  CK(cudaMalloc((void **)dst, std::max<size_t>(n, 1) * sizeof(T)));
+// n elements from the library pool on st, copied from src; the bytes are added to *acc
+static int upload(T **dst, const T *src, size_t n, cudaStream_t st, int64_t *acc = nullptr) {
+  const size_t b = std::max<size_t>(n, 1) * sizeof(T);
+  CK(pool_alloc((void **)dst, b, st));
+  if (acc) *acc += (int64_t)b;
   if (n) CK(cudaMemcpyAsync(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
   return EPHG_OK;
 }
@@ -145,10 +148,13 @@ int ephg_destroy(ephg_handle *h) {
                   h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_rden,
                   h->rcartq, h->D, h->err, h->kposk, h->kposq, h->polar_G, h->polar_Gcell,
                   h->polar_born, h->polar_tau, h->polar_Da};
+  // stream-ordered frees back to the library pool, which keeps the memory
+  // mapped for the next handle
   for (void *p : ptrs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, h->st);
   h->ws.release();
-  tc::free_split(h->split);
+  tc::free_split(h->split, h->st);
+  cudaStreamSynchronize(h->st);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return EPHG_OK;
@@ -177,8 +183,6 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
     ephg_destroy(h);
     return r;
   };
-  size_t free0 = 0, total0 = 0;
-  cudaMemGetInfo(&free0, &total0);
   if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaGetDevice"));
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(EPHG_ERR_CUDA, "cudaStreamCreate"));
@@ -205,10 +209,10 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
   std::vector<int> rk = rows(d->rcells_k, nwsk), rq = rows(d->rcells_q, nwsq), rg = rows(d->rcells_g, nwsq);
   std::vector<double> dk(d->elwsdeg, d->elwsdeg + nwsk), dq(d->phwsdeg, d->phwsdeg + nwsq),
       dg(d->gwsdeg, d->gwsdeg + nwsq);
-  if ((rc = upload(&h->Rk, rk.data(), rk.size(), h->st)) || (rc = upload(&h->Rq, rq.data(), rq.size(), h->st)) ||
-      (rc = upload(&h->Rg, rg.data(), rg.size(), h->st)) || (rc = upload(&h->degk, dk.data(), dk.size(), h->st)) ||
-      (rc = upload(&h->degq, dq.data(), dq.size(), h->st)) || (rc = upload(&h->degg, dg.data(), dg.size(), h->st)) ||
-      (rc = upload(&h->masses, d->masses, (size_t)h->nat, h->st)))
+  if ((rc = upload(&h->Rk, rk.data(), rk.size(), h->st, &h->resident_bytes)) || (rc = upload(&h->Rq, rq.data(), rq.size(), h->st, &h->resident_bytes)) ||
+      (rc = upload(&h->Rg, rg.data(), rg.size(), h->st, &h->resident_bytes)) || (rc = upload(&h->degk, dk.data(), dk.size(), h->st, &h->resident_bytes)) ||
+      (rc = upload(&h->degq, dq.data(), dq.size(), h->st, &h->resident_bytes)) || (rc = upload(&h->degg, dg.data(), dg.size(), h->st, &h->resident_bytes)) ||
+      (rc = upload(&h->masses, d->masses, (size_t)h->nat, h->st, &h->resident_bytes)))
     return bail(rc);
   // H(Re) with the velocity companions i*rcart*H (wannier.f90:466-478)
   {
@@ -227,14 +231,15 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
           hx[(size_t)r * 4 * nn + (1 + p) * nn + e] = make_double2(-rc3[p] * v.y, rc3[p] * v.x);
       }
     }
-    if ((rc = upload(&h->Hext, hx.data(), hx.size(), h->st))) return bail(rc);
+    if ((rc = upload(&h->Hext, hx.data(), hx.size(), h->st, &h->resident_bytes))) return bail(rc);
   }
   // g(Re,Rp): raw epmatwp order and the stage-A layout
   {
     size_t n = (size_t)nw * nw * nwsk * nb * nwsq;
-    if ((rc = upload(&h->graw, (const double2 *)d->gwann, n, h->st))) return bail(rc);
-    if (cudaMalloc(&h->G64, n * sizeof(double2)) != cudaSuccess)
-      return bail(fail(EPHG_ERR_NOMEM, "cudaMalloc g(Re,Rp) %zu bytes", n * 16));
+    if ((rc = upload(&h->graw, (const double2 *)d->gwann, n, h->st, &h->resident_bytes))) return bail(rc);
+    if (pool_alloc((void **)&h->G64, n * sizeof(double2), h->st) != cudaSuccess)
+      return bail(fail(EPHG_ERR_NOMEM, "device allocation of g(Re,Rp), %zu bytes", n * 16));
+    h->resident_bytes += (int64_t)(n * sizeof(double2));
     launch_permute_gwann(nw, nb, nwsk, nwsq, h->graw, h->G64, h->st);
   }
   // phonon terms: for each atom pair and WS cell, the shortest wraps
@@ -276,13 +281,13 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
       for (int i = 0; i < 3; ++i)
         rcq[r + (size_t)nwsq * i] = h->lattvecs[i] * rq[3 * r] + h->lattvecs[i + 3] * rq[3 * r + 1] +
                                     h->lattvecs[i + 6] * rq[3 * r + 2];
-    if ((rc = upload(&h->pair_off, pair_off.data(), pair_off.size(), h->st)) ||
-        (rc = upload(&h->ent_iuc, ent_iuc.data(), ent_iuc.size(), h->st)) ||
-        (rc = upload(&h->ent_woff, ent_woff.data(), ent_woff.size(), h->st)) ||
-        (rc = upload(&h->wrapR, wrapR.data(), wrapR.size(), h->st)) ||
-        (rc = upload(&h->ent_rden, ent_rden.data(), ent_rden.size(), h->st)) ||
-        (rc = upload(&h->rcartq, rcq.data(), rcq.size(), h->st)) ||
-        (rc = upload(&h->D, (const double2 *)d->Dphwann, (size_t)nwsq * nb * nb, h->st)))
+    if ((rc = upload(&h->pair_off, pair_off.data(), pair_off.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->ent_iuc, ent_iuc.data(), ent_iuc.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->ent_woff, ent_woff.data(), ent_woff.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->wrapR, wrapR.data(), wrapR.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->ent_rden, ent_rden.data(), ent_rden.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->rcartq, rcq.data(), rcq.size(), h->st, &h->resident_bytes)) ||
+        (rc = upload(&h->D, (const double2 *)d->Dphwann, (size_t)nwsq * nb * nb, h->st, &h->resident_bytes)))
       return bail(rc);
     h->terms.npair = h->nat * h->nat;
     h->terms.pair_off = h->pair_off;
@@ -315,18 +320,14 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
       return pos;
     };
     std::vector<int> pk = order(rk, nwsk), pq = order(rq, nwsq);
-    if ((rc = upload(&h->kposk, pk.data(), pk.size(), h->st)) || (rc = upload(&h->kposq, pq.data(), pq.size(), h->st)))
+    if ((rc = upload(&h->kposk, pk.data(), pk.size(), h->st, &h->resident_bytes)) || (rc = upload(&h->kposq, pq.data(), pq.size(), h->st, &h->resident_bytes)))
       return bail(rc);
   }
-  if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "cudaMalloc err"));
+  if (pool_alloc((void **)&h->err, sizeof(int), h->st) != cudaSuccess)
+    return bail(fail(EPHG_ERR_CUDA, "device allocation of the error word"));
   if (cudaMemsetAsync(h->err, 0, sizeof(int), h->st) != cudaSuccess) return bail(fail(EPHG_ERR_CUDA, "memset"));
   if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return bail(fail(EPHG_ERR_CUDA, "create: %s", cudaGetErrorString(cudaGetLastError())));
-  {
-    size_t free1 = 0, total1 = 0;
-    cudaMemGetInfo(&free1, &total1);
-    h->resident_bytes = free0 > free1 ? (int64_t)(free0 - free1) : 0;   // the uploads, at allocation granularity
-  }
   *out = h;
   return EPHG_OK;
 }
@@ -340,10 +341,10 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
 int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born) {
   if (!h) return fail(EPHG_ERR_ARG, "set_polar: bad arguments");
   if (epsilon && !born) return fail(EPHG_ERR_ARG, "set_polar: born effective charges are required");
-  CK(cudaStreamSynchronize(h->st));
   for (void *p : {(void *)h->polar_G, (void *)h->polar_Gcell, (void *)h->polar_born, (void *)h->polar_tau,
                   (void *)h->polar_Da})
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, h->st);
+  CK(cudaStreamSynchronize(h->st));
   h->polar_G = h->polar_Gcell = h->polar_born = h->polar_tau = nullptr;
   h->polar_Da = nullptr;
   h->polar_on = false;
@@ -410,7 +411,7 @@ int ephg_set_polar(ephg_handle *h, const double *epsilon, const double *born) {
       (rc = upload(&h->polar_born, born, 9 * (size_t)nat, h->st)) ||
       (rc = upload(&h->polar_tau, tau.data(), tau.size(), h->st)))
     return rc;
-  CK(cudaMalloc(&h->polar_Da, (size_t)nb * nb * sizeof(double2)));
+  CK(pool_alloc((void **)&h->polar_Da, (size_t)nb * nb * sizeof(double2), h->st));
   P.G = h->polar_G;
   P.Gcell = h->polar_Gcell;
   P.born = h->polar_born;

@@ -2455,9 +2455,9 @@ static int stageA_fused86(const float *PA, int MpA, const float *GA6, int64_t NA
 }
 
 // ------------------------------------------------------------ orchestration
-void free_split(SplitOperands &s) {
-  if (s.G) cudaFree(s.G);
-  if (s.GA6) cudaFree(s.GA6);
+void free_split(SplitOperands &s, cudaStream_t st) {
+  if (s.G) cudaFreeAsync(s.G, st);
+  if (s.GA6) cudaFreeAsync(s.GA6, st);
   s.G = nullptr;
   s.GA6 = nullptr;
   s.bytes = 0;
@@ -2504,7 +2504,7 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   {
   std::lock_guard<std::mutex> build_lock(*build_mu);
   if (!s.G) {
-    TCK(cudaMalloc(&s.G, (size_t)4 * NpA * KpA * sizeof(float)));
+    TCK(pool_alloc((void **)&s.G, (size_t)4 * NpA * KpA * sizeof(float), st));
     s.bytes += (int64_t)4 * NpA * KpA * sizeof(float);
     TCK(cudaMemsetAsync(s.G, 0, (size_t)4 * NpA * KpA * sizeof(float), st));
     dim3 grid((unsigned)((Nn + 31) / 32), (unsigned)((KpA + 31) / 32));
@@ -2726,11 +2726,11 @@ static int split_rates_fused86(SplitOperands &s, Workspace &ws, cudaStream_t st,
   std::lock_guard<std::mutex> build_lock(*build_mu);
   if (!s.GA6 || s.NA != NA || s.KpA6 != KpA) {
     if (s.GA6) {
-      cudaFree(s.GA6);
+      cudaFreeAsync(s.GA6, st);
       s.bytes -= (int64_t)6 * s.NA * s.KpA6 * sizeof(float);
     }
     s.GA6 = nullptr;
-    TCK(cudaMalloc(&s.GA6, (size_t)6 * NA * KpA * sizeof(float)));
+    TCK(pool_alloc((void **)&s.GA6, (size_t)6 * NA * KpA * sizeof(float), st));
     s.bytes += (int64_t)6 * NA * KpA * sizeof(float);
     TCK(cudaMemsetAsync(s.GA6, 0, (size_t)6 * NA * KpA * sizeof(float), st));
     const int64_t ne = NA * nwsk;

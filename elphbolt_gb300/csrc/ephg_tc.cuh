@@ -21,7 +21,8 @@ struct SplitOperands {
   std::atomic<int64_t> bytes{0};   // device bytes held by G and GA6 (read by the serving loop's budget)
 };
 
-void free_split(SplitOperands &s);
+// stream-ordered on st (the handle's stream, synchronised by the caller)
+void free_split(SplitOperands &s, cudaStream_t st);
 const char *last_error();
 
 // Grouped launches of the split form's GEMMs across rate requests that run

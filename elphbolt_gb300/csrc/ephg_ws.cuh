@@ -6,17 +6,57 @@
 
 #include <cstdio>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
 
 namespace ephg {
 
+// The library's device memory: one stream-ordered pool per device that keeps
+// freed memory (up to half the device) mapped for the next allocation instead
+// of returning it at every synchronisation, so that a handle created after
+// another one was destroyed, or a request's workspace after the last one's,
+// reuses mapped memory: cudaFree / first-touch mapping of gigabytes costs
+// milliseconds per call.  Memory above the threshold is returned as usual.
+inline cudaMemPool_t lib_pool(int device) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(device);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return nullptr;
+  } else {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    uint64_t keep = (uint64_t)tot / 2;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  pools[device] = pool;
+  return pool;
+}
+
+// bytes from the current device's library pool, ordered on st
+inline cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t st) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemPool_t pool = lib_pool(dev);
+  if (!pool) return cudaMallocAsync(p, bytes, st);
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
 // Named device buffers that grow on demand and are reused across calls, so a
 // repeated request pays no cudaMalloc.  get() returns 0 or EPHG_ERR_NOMEM (6)
 // and leaves the reason in msg: cudaMalloc failed, or growing the cache would
 // take its total past `limit` (the serving loop's share of the HBM budget).
-// Buffers are allocated and freed stream-ordered on `st` (cudaMallocAsync /
+// Buffers are allocated and freed stream-ordered on `st` (the library pool,
 // cudaFreeAsync): unlike cudaMalloc / cudaFree these do not wait for the other
 // streams of the device, so a request that grows its workspace does not stall
 // behind the kernels of other requests running concurrently.
@@ -67,7 +107,7 @@ struct Workspace {
     }
     void *p = nullptr;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMallocAsync(&p, bytes, st);
+    cudaError_t e = pool_alloc(&p, bytes, st);
     if (e != cudaSuccess) {
       cudaGetLastError();
       if (grow) grow(grow_ctx, -(int64_t)bytes);   // the old buffer is gone too: give back all
