@@ -497,7 +497,7 @@ def run_ours(args, ws, rank, local):
     value = args.steps * vertices / (total_ms * 1e-3)
     split_rates = out["rates"]
     # ---- e2e: one-shot drop-in through the C ABI from pinned host buffers, same step count ----
-    e2e = e2e_measure(wd, req, prec, args.steps)
+    e2e = e2e_measure(wd, req, prec, args.steps, args.warmup)
     # ---- FP64 plain drop-in on the same request (one step) ----
     f = W.el_rates(req, precision=_lib.PREC_FP64)
     fst = f["stats"]
@@ -590,8 +590,9 @@ def run_ours(args, ws, rank, local):
     return 0
 
 
-def e2e_measure(wd, req, prec, steps):
-    """create -> el_rates -> destroy through the C ABI, inputs in pinned host memory."""
+def e2e_measure(wd, req, prec, steps, warmup=0):
+    """create -> el_rates -> destroy through the C ABI, inputs in pinned host memory;
+    `warmup` untimed steps first, as for the resident measurement."""
     import ctypes as ct
     import numpy as np
     import torch
@@ -631,19 +632,24 @@ def e2e_measure(wd, req, prec, steps):
     stats = _lib.RateStats()
     h2d = sum(t.numel() * t.element_size() for t in arrs.values())
     d2h = rates.numel() * 8 + idx.numel() * 8
-    vert = 0
-    torch.cuda.synchronize()
-    t0 = time.time()
-    for _ in range(steps):
+    def step():
         h = ct.c_void_p()
         _lib.check(L.ephg_create(ct.byref(d), ct.byref(h)))
         _lib.check(L.ephg_el_rates(h, ct.byref(r), dp(rates), ip(idx), ct.byref(stats), None, None, None, 0))
         _lib.check(L.ephg_destroy(h))
-        vert += stats.vertices
+        return stats.vertices
+
+    for _ in range(warmup):
+        step()
+    vert = 0
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(steps):
+        vert += step()
     torch.cuda.synchronize()
     t = time.time() - t0
     return {"value": vert / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "steps": steps, "ms_per_step": 1e3 * t / steps,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t / steps,
             "flow": "ephg_create (upload from pinned host) + ephg_el_rates (host rates out) + ephg_destroy"}
 
 
