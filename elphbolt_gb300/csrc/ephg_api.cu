@@ -144,7 +144,7 @@ int ephg_device_count(void) {
 
 int ephg_destroy(ephg_handle *h) {
   if (!h) return EPHG_OK;
-  void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->graw, h->G64,
+  void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->Hbox, h->Dbox, h->graw, h->G64,
                   h->masses, h->pair_off, h->ent_iuc, h->ent_woff, h->wrapR, h->ent_rden,
                   h->rcartq, h->D, h->err, h->kposk, h->kposq, h->polar_G, h->polar_Gcell,
                   h->polar_born, h->polar_tau, h->polar_Da};
@@ -232,6 +232,28 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
       }
     }
     if ((rc = upload(&h->Hext, hx.data(), hx.size(), h->st, &h->resident_bytes))) return bail(rc);
+    // H(Re) / deg(Re) on the box of Re coordinates, for the mesh Fourier sums
+    int hi[3];
+    for (int c = 0; c < 3; ++c) {
+      h->hlo[c] = hi[c] = nwsk > 0 ? rk[c] : 0;
+      for (int r = 0; r < nwsk; ++r) {
+        h->hlo[c] = std::min(h->hlo[c], rk[3 * r + c]);
+        hi[c] = std::max(hi[c], rk[3 * r + c]);
+      }
+      h->hext[c] = hi[c] - h->hlo[c] + 1;
+    }
+    const size_t nbox = (size_t)h->hext[0] * h->hext[1] * h->hext[2];
+    if (nbox > ((size_t)1 << 22)) return bail(fail(EPHG_ERR_ARG, "Re cells span too large a box"));
+    std::vector<double2> hb(nbox * nn, make_double2(0.0, 0.0));
+    for (int r = 0; r < nwsk; ++r) {
+      const size_t cell = ((size_t)(rk[3 * r] - h->hlo[0]) * h->hext[1] + (rk[3 * r + 1] - h->hlo[1])) * h->hext[2] +
+                          (rk[3 * r + 2] - h->hlo[2]);
+      for (size_t e = 0; e < nn; ++e) {
+        const double2 v = hx[(size_t)r * 4 * nn + e];
+        hb[cell * nn + e] = make_double2(v.x / dk[r], v.y / dk[r]);
+      }
+    }
+    if ((rc = upload(&h->Hbox, hb.data(), hb.size(), h->st, &h->resident_bytes))) return bail(rc);
   }
   // g(Re,Rp): raw epmatwp order and the stage-A layout
   {
@@ -289,6 +311,45 @@ int ephg_create(const ephg_wannier_desc *d, ephg_handle **out) {
         (rc = upload(&h->rcartq, rcq.data(), rcq.size(), h->st, &h->resident_bytes)) ||
         (rc = upload(&h->D, (const double2 *)d->Dphwann, (size_t)nwsq * nb * nb, h->st, &h->resident_bytes)))
       return bail(rc);
+    // D(q) on a mesh as one Fourier sum per element over the wrapped vectors R':
+    // X_ab(R') = massnorm_ab sum of rden D(iuc)_ab over the (pair(a, b), iuc)
+    // entries whose wraps include R' (k_dbuild's sum, regrouped)
+    {
+      const int ne = nb * nb;
+      int lo3[3] = {0, 0, 0}, hi3[3] = {0, 0, 0};
+      const int nwr = (int)(wrapR.size() / 3);
+      for (int c = 0; c < 3; ++c) {
+        lo3[c] = hi3[c] = nwr > 0 ? wrapR[c] : 0;
+        for (int i = 0; i < nwr; ++i) {
+          lo3[c] = std::min(lo3[c], wrapR[3 * i + c]);
+          hi3[c] = std::max(hi3[c], wrapR[3 * i + c]);
+        }
+        h->dlo[c] = lo3[c];
+        h->dext[c] = hi3[c] - lo3[c] + 1;
+      }
+      const size_t nbox = (size_t)h->dext[0] * h->dext[1] * h->dext[2];
+      if (nbox > ((size_t)1 << 22)) return bail(fail(EPHG_ERR_ARG, "phonon cells span too large a box"));
+      std::vector<double2> xb(nbox * ne, make_double2(0.0, 0.0));
+      const double2 *Dw = (const double2 *)d->Dphwann;
+      for (int e = 0; e < ne; ++e) {
+        const int a = e % nb, b = e / nb;
+        const int pair = (a / 3) + h->nat * (b / 3);
+        const double massnorm = 1.0 / std::sqrt(d->masses[a / 3] * d->masses[b / 3]) * Ryd2amu;
+        for (int iuc = 0; iuc < nwsq; ++iuc) {
+          const int en = pair * nwsq + iuc;   // entries (pair, cell) in cell order
+          const double2 dv = Dw[iuc + (size_t)nwsq * (a + (size_t)nb * b)];
+          const double f = ent_rden[en] * massnorm;
+          for (int wv = ent_woff[en]; wv < ent_woff[en + 1]; ++wv) {
+            const size_t cell =
+                ((size_t)(wrapR[3 * wv] - lo3[0]) * h->dext[1] + (wrapR[3 * wv + 1] - lo3[1])) * h->dext[2] +
+                (wrapR[3 * wv + 2] - lo3[2]);
+            xb[cell * ne + e].x += f * dv.x;
+            xb[cell * ne + e].y += f * dv.y;
+          }
+        }
+      }
+      if ((rc = upload(&h->Dbox, xb.data(), xb.size(), h->st, &h->resident_bytes))) return bail(rc);
+    }
     h->terms.npair = h->nat * h->nat;
     h->terms.pair_off = h->pair_off;
     h->terms.ent_iuc = h->ent_iuc;
@@ -871,11 +932,10 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   (*x.tb).reset();
   CK(cudaEventRecord(ev.e[0], st));
   // ---- set-up: electrons on the full mesh (el_wann, electron.f90:364) ----
-  double2 *roots, *P, *Hk, *V, *Dq, *Vq, *u;
+  double2 *roots, *Hk, *V, *Dq, *Vq, *u;
   double *w, *ens, *wq, *om, *bose, *rates_d;
   int *flag, *widx, *nwv_d, *sflag, *iota, *st_code, *nst_d, *nin_k, *cum;
-  if ((rc = wsget((*x.ws), "r_roots", (size_t)L, &roots)) || (rc = wsget((*x.ws), "r_P", (size_t)N * nwsk, &P)) ||
-      (rc = wsget((*x.ws), "r_Hk", (size_t)N * nn, &Hk)) || (rc = wsget((*x.ws), "r_w", (size_t)N * nw, &w)) ||
+  if ((rc = wsget((*x.ws), "r_roots", (size_t)L, &roots)) || (rc = wsget((*x.ws), "r_Hk", (size_t)N * nn, &Hk)) || (rc = wsget((*x.ws), "r_w", (size_t)N * nw, &w)) ||
       (rc = wsget((*x.ws), "r_V", (size_t)N * nn, &V)) || (rc = wsget((*x.ws), "r_ens", (size_t)N * nw, &ens)) ||
       (rc = wsget((*x.ws), "r_flag", (size_t)N, &flag)) || (rc = wsget((*x.ws), "r_widx", (size_t)N, &widx)) ||
       (rc = wsget((*x.ws), "r_nwv", 4, &nwv_d)) || (rc = wsget((*x.ws), "r_iota", (size_t)N * nw, &iota)) ||
@@ -885,8 +945,13 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
       (rc = wsget((*x.ws), "r_rates", (size_t)N * nw, &rates_d)))
     return WSFAILX(rc);
   launch_roots(L, roots, st);
-  launch_phase_mesh(N, nullptr, mesh, L, nwsk, h->Rk, h->degk, 0, roots, P, nwsk, st);
-  launch_zgemm(N, (int)nn, nwsk, P, nwsk, h->Hext, 4 * (int64_t)nn, Hk, nn, st);
+  {   // H(k) on the whole mesh: the Re sum one dimension at a time
+    double2 *t1, *t2;
+    if ((rc = wsget((*x.ws), "r_ht1", (size_t)h->hext[0] * h->hext[1] * mesh[2] * nn, &t1)) ||
+        (rc = wsget((*x.ws), "r_ht2", (size_t)h->hext[0] * mesh[1] * mesh[2] * nn, &t2)))
+      return WSFAILX(rc);
+    launch_mesh_fourier(h->Hbox, h->hlo, h->hext, (int)nn, mesh, L, roots, t1, t2, Hk, st);
+  }
   launch_heig(N, nw, Hk, nn, w, V, x.err, st);
   launch_el_post(N, nw, w, V, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, ens, st);
   // ---- crystal symmetry: every mesh point takes the energies of its orbit's
@@ -936,7 +1001,14 @@ int ephg::el_rates_view(ephg_handle *h, const ExecView &x, const ephg_rate_reque
   if ((rc = check_err_view(x))) return rc;
   if (nwv == 0) return fail(EPHG_ERR_EMPTY_WINDOW, "No states found within Fermi window.");
   // ---- phonons on the q mesh (phonon.f90:208-214) ----
-  launch_dbuild(N, iota, mesh, L, roots, nullptr, h->terms, 0, Dq, nullptr, st);
+  {   // D(q) on the whole mesh: the sum over wrapped cells one dimension at a time
+    double2 *t1, *t2;
+    const size_t ne = (size_t)nb * nb;
+    if ((rc = wsget((*x.ws), "r_dt1", (size_t)h->dext[0] * h->dext[1] * mesh[2] * ne, &t1)) ||
+        (rc = wsget((*x.ws), "r_dt2", (size_t)h->dext[0] * mesh[1] * mesh[2] * ne, &t2)))
+      return WSFAILX(rc);
+    launch_mesh_fourier(h->Dbox, h->dlo, h->dext, (int)ne, mesh, L, roots, t1, t2, Dq, st);
+  }
   double2 *Lq = nullptr, *glp = nullptr;
   float2 *glpf = nullptr;
   if (h->polar_on) {   // dyn_nonanalytic into D(q) and the long-range vector of every mesh q

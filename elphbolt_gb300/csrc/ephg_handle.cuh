@@ -23,6 +23,10 @@ struct ephg_handle {
   int *Rk = nullptr, *Rq = nullptr, *Rg = nullptr;         // (n,3) int
   double *degk = nullptr, *degq = nullptr, *degg = nullptr;
   double2 *Hext = nullptr;   // [Re][4*nw*nw]: H, i rx H, i ry H, i rz H
+  double2 *Hbox = nullptr;   // H(Re) / deg(Re) on the box of Re coordinates [hlo, hlo + hext) (mesh Fourier sums)
+  int hlo[3] = {0, 0, 0}, hext[3] = {1, 1, 1};
+  double2 *Dbox = nullptr;   // mass-normalised D terms on the box of wrapped cell vectors [dlo, dlo + dext)
+  int dlo[3] = {0, 0, 0}, dext[3] = {1, 1, 1};
   double2 *graw = nullptr;   // epmatwp order (i,j,Re,s,Rp)
   double2 *G64 = nullptr;    // stage-A matrix [Re][Nn]
   double *masses = nullptr;

@@ -63,6 +63,48 @@ void launch_phase_mesh(int nrows, const int *rowp, const int mesh[3], int L, int
                                                              roots, out, ldo);
 }
 
+// ---- a Fourier sum over integer cells onto a whole mesh, one dimension at a time ----
+// On a mesh, sum_R e^{2 pi i k.R} X(R) separates: with X placed on the box of
+// cell coordinates [lo, lo + ext) per dimension (zero where there is no cell),
+// three 1-D sums of ext terms each replace the N_k x N_R phase matrix and its
+// GEMM (for H(k), wannier.f90:467-479: ~40x fewer FP64 flops at 24^3, 6^3 WS).
+// Every factor e^{2 pi i v (r + lo) / m} is the exact integer-indexed root of
+// unity.  One pass: out[a][v][b][e] = sum_r root(v (r + lo) L / m) in[a][r][b][e],
+// or with TRANS out[a][b][v][e]: the second and third passes write [r1][v3][v2]
+// and then [v3][v2][v1], the muxed mesh index v1 + m1 (v2 + m2 v3) in row order.
+template <bool TRANS>
+__global__ void k_dft1(int64_t total, int R, int B, int M, int nn, int lo, int Lm, int L,
+                       const double2 *__restrict__ roots, const double2 *__restrict__ in,
+                       double2 *__restrict__ out) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int e = (int)(idx % nn);
+  int64_t t = idx / nn;
+  const int b = (int)(t % B);
+  t /= B;
+  const int v = (int)(t % M);
+  const int64_t a = t / M;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int r = 0; r < R; ++r)
+    cfma(acc, roots[floormod((int64_t)v * (r + lo) * Lm, L)], in[((a * R + r) * B + b) * nn + e]);
+  out[TRANS ? ((a * B + b) * M + v) * nn + e : idx] = acc;
+}
+
+void launch_mesh_fourier(const double2 *box, const int lo[3], const int ext[3], int nn, const int mesh[3], int L,
+                         const double2 *roots, double2 *t1, double2 *t2, double2 *out, cudaStream_t st) {
+  const int64_t n1 = (int64_t)ext[0] * ext[1] * mesh[2] * nn, n2 = (int64_t)ext[0] * mesh[1] * mesh[2] * nn,
+                n3 = (int64_t)mesh[0] * mesh[1] * mesh[2] * nn;
+  // along R3: [r1 r2][r3][e] -> [r1 r2][v3][e]
+  k_dft1<false><<<(unsigned)((n1 + 255) / 256), 256, 0, st>>>(n1, ext[2], 1, mesh[2], nn, lo[2], L / mesh[2], L,
+                                                              roots, box, t1);
+  // along R2: [r1][r2][v3][e] -> [r1][v3][v2][e]
+  k_dft1<true><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(n2, ext[1], mesh[2], mesh[1], nn, lo[1], L / mesh[1],
+                                                             L, roots, t1, t2);
+  // along R1: [r1][v3 v2][e] -> [v3 v2][v1][e], rows in muxed mesh order
+  k_dft1<true><<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(n3, ext[0], mesh[1] * mesh[2], mesh[0], nn, lo[0],
+                                                             L / mesh[0], L, roots, t2, out);
+}
+
 // expi(twopi * dot_product(k, R)) / deg, misc.f90:588 with wannier.f90:467,1097
 __global__ void k_phase_frac(int nrows, const double *kv, int nR, const int *R,
                              const double *deg, double2 *out, int64_t ldo) {

@@ -15,6 +15,13 @@ void launch_phase_mesh(int nrows, const int *rowp, const int mesh[3], int L, int
 void launch_phase_frac(int nrows, const double *kv, int nR, const int *R, const double *deg,
                        double2 *out, int64_t ldo, cudaStream_t st);
 
+// out[p][e] = sum_R e^{2 pi i k_p.R} X(R)[e] for every point p of the mesh (muxed
+// order), X given on the box of cell coordinates [lo, lo + ext) per dimension
+// (box[((r1 ext2 + r2) ext3 + r3) nn + e], zero where there is no cell); three
+// 1-D passes through t1 (ext1 ext2 m3 nn) and t2 (ext1 m2 m3 nn).
+void launch_mesh_fourier(const double2 *box, const int lo[3], const int ext[3], int nn, const int mesh[3], int L,
+                         const double2 *roots, double2 *t1, double2 *t2, double2 *out, cudaStream_t st);
+
 // ---- FP64 complex GEMM: C[M][N] = A[M][K] * B[K][N], row-major ----
 void launch_zgemm(int M, int N, int K, const double2 *A, int64_t lda, const double2 *B,
                   int64_t ldb, double2 *C, int64_t ldc, cudaStream_t st);

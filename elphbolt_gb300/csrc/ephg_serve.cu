@@ -435,8 +435,8 @@ struct HandleExecutor : Executor {
   int64_t min_bytes(int c, const ephg_rate_request &r) const override {
     const ephg_handle *h = hs[c];
     const int64_t N = r.mesh[0] * r.mesh[1] * r.mesh[2];
-    // set-up arrays of el_rates on the whole mesh: phases, H(k) + eigenvectors, D(q) + eigenvectors + u
-    return N * ((int64_t)h->nwsk + 2 * (int64_t)h->nw * h->nw + 3 * (int64_t)h->nb * h->nb) * 16;
+    // set-up arrays of el_rates on the whole mesh: H(k) + eigenvectors, D(q) + eigenvectors + u
+    return N * (2 * (int64_t)h->nw * h->nw + 3 * (int64_t)h->nb * h->nb) * 16;
   }
   void set_grow(int s, bool (*fn)(void *, int64_t), void *ctx) override {
     slots[s]->ws.grow = fn;
