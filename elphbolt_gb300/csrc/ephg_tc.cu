@@ -238,6 +238,8 @@ struct GemmArgs {
   float *Cr, *Ci;            // [Mp][ldc] outputs
   int64_t ldc;
   int *err;
+  int ileave;                // 1: outputs interleaved by 32 rows in groups of 4 columns: (r, c) at
+                             //    (r / 32) ldc 32 + (c / 4) 128 + (r % 32) 4 + c % 4 (ldc a multiple of 4)
 };
 
 // One output tile as the three roles see it: operand maps, first A / B row of
@@ -248,6 +250,7 @@ struct TileJob {
   int Astride, Bstride;
   float *Cr, *Ci;
   int64_t ldc;
+  int ileave;
 };
 
 __host__ __device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, const CUtensorMap *tB, const GemmArgs &g,
@@ -261,10 +264,12 @@ __host__ __device__ __forceinline__ TileJob tile_job(const CUtensorMap *tA, cons
   j.nkb = g.nkb;
   j.Astride = (int)g.Astride;
   j.Bstride = (int)g.Bstride;
-  const int64_t off = (int64_t)mt * BM * g.ldc + (int64_t)nt * BN;
+  const int64_t off = g.ileave ? ((int64_t)mt * (BM / 32) * g.ldc + (int64_t)nt * BN) * 32
+                               : (int64_t)mt * BM * g.ldc + (int64_t)nt * BN;
   j.Cr = g.Cr + off;
   j.Ci = g.Ci + off;
   j.ldc = g.ldc;
+  j.ileave = g.ileave;
   return j;
 }
 
@@ -445,8 +450,10 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
       if (!mbar_wait(&tfull[0], it & 1, err)) break;
       tc_fence_after();
       const uint32_t tr = tmem + ((uint32_t)(quad * 32) << 16);
-      float *cr = j.Cr + (int64_t)row * j.ldc;
-      float *ci = j.Ci + (int64_t)row * j.ldc;
+      // row-major: the row's 16 columns as float4 stores; interleaved: each group of
+      // 4 columns of the warp's 32 rows is 512 consecutive bytes (one float4 per lane)
+      float *cr = j.ileave ? j.Cr + (int64_t)quad * j.ldc * 32 + 4 * lane : j.Cr + (int64_t)row * j.ldc;
+      float *ci = j.ileave ? j.Ci + (int64_t)quad * j.ldc * 32 + 4 * lane : j.Ci + (int64_t)row * j.ldc;
 #pragma unroll 1
       for (int c0 = cbeg; c0 < cbeg + CW; c0 += 16) {
         uint32_t ar[16], ai[16], br[16], bi[16];
@@ -461,11 +468,21 @@ __device__ __forceinline__ void cgemm_body(const Jobs &jobs, int t0, int t1, int
           vr[q] = __uint_as_float(ar[q]) + __uint_as_float(br[q]);
           vi[q] = __uint_as_float(ai[q]) + __uint_as_float(bi[q]);
         }
+        // streaming stores: the output is read once, later, by another kernel
+        if (j.ileave) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          // streaming stores: the output is read once, later, by another kernel
-          __stcs((float4 *)(cr + c0 + 4 * q), make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]));
-          __stcs((float4 *)(ci + c0 + 4 * q), make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]));
+          for (int q = 0; q < 4; ++q) {
+            __stcs((float4 *)(cr + (int64_t)(c0 + 4 * q) * 32),
+                   make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]));
+            __stcs((float4 *)(ci + (int64_t)(c0 + 4 * q) * 32),
+                   make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]));
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            __stcs((float4 *)(cr + c0 + 4 * q), make_float4(vr[4 * q], vr[4 * q + 1], vr[4 * q + 2], vr[4 * q + 3]));
+            __stcs((float4 *)(ci + c0 + 4 * q), make_float4(vi[4 * q], vi[4 * q + 1], vi[4 * q + 2], vi[4 * q + 3]));
+          }
         }
       }
       tc_fence_before();
@@ -668,7 +685,7 @@ void batcher_stats(const GemmBatcher *b, int64_t *launches, int64_t *problems, i
 // With a batch member the GEMM joins its batcher's next grouped launch.
 static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const float *Bp, int64_t Bstride,
                  int64_t Boff, int Np, int Kp, float *Cr, float *Ci, int64_t ldc, int *err, cudaStream_t st,
-                 int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr) {
+                 int chunk_us = 0, const Yield &yield = Yield(), const BatchMember *bm = nullptr, int ileave = 0) {
   if (Mp % BM || Np % BN || Kp % BK || Mp <= 0 || Np <= 0) return tfail(1, "cgemm: shapes not tile multiples");
   if (4 * Astride > INT32_MAX || 4 * Bstride > INT32_MAX) return tfail(1, "cgemm: operand too tall for TMA coords");
   if (bm && bm->gb) {
@@ -687,6 +704,7 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
     p.g.Ci = Ci;
     p.g.ldc = ldc;
     p.g.err = err;
+    p.g.ileave = ileave;
     return bm->gb->submit(bm->id, p, st);
   }
   CUtensorMap ta, tb;
@@ -709,6 +727,7 @@ static int cgemm(const float *Ap, int64_t Astride, int64_t Aoff, int Mp, const f
   g.Ci = Ci;
   g.ldc = ldc;
   g.err = err;
+  g.ileave = ileave;
   int tiles = g.mtiles * g.ntiles;
   int grid = std::min(tiles, num_sms());
   // chunk_us > 0: launches of about that length (a tile is ~0.4 us per 16 K positions) so
@@ -1379,10 +1398,10 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
 
 // Generic-shape split epilogue without shared-memory staging: one thread per
 // (k' row, state), EPI_ROWS consecutive rows of one state per block.  A thread
-// reads its row's nw x nb complex Rp sums as 16-byte loads straight from the
-// GEMM output (the two 16-byte halves of a sector meet in L1), so that shared
-// memory does not cap the resident warps.  NW bands fixed at compile time (the
-// band and mode arrays then live in registers), nb <= EPR_NB.
+// reads its row's nw x nb complex Rp sums straight from the GEMM output, which
+// the GEMM wrote interleaved by 32 rows in 4-column groups (GemmArgs::ileave):
+// each float4 load of a warp is 512 consecutive bytes.  NW bands fixed
+// at compile time (the band and mode arrays then live in registers), nb <= EPR_NB.
 constexpr int EPR_NB = 18;
 
 template <int NW>
@@ -1407,7 +1426,10 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
     const int b1 = pp % rp.mesh[0], b2 = (pp / rp.mesh[0]) % rp.mesh[1], b3 = pp / (rp.mesh[0] * rp.mesh[1]);
     const int q = (int)(floormod(b1 - a1, rp.mesh[0]) +
                         rp.mesh[0] * (floormod(b2 - a2, rp.mesh[1]) + rp.mesh[1] * floormod(b3 - a3, rp.mesh[2])));
-    const int64_t base = (int64_t)ip * ldc + (int64_t)(j - j0) * ncol;
+    // the GEMM output interleaved by 32 rows in groups of 4 columns: columns c..c+3
+    // (c % 4 = 0) of this row are the float4 at rr + 32 c, so that a warp's 32 rows
+    // read 512 consecutive bytes per group
+    const int64_t base = ((int64_t)(ip >> 5) * ldc + (int64_t)(j - j0) * ncol) * 32 + 4 * (ip & 31);
     const float *rr = Cr + base, *ri = Ci + base;
     const bool ph = d.phr || d.yv;
     const YOcc yo = y_occ(E, rp.chempot, kB * rp.T);   // also e^-x of the Fermi factors
@@ -1433,8 +1455,8 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
         for (int c = 0; c < NW; c += 4) {
-          const float4 xr = __ldg((const float4 *)(rr + c + NW * s));
-          const float4 xi = __ldg((const float4 *)(ri + c + NW * s));
+          const float4 xr = __ldg((const float4 *)(rr + 32 * (c + NW * s)));
+          const float4 xi = __ldg((const float4 *)(ri + 32 * (c + NW * s)));
           cfmaf_cj(a, uk[c], make_float2(xr.x, xi.x));
           cfmaf_cj(a, uk[c + 1], make_float2(xr.y, xi.y));
           cfmaf_cj(a, uk[c + 2], make_float2(xr.z, xi.z));
@@ -2638,16 +2660,18 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
   const RateParams &rp0 = rp;
   double *const partial0 = partial;
   const EpiData eds = ed, eds_in = ed_in;
+  // the row epilogue reads the GEMM output interleaved by 32 rows (coalesced), the others row-major
+  const bool rows_kernel = rp.delta_kind == 0 && nb <= EPR_NB && (nw == 8 || nw == 16 || nw == 24 || nw == 32);
   for (int64_t j0 = 0; j0 < nst; j0 += sc) {
     const int ns = (int)std::min<int64_t>(sc, nst - j0);
     const int Npc = (int)rup((int64_t)ns * ncol, BN);
     tB->begin(st);
     if (j0 > 0) yield();
-    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st, chunk_us, yield, bm)))
+    if ((rc = cgemm(PB, MpB, 0, MpB, B2, Np2, j0 * ncol, Npc, KpB, CBr, CBi, NpC, err, st, chunk_us, yield, bm,
+                    rows_kernel ? 1 : 0)))
       return rc;
     tB->end(st);
     const size_t esm = (size_t)2 * EPI_ROWS * (ncol + 1) * sizeof(float);
-    const bool rows_kernel = rp.delta_kind == 0 && nb <= EPR_NB && (nw == 8 || nw == 16 || nw == 24 || nw == 32);
     for (int set = 0; set < nsets; ++set) {   // one epilogue per parameter set over the same GEMM output
     const RateParams &rp = set ? sets->rp[set] : rp0;
     const QTab &qt = qts[set];
