@@ -1404,8 +1404,8 @@ __global__ void __launch_bounds__(EPI_ROWS) k_epilogue_split2(int nwv, int j0, i
 // at compile time (the band and mode arrays then live in registers), nb <= EPR_NB.
 constexpr int EPR_NB = 18;
 
-template <int NW>
-__global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, const float *Cr, const float *Ci,
+template <int NW, int NB>
+__global__ void __launch_bounds__(EPI_ROWS, NW * NB <= 96 ? 4 : 3) k_epilogue_rows(int nwv, int j0, const float *Cr, const float *Ci,
                                                             int64_t ldc, RateParams rp, EpiData d, QTab qt,
                                                             double *partial, int nblk) {
   static_assert(NW % 4 == 0, "16-byte row loads");
@@ -1448,9 +1448,9 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
 #pragma unroll
         for (int c = 0; c < NW; ++c) cfmaf_cj(unm, uk[c], Uk[c]);
       }
-      float2 h[EPR_NB];
+      float2 h[NB];
 #pragma unroll
-      for (int s = 0; s < EPR_NB; ++s) {
+      for (int s = 0; s < NB; ++s) {
         if (s >= nb) break;
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
@@ -1466,13 +1466,13 @@ __global__ void __launch_bounds__(EPI_ROWS, 3) k_epilogue_rows(int nwv, int j0, 
       }
       const F2 dn = f2_of((E - eps) * inv_sig);
 #pragma unroll
-      for (int s = 0; s < EPR_NB; ++s) {
+      for (int s = 0; s < NB; ++s) {
         if (s >= nb) break;
         const int qs = q * nb + s;
         const float2 *u = d.uf + (size_t)qs * nb;
         float2 g = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int sp = 0; sp < EPR_NB; ++sp)
+        for (int sp = 0; sp < NB; ++sp)
           if (sp < nb) cfmaf(g, u[sp], h[sp]);
         if (d.glpf) cfmaf(g, d.glpf[qs], unm);   // long-range term (wannier.f90:998-1006)
         const float g2c = (g.x * g.x + g.y * g.y) * qt.cx[qs];
@@ -2684,14 +2684,23 @@ static int split_rates_generic(SplitOperands &s, Workspace &ws, cudaStream_t st,
     }
     if (rows_kernel) {
       dim3 grid(nblk, ns);
+      // NB: the mode arrays' size (6, 12 or 18), the smallest that holds nb
+      auto rows = [&](auto kernel) {
+        kernel<<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+      };
+      const int nbc = nb <= 6 ? 6 : nb <= 12 ? 12 : 18;
+#define EPHG_ROWS_NB(NWV)                                                          \
+  (nbc == 6 ? rows(k_epilogue_rows<NWV, 6>) : nbc == 12 ? rows(k_epilogue_rows<NWV, 12>) \
+            : rows(k_epilogue_rows<NWV, 18>))
       if (nw == 8)
-        k_epilogue_rows<8><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+        EPHG_ROWS_NB(8);
       else if (nw == 16)
-        k_epilogue_rows<16><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+        EPHG_ROWS_NB(16);
       else if (nw == 24)
-        k_epilogue_rows<24><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+        EPHG_ROWS_NB(24);
       else
-        k_epilogue_rows<32><<<grid, EPI_ROWS, 0, st>>>(nwv, (int)j0, CBr, CBi, NpC, rp, ed, qt, partial, nblk);
+        EPHG_ROWS_NB(32);
+#undef EPHG_ROWS_NB
       TCK(cudaGetLastError());
     } else if (rp.delta_kind == 0 && esm > 200 * 1024) {
       dim3 grid(nblk, ns);
