@@ -3,7 +3,7 @@
 Tolerances (split form): GEMM normwise relative error <= 1e-5 against the
 complex128 product (FP32 accumulation over K ~ 300 complex terms dominates:
 sqrt(6K) * 2^-24 ~ 2.5e-6 typical); |g|^2 per vertex |a-b| <= 1e-5 |b| + 1e-6 max|b|; RTA rates
-<= 1e-6 relative per state (the benchmark spec's split-form bound).
+<= 1e-6 relative per state (the split form's stated bound).
 """
 import ctypes as ct
 
