@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -119,12 +120,43 @@ int ephg::api_check_err(ephg_handle *h) {
 // workspace failures carry their own message
 #define WSFAIL(rc) fail((rc), "%s", h->ws.msg.c_str())
 
+// Small host arrays (tables built on the host, caller arrays of a few MB) reach
+// the device through one pinned staging buffer of the library instead of the
+// driver's staging of pageable memory, whose occasional page pinning cost
+// handle creation ~15 ms every few calls.  Arrays above kStageMax are copied
+// directly (the caller's pinned arrays stay asynchronous).
+constexpr size_t kStageMax = (size_t)64 << 20;
+static int staged_copy(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static void *stage = nullptr;
+  static size_t cap = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (cap < bytes) {
+    if (stage) cudaFreeHost(stage);
+    stage = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, (size_t)8 << 20);
+    if (cudaMallocHost(&stage, want) != cudaSuccess) {
+      cudaGetLastError();
+      stage = nullptr;
+      CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));   // no pinned memory: the plain path
+      return EPHG_OK;
+    }
+    cap = want;
+  }
+  memcpy(stage, src, bytes);
+  CK(cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));   // the staging buffer is free again for the next copy
+  return EPHG_OK;
+}
+
 template <typename T>
 // n elements from the library pool on st, copied from src; the bytes are added to *acc
 static int upload(T **dst, const T *src, size_t n, cudaStream_t st, int64_t *acc = nullptr) {
   const size_t b = std::max<size_t>(n, 1) * sizeof(T);
   CK(pool_alloc((void **)dst, b, st));
   if (acc) *acc += (int64_t)b;
+  if (n && n * sizeof(T) <= kStageMax) return staged_copy(*dst, src, n * sizeof(T), st);
   if (n) CK(cudaMemcpyAsync(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
   return EPHG_OK;
 }
