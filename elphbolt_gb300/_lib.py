@@ -35,7 +35,7 @@ EXPORTS = ["ephg_create", "ephg_destroy", "ephg_last_error", "ephg_device_count"
            "ephg_server_create", "ephg_server_destroy", "ephg_submit", "ephg_poll", "ephg_wait",
            "ephg_server_stats_get", "ephg_el_wann_noalloc", "ephg_ph_rates", "ephg_set_polar",
            "ephg_crystal_symmetry", "ephg_set_symmetry", "ephg_irred_wedge", "ephg_el_rates_batch",
-           "ephg_g2_average_degenerate", "ephg_el_rates_sets", "ephg_server_set_merge"]
+           "ephg_g2_average_degenerate", "ephg_el_rates_sets", "ephg_server_set_merge", "ephg_trim_memory"]
 
 TICKET_QUEUED, TICKET_RUNNING, TICKET_DONE, TICKET_FAILED = 0, 1, 2, 3
 DEGAVG_REFERENCE, DEGAVG_MEAN = 0, 1
@@ -144,6 +144,7 @@ def load(path: str = LIB_PATH):
                                       ct.POINTER(c_i64p), ct.POINTER(RateStats), ct.POINTER(ct.c_int),
                                       ct.POINTER(BatchOpts), ct.POINTER(BatchStats)]
     L.ephg_server_set_merge.argtypes = [vp, ct.c_int]
+    L.ephg_trim_memory.argtypes = []
     L.ephg_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_int64, ct.c_int, ct.POINTER(vp)]
     L.ephg_server_destroy.argtypes = [vp]
     L.ephg_submit.argtypes = [vp, ct.c_int, ct.POINTER(RateRequest), c_i64p]

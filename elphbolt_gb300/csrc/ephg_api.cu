@@ -174,6 +174,16 @@ int ephg_device_count(void) {
   return n;
 }
 
+int ephg_trim_memory(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(EPHG_ERR_CUDA, "trim_memory: no device");
+  cudaMemPool_t pool = lib_pool(dev);
+  if (!pool) return fail(EPHG_ERR_CUDA, "trim_memory: no memory pool");
+  CK(cudaDeviceSynchronize());   // frees still queued on streams reach the pool first
+  CK(cudaMemPoolTrimTo(pool, 0));
+  return EPHG_OK;
+}
+
 int ephg_destroy(ephg_handle *h) {
   if (!h) return EPHG_OK;
   void *ptrs[] = {h->Rk, h->Rq, h->Rg, h->degk, h->degq, h->degg, h->Hext, h->Hbox, h->Dbox, h->graw, h->G64,

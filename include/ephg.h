@@ -108,6 +108,12 @@ int ephg_destroy(ephg_handle *h);
 const char *ephg_last_error(void);
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int ephg_device_count(void);
+/* The library keeps device memory freed by ephg_destroy and by released
+ * workspaces mapped in a pool of its own (up to half the device), so that the
+ * next handle or request reuses it at no cost.  This returns the pool's unused
+ * memory on the current device to the driver, for a caller that needs it for
+ * other allocations; memory of live handles is untouched. */
+int ephg_trim_memory(void);
 
 /* The crystal fields of a polar crystal (crys%polar = .true.; crystal.f90:45-49):
  * epsilon (3,3) the high-frequency dielectric tensor and born (3,3,numatoms)

@@ -91,6 +91,11 @@ module ephg_c
        import :: c_int
      end function ephg_device_count
 
+     integer(c_int) function ephg_trim_memory() bind(C, name="ephg_trim_memory")
+       !! return the library pool's unused device memory to the driver
+       import :: c_int
+     end function ephg_trim_memory
+
      integer(c_int) function ephg_set_polar(h, epsilon, born) bind(C, name="ephg_set_polar")
        import :: c_int, c_ptr
        type(c_ptr), value :: h, epsilon, born
